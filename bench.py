@@ -1,0 +1,401 @@
+#!/usr/bin/env python
+"""Benchmark: ms per solve to 1e-10 relative residual on one GB300.
+
+Workload (the reference's configuration 2): 4096^2 vertex-centred 2D
+9-point masked Laplacian, F-cycle, 10 levels, Jacobi 3/3 (omega 0.8),
+smoothed-noise coastline with 30 % land, N(0,1) right-hand side with the wet
+mean removed (tests/workloads.py). One step = one solve from x = 0 to
+||r||_2/||b||_2 <= 1e-10. `value` is the mixed-precision form (FP32 cycles
+inside FP64 defect correction); the plain FP64 drop-in is timed beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+The reference arm (--impl reference) times the CPU restatement of the
+reference (oracle/, OpenMP over all host cores; the Julia reference cannot
+run on this machine) on the same workload and prints the same JSON line.
+With N > 1 (torchrun), every rank solves its own replica (replicas only:
+the path has no data exchange between independent solves).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "cfmultigrid.jl_gb300"), os.path.join(ROOT, "tests")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "ms/solve to 1e-10 rel residual (mixed FP32-in-FP64), 4096^2 vertex 9-point F-cycle"
+UNIT = "ms/solve"
+TOL = 1e-10
+MAXITE = 60
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=4096, help="grid size (4096 = the configuration)")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the single-thread CPU sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------ distributed
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v: float, world: int) -> float:
+    """Max of a float over all ranks (identity when world == 1)."""
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ clocks
+class Clocks:
+    """nvidia-smi sampling of SM clock and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        if self.path and os.path.exists(self.path):
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------- our arm
+def make_gmg(cfmg, param, vmsk, noise, precision, stream_ptr):
+    import workloads as W
+
+    p = cfmg.Param(**param, tol=TOL, maxite=MAXITE, residual_norm="l2", precision=precision, verbose=False)
+    mg = cfmg.get_gmg(p)
+    mg.set_stream(stream_ptr)
+    mg.data[1].msk = vmsk
+    cfmg.setup_operators(mg)
+    for lev in range(1, mg.nlevels + 1):
+        for f in ("b", "x", "y", "r"):
+            cfmg.set_to_zero(mg, lev, f)
+    b = W.rhs(noise, mg.download(1, "msk"))
+    mg.data[1].b = b
+    return mg, b
+
+
+def launch_count(cfmg, mg):
+    import ctypes
+
+    n = ctypes.c_longlong()
+    mg._check(mg._L.cfmg_launch_count(mg.handle, ctypes.byref(n)))
+    return n.value
+
+
+def profile(cfmg, mg, cls, lev, precision, fn):
+    import ctypes
+
+    L = mg._L
+    mg._check(L.cfmg_profile(mg.handle, cfmg._lib.KERNEL_CLASSES[cls], lev, cfmg._lib.PRECISIONS[precision]))
+    fn()
+    n = ctypes.c_longlong()
+    ms = ctypes.c_double()
+    mg._check(L.cfmg_profile_read(mg.handle, ctypes.byref(n), ctypes.byref(ms)))
+    mg._check(L.cfmg_profile(mg.handle, -1, 0, 0))
+    return n.value, ms.value
+
+
+def run_ours(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    import cfmg
+    import workloads as W
+
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    param, vmsk, noise = W.config2(args.n)
+    mgm, b = make_gmg(cfmg, param, vmsk, noise, "mixed", sp)
+    mgd, _ = make_gmg(cfmg, param, vmsk, noise, "fp64", sp)
+    level_cells = [g.tx * g.ty * g.tz for g in mgm.levels]
+
+    def solve(mg):
+        cfmg.set_to_zero(mg, 1, "x")
+        return cfmg.solve(mg)
+
+    # warm-up (graph capture happens in the first solve)
+    for _ in range(max(args.warmup, 3)):
+        res_m, nit_m = solve(mgm)
+    barrier(world)
+    torch.cuda.synchronize()
+    n0 = launch_count(cfmg, mgm)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            res_m, nit_m = solve(mgm)
+        e1.record(stream)
+        e1.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    ms_mixed = e0.elapsed_time(e1) / args.steps
+    launches = launch_count(cfmg, mgm) - n0
+    clocks = clk.summary()
+    x_mixed = mgm.download(1, "x")
+
+    # plain FP64 drop-in, same workload
+    res_d, nit_d = solve(mgd)
+    k64 = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(k64):
+        res_d, nit_d = solve(mgd)
+    e1.record(stream)
+    e1.synchronize()
+    ms_fp64 = e0.elapsed_time(e1) / k64
+    x_fp64 = mgd.download(1, "x")
+    wet = mgm.download(1, "msk").astype(bool)
+    err = float(np.linalg.norm((x_mixed - x_fp64)[wet]) / np.linalg.norm(x_fp64[wet]))
+
+    # end to end through the C ABI with host buffers: b in from pinned host
+    # memory, solve, x out to pinned host memory, every step
+    hb = torch.from_numpy(np.ascontiguousarray(b.ravel(order="F"))).pin_memory()
+    hx = torch.empty_like(hb).pin_memory()
+    nbytes = hb.numel() * 8
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(args.steps):
+        mgm.upload_ptr(1, "b", hb.data_ptr())
+        cfmg.set_to_zero(mgm, 1, "x")
+        cfmg.solve(mgm)
+        mgm.download_ptr(1, "x", hx.data_ptr())
+    e1.record(stream)
+    e1.synchronize()
+    wall_e2e = (time.perf_counter() - t0) * 1e3 / args.steps
+    ms_e2e = e0.elapsed_time(e1) / args.steps
+
+    # roofline: level-1 FP32 sweep of the mixed form, timed per launch with
+    # CUDA events on the library's stream during one solve
+    nl, tl = profile(cfmg, mgm, "sweep", 1, "mixed", lambda: solve(mgm))
+    g1 = mgm.levels[1]
+    sweep_cells = (g1.nx + 2) * (g1.ny + 2) * g1.nz  # the 9-point sweep ranges average ~ (n+1)^2; see the design doc
+    bytes_per_launch = 16.0 * sweep_cells  # x, b, omega*idiag read + y written, FP32
+    ms_launch = tl / max(nl, 1)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = bytes_per_launch / (ms_launch * 1e-3) / 1e9 if ms_launch > 0 else 0.0
+    # FP64 sweep of the drop-in: FP64-issue bound, reported beside it
+    nl64, tl64 = profile(cfmg, mgd, "sweep", 1, "fp64", lambda: solve(mgd))
+    ms_launch64 = tl64 / max(nl64, 1)
+    ach64 = 32.0 * sweep_cells / (ms_launch64 * 1e-3) / 1e9 if ms_launch64 > 0 else 0.0
+
+    ms_mixed = max_over_ranks(ms_mixed, world)
+    ms_e2e = max_over_ranks(ms_e2e, world)
+    out = {
+        "metric": METRIC, "value": ms_mixed / world, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32-in-f64", "data": "synthetic (seeded coastline mask, N(0,1) rhs)",
+        "config": {"workload": f"config2: {args.n}^2 vertex-centred 2D 9-point masked Laplacian, F-cycle, "
+                               f"10 levels, Jacobi 3/3, omega 0.8, 30% land",
+                   "levels": mgm.nlevels, "fine_cells": level_cells[0], "tol_l2": TOL,
+                   "l2_flush": "inputs larger than L2 (level-1 FP64 field = %.0f MB)" % (level_cells[0] * 8 / 1e6),
+                   "parallelism": f"replicas x{world}"},
+        "cycles_mixed": nit_m, "res_mixed": res_m, "cycles_fp64": nit_d, "res_fp64": res_d,
+        "ms_per_solve_fp64": ms_fp64, "mixed_speedup_vs_fp64": ms_fp64 / ms_mixed,
+        "mixed_rel_err_vs_fp64": err,
+        "e2e": {"value": ms_e2e / world, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                "wall_ms_per_step": wall_e2e},
+        "gpu_launches": launches,
+        "roofline": {"kernel": "FP32 9-point Jacobi sweep, level 1 (mixed form)", "bound": "hbm",
+                     "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                     "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)", "traffic": None,
+                     "launches_timed": nl, "ms_per_launch": ms_launch, "bytes_per_launch": bytes_per_launch},
+        "roofline_fp64_sweep": {"kernel": "FP64 9-point Jacobi sweep, level 1 (drop-in)", "ms_per_launch": ms_launch64,
+                                "effective_gbs": ach64, "bound": "fp64 issue (DADD/DMUL at 506 Gop/s measured)"},
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(param, vmsk, noise, nit_d, args.cpu_seconds)
+    return out
+
+
+# -------------------------------------------------------------- CPU side
+def _oracle_setup(param, vmsk, noise):
+    import oracle as O
+    import workloads as W
+
+    p = dict(param, tol=TOL, maxite=MAXITE)
+    og = O.OracleGmg(p)
+    og.field(1, "msk")[...] = vmsk
+    og.setup_operators()
+    for lev in range(1, og.nlevels + 1):
+        for f in ("x", "y", "r", "b"):
+            og.field(lev, f)[...] = 0.0
+    og.field(1, "b")[...] = W.rhs(noise, og.field(1, "msk"))
+    return og
+
+
+def cpu_baseline(param, vmsk, noise, cycles_needed, budget_s):
+    """The single-thread oracle (the reference's PlainCPU arithmetic) on a
+    bounded sample: full-size F-cycles + residual norms until the budget is
+    spent, scaled to one solve of `cycles_needed` cycles."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    os.environ["CFMG_ORACLE_THREADS"] = "1"
+    og = _oracle_setup(param, vmsk, noise)
+    t0 = time.perf_counter()
+    normb = og.norm(1, "b")
+    og.normresidual(normb)
+    t_head = time.perf_counter() - t0
+    times = []
+    while len(times) < cycles_needed and sum(times) < budget_s:
+        t = time.perf_counter()
+        og.cycle("f")
+        og.normresidual(normb)
+        times.append(time.perf_counter() - t)
+    per = sum(times) / len(times)
+    ms = (t_head + per * cycles_needed) * 1e3
+    return {"value": ms, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{len(times)} of {cycles_needed} full-size F-cycles (+ residual norm) timed, "
+                      f"scaled to one solve; single thread, FP64, oracle restatement of the reference"}
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the CPU restatement (OpenMP, all host cores), full
+    solves of the same workload to the same tolerance."""
+    if rank != 0:
+        return None
+    cores = os.cpu_count() or 1
+    os.environ["CFMG_ORACLE_THREADS"] = str(cores)
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import workloads as W
+
+    param, vmsk, noise = W.config2(args.n)
+    og = _oracle_setup(param, vmsk, noise)
+
+    def one():
+        og.field(1, "x")[...] = 0.0
+        t = time.perf_counter()
+        r = solve_l2(og)
+        return time.perf_counter() - t, r
+
+    for _ in range(args.warmup):
+        one()
+    ts = []
+    for _ in range(args.steps):
+        dt, (res, nite) = one()
+        ts.append(dt)
+    ms = sum(ts) / len(ts) * 1e3
+    return {"metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded coastline mask, N(0,1) rhs)",
+            "impl": "reference",
+            "config": {"workload": f"config2: {args.n}^2 vertex-centred 2D 9-point masked Laplacian, F-cycle, "
+                                   f"10 levels, Jacobi 3/3, omega 0.8, 30% land", "tol_l2": TOL,
+                       "cycles": nite, "res": res},
+            "cpu_baseline": {"value": ms, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "full FP64 solves with the oracle restatement of the reference "
+                                       f"(OpenMP, {cores} threads); Julia is not installed on this box"},
+            "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def solve_l2(og):
+    """solve! with the ||r||/||b|| <= TOL rule (the reference's loop,
+    src/gmg_solver.jl:9-42, on the square root of its ratio)."""
+    normb = og.norm(1, "b")
+    res = og.normresidual(normb) ** 0.5
+    nite = 0
+    while res > TOL and nite < MAXITE:
+        nite += 1
+        og.cycle("f")
+        res = og.normresidual(normb) ** 0.5
+    return res, nite
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_init()
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        out = run_ours(args, rank, world, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

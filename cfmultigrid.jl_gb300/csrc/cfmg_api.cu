@@ -1,0 +1,1059 @@
+// libcfmg host runtime: handle, level hierarchy, operator dispatch, cycles
+// and the solve loop, behind the C ABI of include/cfmg.h.
+//
+// Structure mirrors the reference's Gmg object (src/gmg_types.jl:121-132):
+// a handle owns the levels, and every operator is dispatched on
+// (case, operator, location) exactly as allocate_mg binds the function
+// tables (src/gmg_setup.jl:86-101,124-157). There is no CPU fallback:
+// every operator is a CUDA kernel launch on the handle's stream.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "cfmg_internal.h"
+
+using namespace cfmg;
+
+// ------------------------------------------------------------------ handle
+struct cfmg_handle {
+  cfmg_desc d;
+  std::vector<Level> lv;  // lv[0] is level 1
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+  double* partials = nullptr;  // kNormParts FP64 partial sums
+  double* dscal = nullptr;     // device scalars, see enum Scal
+  double* hscal = nullptr;     // pinned host mirror of dscal
+  std::string err;
+  bool mixed_dirty = true;     // FP32 coefficient copies need refreshing
+  // captured graphs: one cycle + normresidual per cycle kind and precision
+  cudaGraphExec_t graph[2][6] = {{nullptr}};
+  long long graph_launches[2][6] = {{0}};
+  long long launches = 0;      // kernels launched (graph replays count every kernel node)
+  bool capturing = false;
+  // device-time profile of one kernel class on one level (cfmg_profile)
+  int prof_cls = -1, prof_lev = 0, prof_prec = 0;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pending;
+  long long prof_launches = 0;
+  double prof_ms = 0.0;
+};
+
+enum Scal { S_NORM = 0, S_RES = 1, S_NORMB = 2, S_NWET = 3, S_SCALE = 4, S_MEAN = 5, S_TMP0 = 6, S_ISCALE = 7,
+            S_COUNT = 16 };
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_create_err;
+
+int fail(cfmg_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  else {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_create_err = msg;
+  }
+  return code;
+}
+
+#define CUDA_OK(h, call)                                                                       \
+  do {                                                                                         \
+    cudaError_t _e = (call);                                                                   \
+    if (_e != cudaSuccess)                                                                     \
+      return fail((h), CFMG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e));     \
+  } while (0)
+
+#define LAUNCH_OK(h)                                                                           \
+  do {                                                                                         \
+    cudaError_t _e = cudaGetLastError();                                                       \
+    if (_e != cudaSuccess) return fail((h), CFMG_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(_e)); \
+  } while (0)
+
+#define TRY(expr)              \
+  do {                         \
+    int _rc = (expr);          \
+    if (_rc != CFMG_OK) return _rc; \
+  } while (0)
+
+bool threed(const cfmg_handle* h) { return h->d.kase == CFMG_THREED; }
+bool vertices(const cfmg_handle* h) { return h->d.location == CFMG_VERTICES; }
+bool xperio(const cfmg_handle* h) { return h->d.topology == CFMG_XPERIO; }
+int L(const cfmg_handle* h) { return (int)h->lv.size(); }
+
+Box interior(const Level& l) { return Box{l.ic0, l.ic1, l.jc0, l.jc1, l.kc0, l.kc1}; }
+
+int harvest(cfmg_handle* h) {
+  for (auto& pr : h->ev_pending) {
+    float ms = 0.f;
+    CUDA_OK(h, cudaEventElapsedTime(&ms, pr.first, pr.second));
+    h->prof_ms += ms;
+    h->prof_launches += 1;
+    h->ev_pool.push_back(pr.first);
+    h->ev_pool.push_back(pr.second);
+  }
+  h->ev_pending.clear();
+  return CFMG_OK;
+}
+
+int sync(cfmg_handle* h) {
+  CUDA_OK(h, cudaStreamSynchronize(h->stream));
+  return harvest(h);
+}
+
+// Kernel accounting and the optional per-class event profile. Every launch
+// of the runtime goes through Launch: it counts the kernel and, when the
+// profiled (class, level, precision) matches, brackets it with events.
+struct Launch {
+  cfmg_handle* h;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  Launch(cfmg_handle* hh, int cls, int lev, int prec, int nkernels = 1) : h(hh) {
+    h->launches += nkernels;
+    if (h->prof_cls == cls && h->prof_lev == lev && h->prof_prec == prec && !h->capturing) {
+      for (cudaEvent_t* e : {&e0, &e1}) {
+        if (h->ev_pool.empty()) {
+          cudaEvent_t ev;
+          cudaEventCreate(&ev);
+          h->ev_pool.push_back(ev);
+        }
+        *e = h->ev_pool.back();
+        h->ev_pool.pop_back();
+      }
+      cudaEventRecord(e0, h->stream);
+    }
+  }
+  ~Launch() {
+    if (e0) {
+      cudaEventRecord(e1, h->stream);
+      h->ev_pending.emplace_back(e0, e1);
+    }
+  }
+};
+
+template <class T>
+constexpr int prec_of() {
+  return sizeof(T) == 8 ? CFMG_FP64 : CFMG_MIXED;
+}
+
+// Typed view of one level's arrays (FP64 drop-in or FP32 cycles).
+template <class T>
+struct View {
+  T *x, *y, *r, *b;
+  const T *diag, *widiag, *Rcoef, *Pcoef, *cE, *cN;
+  const uint8_t* msk;
+};
+template <class T>
+View<T> view(const Level& l);
+template <>
+View<double> view<double>(const Level& l) {
+  return View<double>{l.x, l.y, l.r, l.b, l.diag, l.widiag, l.Rcoef, l.Pcoef, l.cE, l.cN, l.msk};
+}
+template <>
+View<float> view<float>(const Level& l) {
+  return View<float>{l.x32, l.y32, l.r32, l.b32, l.diag32, l.widiag32, l.Rcoef32, l.Pcoef32, l.cE32, l.cN32, l.msk};
+}
+
+template <class T>
+T* field_ptr(const Level& l, int f) {
+  View<T> v = view<T>(l);
+  switch (f) {
+    case CFMG_X: return v.x;
+    case CFMG_R: return v.r;
+    case CFMG_B: return v.b;
+    case CFMG_Y: return v.y;
+    default: return nullptr;
+  }
+}
+
+template <class T>
+void fill_if(cfmg_handle* h, int lev, T* x) {
+  if (!xperio(h)) return;
+  Launch k(h, CFMG_K_FILL, lev, prec_of<T>());
+  launch_fill_xperio<T>(x, geom(h->lv[lev - 1]), h->stream);
+}
+
+// ------------------------------------------------------- per-level operators
+// mg.smoother[lev] (src/gmg_setup.jl:124-139 selects among these)
+template <class T>
+int smooth_t(cfmg_handle* h, int lev, int nite) {
+  const Level& l = h->lv[lev - 1];
+  View<T> v = view<T>(l);
+  const Geom g = geom(l);
+  const T cff = (T)(1.0 - h->d.omega);
+  cudaStream_t s = h->stream;
+  if (h->d.op == CFMG_LAPLACIAN9 && threed(h)) {
+    // smooth_laplacian9! (src/laplacian9.jl:2-47): one pair whatever nite
+    // is; sweep 1 over icp x jcp x kcp, sweep 2 over the interior; no fill!
+    Box ext{l.nh, l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, l.nh, l.nz + l.nh + 1};
+    { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep19_3d<T>(v.x, v.y, v.b, v.widiag, cff, g, ext, s); }
+    { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep19_3d<T>(v.y, v.x, v.b, v.widiag, cff, g, interior(l), s); }
+    LAUNCH_OK(h);
+    return CFMG_OK;
+  }
+  for (int kt = 0; kt < nite; ++kt) {
+    if (h->d.op == CFMG_LAPLACIAN9) {  // 2D 9-point extension
+      Box ext{l.nh, l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, 1, l.nz};
+      { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep9_2d<T>(v.x, v.y, v.b, v.widiag, cff, g, ext, s); }
+      { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep9_2d<T>(v.y, v.x, v.b, v.widiag, cff, g, interior(l), s); }
+    } else if (h->d.op == CFMG_VARCOEF) {
+      { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep_vc_2d<T>(v.x, v.y, v.b, v.widiag, v.cE, v.cN, cff, g, s); }
+      { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep_vc_2d<T>(v.y, v.x, v.b, v.widiag, v.cE, v.cN, cff, g, s); }
+    } else if (threed(h)) {  // smooth_laplacian! (src/laplacian.jl:24-41)
+      { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep7_3d<T>(v.x, v.y, v.b, v.widiag, cff, g, s); }
+      { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep7_3d<T>(v.y, v.x, v.b, v.widiag, cff, g, s); }
+    } else {  // smooth_laplacian2d! (src/laplacian.jl:95-112)
+      { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep5_2d<T>(v.x, v.y, v.b, v.widiag, cff, g, s); }
+      { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep5_2d<T>(v.y, v.x, v.b, v.widiag, cff, g, s); }
+    }
+    fill_if<T>(h, lev, v.x);
+  }
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
+// mg.residual[lev]
+template <class T>
+int residual_t(cfmg_handle* h, int lev) {
+  const Level& l = h->lv[lev - 1];
+  View<T> v = view<T>(l);
+  const Geom g = geom(l);
+  cudaStream_t s = h->stream;
+  if (h->d.op == CFMG_LAPLACIAN9 && threed(h)) {  // residual_laplacian9!: interior, no fill!
+    { Launch k(h, CFMG_K_RESIDUAL, lev, prec_of<T>()); launch_resid19_3d<T>(v.r, v.x, v.b, v.diag, v.msk, g, interior(l), s); }
+    LAUNCH_OK(h);
+    return CFMG_OK;
+  }
+  if (h->d.op == CFMG_LAPLACIAN9) { Launch k(h, CFMG_K_RESIDUAL, lev, prec_of<T>()); launch_resid9_2d<T>(v.r, v.x, v.b, v.diag, v.msk, g, interior(l), s); }
+  else if (h->d.op == CFMG_VARCOEF) { Launch k(h, CFMG_K_RESIDUAL, lev, prec_of<T>()); launch_resid_vc_2d<T>(v.r, v.x, v.b, v.diag, v.cE, v.cN, v.msk, g, s); }
+  else if (threed(h)) { Launch k(h, CFMG_K_RESIDUAL, lev, prec_of<T>()); launch_resid7_3d<T>(v.r, v.x, v.b, v.diag, v.msk, g, interior(l), s); }
+  else { Launch k(h, CFMG_K_RESIDUAL, lev, prec_of<T>()); launch_resid5_2d<T>(v.r, v.x, v.b, v.diag, v.msk, g, s); }
+  fill_if<T>(h, lev, v.r);
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
+int rp_kind(const cfmg_handle* h) { return (vertices(h) ? 2 : 0) + (threed(h) ? 1 : 0); }
+
+// mg.restriction[lev]: field of lev -> b of lev+1, then fill!
+template <class T>
+int restrict_t(cfmg_handle* h, int lev, int field) {
+  const Level& f = h->lv[lev - 1];
+  const Level& c = h->lv[lev];
+  View<T> vc = view<T>(c);
+  const T* src = field_ptr<T>(f, field);
+  {
+    Launch k(h, CFMG_K_RESTRICT, lev, prec_of<T>());
+    launch_restrict<T>(rp_kind(h), src, vc.b, vc.Rcoef, geom(f), geom(c), interior(c), h->stream);
+  }
+  fill_if<T>(h, lev + 1, vc.b);
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
+// mg.prolongation[lev]: x of lev += Pcoef * P(x of lev+1), then fill!
+template <class T>
+int prolong_t(cfmg_handle* h, int lev) {
+  const Level& f = h->lv[lev - 1];
+  const Level& c = h->lv[lev];
+  View<T> vf = view<T>(f);
+  View<T> vc = view<T>(c);
+  {
+    Launch k(h, CFMG_K_PROLONG, lev, prec_of<T>());
+    launch_prolong<T>(rp_kind(h), vf.x, vc.x, vf.Pcoef, geom(f), geom(c), f.nx, f.ny, f.nz, f.kc0, f.kc1, h->stream);
+  }
+  fill_if<T>(h, lev, vf.x);
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
+template <class T>
+int zero_t(cfmg_handle* h, int lev, int field) {
+  const Level& l = h->lv[lev - 1];
+  T* p = field_ptr<T>(l, field);
+  CUDA_OK(h, cudaMemsetAsync(p, 0, l.len * sizeof(T), h->stream));
+  return CFMG_OK;
+}
+
+// Mixed form: the coarsest level is solved in FP64 (FP32 b -> FP64 b,
+// ndeepest FP64 pairs, FP64 x -> FP32 x).
+__global__ void k_f32_to_f64(const float* a, double* out, long long n) {
+  long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I < n) out[I] = (double)a[I];
+}
+__global__ void k_f64_to_f32(const double* a, float* out, long long n) {
+  long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I < n) out[I] = (float)a[I];
+}
+
+template <class T>
+int coarsest_t(cfmg_handle* h, int nite);
+template <>
+int coarsest_t<double>(cfmg_handle* h, int nite) {
+  return smooth_t<double>(h, L(h), nite);
+}
+template <>
+int coarsest_t<float>(cfmg_handle* h, int nite) {
+  if (L(h) == 1) return smooth_t<float>(h, 1, nite);
+  const Level& c = h->lv[L(h) - 1];
+  long long n = (long long)c.len;
+  unsigned nb = (unsigned)((n + 255) / 256);
+  {
+    Launch k(h, CFMG_K_CONVERT, L(h), CFMG_MIXED, 2);
+    k_f32_to_f64<<<nb, 256, 0, h->stream>>>(c.b32, c.b, n);
+    k_f32_to_f64<<<nb, 256, 0, h->stream>>>(c.x32, c.x, n);
+  }
+  TRY(smooth_t<double>(h, L(h), nite));
+  {
+    Launch k(h, CFMG_K_CONVERT, L(h), CFMG_MIXED);
+    k_f64_to_f32<<<nb, 256, 0, h->stream>>>(c.x, c.x32, n);
+  }
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
+// ------------------------------------------------------------------ cycles
+// vcycle! (src/gmg_cycles.jl:67-83)
+template <class T>
+int vcycle_t(cfmg_handle* h, int lev0) {
+  const cfmg_desc& d = h->d;
+  const int nl = L(h);
+  for (int lev = lev0; lev <= nl - 1; ++lev) {
+    TRY(smooth_t<T>(h, lev, d.npre));
+    TRY(residual_t<T>(h, lev));
+    TRY(restrict_t<T>(h, lev, CFMG_R));
+    TRY(zero_t<T>(h, lev + 1, CFMG_X));
+  }
+  TRY(coarsest_t<T>(h, d.ndeepest));
+  for (int lev = nl - 1; lev >= lev0; --lev) {
+    TRY(prolong_t<T>(h, lev));
+    TRY(smooth_t<T>(h, lev, d.npost));
+  }
+  return CFMG_OK;
+}
+
+// fcycle! (src/gmg_cycles.jl:85-100)
+template <class T>
+int fcycle_t(cfmg_handle* h) {
+  const int nl = L(h);
+  for (int lev = 1; lev <= nl - 1; ++lev) {
+    TRY(restrict_t<T>(h, lev, lev > 1 ? CFMG_B : CFMG_R));
+    TRY(zero_t<T>(h, lev + 1, CFMG_X));
+  }
+  TRY(coarsest_t<T>(h, h->d.ndeepest));
+  for (int lev = nl - 1; lev >= 1; --lev) {
+    TRY(prolong_t<T>(h, lev));
+    TRY(vcycle_t<T>(h, lev));
+  }
+  return CFMG_OK;
+}
+
+template <class T>
+int cycle_t(cfmg_handle* h, int kind) {
+  const cfmg_desc& d = h->d;
+  switch (kind) {
+    case CFMG_CYCLE_V:
+    case CFMG_CYCLE_VREC:  // vcycle_recursive! is vcycle! when not verbose (src/gmg_cycles.jl:43-66)
+      return vcycle_t<T>(h, 1);
+    case CFMG_CYCLE_F:
+      return fcycle_t<T>(h);
+    case CFMG_CYCLE_ONELEV:  // onelevel! (src/gmg_cycles.jl:3-6)
+      return smooth_t<T>(h, 1, d.ndeepest);
+    case CFMG_CYCLE_TWOLEV:  // twolevels! (src/gmg_cycles.jl:8-23)
+      if (L(h) < 2) return fail(h, CFMG_ERR_ARG, "twolev cycle needs at least 2 levels");
+      TRY(smooth_t<T>(h, 1, d.npre));
+      TRY(residual_t<T>(h, 1));
+      TRY(restrict_t<T>(h, 1, CFMG_R));
+      TRY(zero_t<T>(h, 2, CFMG_X));
+      TRY(smooth_t<T>(h, 2, d.ndeepest));
+      TRY(prolong_t<T>(h, 1));
+      return smooth_t<T>(h, 1, d.npost);
+    case CFMG_CYCLE_NLEV:  // nlevels! (src/gmg_cycles.jl:25-41), quirks kept
+      if (L(h) < 3) return fail(h, CFMG_ERR_ARG, "nlev cycle needs at least 3 levels");
+      for (int lev = 1; lev <= 2; ++lev) {
+        TRY(smooth_t<T>(h, lev, d.npre));
+        TRY(residual_t<T>(h, lev));
+        TRY(restrict_t<T>(h, lev, CFMG_R));
+        TRY(zero_t<T>(h, lev + 1, CFMG_X));
+      }
+      return smooth_t<T>(h, L(h), d.ndeepest);
+    default:
+      return fail(h, CFMG_ERR_ARG, "unknown cycle kind");
+  }
+}
+
+// norm of one FP64 field into dscal[S_NORM] (and dscal[S_RES] when normb given)
+int norm_dev(cfmg_handle* h, int lev, const double* x, const double* normb, int kind) {
+  const Level& l = h->lv[lev - 1];
+  Launch k(h, CFMG_K_NORM, lev, CFMG_FP64, 2);
+  launch_norm<double>(x, l.msk, l.len, h->partials, h->dscal + S_NORM, normb, kind, h->stream);
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
+// residual at level 1 followed by its norm ratio into dscal[S_RES]
+int normresidual_dev(cfmg_handle* h, int kind) {
+  TRY(residual_t<double>(h, 1));
+  return norm_dev(h, 1, h->lv[0].r, h->dscal + S_NORMB, kind);
+}
+
+int check_lev(cfmg_handle* h, int lev, int lo_off = 0) {
+  if (!h) return CFMG_ERR_ARG;
+  if (lev < 1 || lev > L(h) - lo_off)
+    return fail(h, CFMG_ERR_ARG, "level " + std::to_string(lev) + " out of range 1.." + std::to_string(L(h) - lo_off));
+  return CFMG_OK;
+}
+
+
+
+// ------------------------------------------------------------------ setup
+int setup_operators(cfmg_handle* h) {
+  const int nl = L(h);
+  const bool vert = vertices(h), t3 = threed(h), xp = xperio(h);
+  cudaStream_t s = h->stream;
+  // compute_msk_dev (src/gmg_setup.jl:322-366)
+  for (int lev = 1; lev <= nl - 1; ++lev) {
+    Level& f = h->lv[lev - 1];
+    Level& c = h->lv[lev];
+    const double threshold = vert ? 0.67 : 0.18;
+    launch_fill_f64(c.Rcoef, 1.0, c.len, s);
+    if (lev == 1) launch_u8_to_f64(f.msk, f.b, f.len, s);
+    TRY(restrict_t<double>(h, lev, CFMG_B));
+    const double coef = t3 ? (vert ? 1.0 / 64 : 1.0 / 8) : (vert ? 1.0 / 16 : 1.0 / 4);
+    launch_default_msk(DEFMSK_SCALE_F64, nullptr, c.b, coef, c, vert, t3, xp, s);
+    launch_threshold(c.b, c.msk, threshold, c.len, s);
+    launch_default_msk(DEFMSK_MUL, f.msk, nullptr, 0.0, f, vert, t3, xp, s);
+  }
+  if (h->d.op == CFMG_VARCOEF) {
+    for (int lev = 1; lev <= nl - 1; ++lev) {
+      Level& f = h->lv[lev - 1];
+      Level& c = h->lv[lev];
+      launch_fill_f64(c.kappa, 1.0, c.len, s);
+      launch_restrict_kappa(f.kappa, f.msk, c.kappa, geom(f), geom(c), interior(c), s);
+      fill_if<double>(h, lev + 1, c.kappa);
+    }
+    for (int lev = 1; lev <= nl; ++lev) {
+      Level& l = h->lv[lev - 1];
+      launch_face_coef(l.kappa, l.msk, l.cE, l.cN, geom(l), s);
+    }
+  }
+  for (int lev = 1; lev <= nl - 1; ++lev) {
+    Level& f = h->lv[lev - 1];
+    Level& c = h->lv[lev];
+    // compute_Rcoef! (src/gmg_setup.jl:186-212)
+    launch_u8_to_f64(c.msk, c.Rcoef, c.len, s);
+    if (vert) launch_u8_to_f64(f.msk, f.b, f.len, s);
+    else launch_fill_f64(f.b, 1.0, f.len, s);
+    TRY(restrict_t<double>(h, lev, CFMG_B));
+    launch_rcoef(c.msk, c.b, c.Rcoef, vert, t3 ? 1.0 / 16 : 1.0 / 4, c.len, s);
+    // compute_Pcoef! (src/gmg_setup.jl:214-237)
+    launch_u8_to_f64(f.msk, f.Pcoef, f.len, s);
+    launch_fill_f64(f.x, 0.0, f.len, s);
+    if (vert) launch_fill_f64(c.x, 1.0, c.len, s);
+    else launch_u8_to_f64(c.msk, c.x, c.len, s);
+    TRY(prolong_t<double>(h, lev));
+    launch_pcoef(f.msk, f.x, f.Pcoef, f.len, s);
+  }
+  // compute_diag! (src/gmg_setup.jl:239-262)
+  for (int lev = 1; lev <= nl; ++lev) {
+    Level& l = h->lv[lev - 1];
+    if (vert) launch_fill_f64(l.x, 1.0, l.len, s);
+    else launch_u8_to_f64(l.msk, l.x, l.len, s);
+    launch_fill_f64(l.b, 0.0, l.len, s);
+    launch_fill_f64(l.diag, 0.0, l.len, s);
+    TRY(residual_t<double>(h, lev));
+    launch_diag(l.msk, l.r, l.diag, l.idiag, l.len, s);
+    launch_widiag(l.idiag, l.widiag, h->d.omega, l.len, s);
+  }
+  LAUNCH_OK(h);
+  h->mixed_dirty = true;
+  return CFMG_OK;
+}
+
+// FP32 copies of the operator coefficients for the mixed-precision cycles.
+int prepare_mixed(cfmg_handle* h) {
+  if (!h->mixed_dirty) return CFMG_OK;
+  for (Level& l : h->lv) {
+    launch_to_f32(l.widiag, l.widiag32, l.len, h->stream);
+    launch_to_f32(l.diag, l.diag32, l.len, h->stream);
+    launch_to_f32(l.Rcoef, l.Rcoef32, l.len, h->stream);
+    launch_to_f32(l.Pcoef, l.Pcoef32, l.len, h->stream);
+    if (h->d.op == CFMG_VARCOEF) {
+      launch_to_f32(l.cE, l.cE32, l.len, h->stream);
+      launch_to_f32(l.cN, l.cN32, l.len, h->stream);
+    }
+  }
+  // number of wet cells of level 1 (for the residual scaling)
+  const Level& l1 = h->lv[0];
+  launch_fill_f64(l1.y, 1.0, l1.len, h->stream);
+  launch_norm<double>(l1.y, l1.msk, l1.len, h->partials, h->dscal + S_TMP0, nullptr, CFMG_NORM_L2, h->stream);
+  CUDA_OK(h, cudaMemcpyAsync(h->dscal + S_NWET, h->dscal + S_TMP0, sizeof(double), cudaMemcpyDeviceToDevice,
+                             h->stream));
+  CUDA_OK(h, cudaMemsetAsync(l1.y, 0, l1.len * sizeof(double), h->stream));
+  LAUNCH_OK(h);
+  h->mixed_dirty = false;
+  return CFMG_OK;
+}
+
+// ------------------------------------------------------- mixed-precision
+// Defect correction: r (FP64) -> scaled FP32 right-hand side of the
+// correction equation on level 1, with the wet mean removed for the
+// cell-centred (Neumann) operator.
+__global__ void k_mean_partial(const double* r, const uint8_t* m, long long n, double* partials) {
+  // Neumaier-compensated per-thread sums, fixed-order tree across the block
+  double s = 0.0, c = 0.0;
+  for (long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x; I < n; I += (long long)gridDim.x * blockDim.x) {
+    if (!m[I]) continue;
+    double v = r[I];
+    double t = __dadd_rn(s, v);
+    c = __dadd_rn(c, (fabs(s) >= fabs(v)) ? __dadd_rn(__dsub_rn(s, t), v) : __dadd_rn(__dsub_rn(v, t), s));
+    s = t;
+  }
+  s = __dadd_rn(s, c);
+  __shared__ double sh[256];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partials[blockIdx.x] = sh[0];
+}
+
+__global__ void k_scale_from_norm(double* dscal, const double* partials, int nparts, bool remove_mean) {
+  // dscal[S_NORM] = sum msk r^2 (raw or 1 if 0), dscal[S_NWET] = number of wet cells
+  __shared__ double sh[kNormParts];
+  double v = 0.0;
+  if (remove_mean && (int)threadIdx.x < nparts) v = partials[threadIdx.x];
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int w = kNormParts / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double nwet = dscal[S_NWET] > 0 ? dscal[S_NWET] : 1.0;
+    double rms = sqrt(dscal[S_NORM] / nwet);
+    const bool ok = rms > 0 && isfinite(rms);
+    dscal[S_SCALE] = ok ? 1.0 / rms : 1.0;
+    dscal[S_ISCALE] = ok ? rms : 1.0;
+    dscal[S_MEAN] = remove_mean ? sh[0] / nwet : 0.0;
+  }
+}
+
+__global__ void k_rhs32(const double* r, const uint8_t* m, const double* dscal, float* b32, float* r32, long long n) {
+  long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= n) return;
+  double v = m[I] ? (r[I] - dscal[S_MEAN]) * dscal[S_SCALE] : 0.0;
+  float f = (float)v;
+  b32[I] = f;
+  r32[I] = f;
+}
+
+// x += e / scale (the FP64 solution update)
+__global__ void k_update(double* x, const float* e, const double* dscal, long long n) {
+  long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= n) return;
+  x[I] = __fma_rn((double)e[I], dscal[S_ISCALE], x[I]);
+}
+
+int mixed_iteration(cfmg_handle* h, int kind) {
+  const Level& l1 = h->lv[0];
+  const long long n = (long long)l1.len;
+  const unsigned nb = (unsigned)((n + 255) / 256);
+  const bool remove_mean = !vertices(h);
+  {
+    Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED, remove_mean ? 3 : 2);
+    if (remove_mean) k_mean_partial<<<kNormParts, 256, 0, h->stream>>>(l1.r, l1.msk, n, h->partials);
+    k_scale_from_norm<<<1, kNormParts, 0, h->stream>>>(h->dscal, h->partials, kNormParts, remove_mean);
+    k_rhs32<<<nb, 256, 0, h->stream>>>(l1.r, l1.msk, h->dscal, l1.b32, l1.r32, n);
+  }
+  CUDA_OK(h, cudaMemsetAsync(l1.x32, 0, l1.len * sizeof(float), h->stream));
+  LAUNCH_OK(h);
+  TRY(cycle_t<float>(h, kind));
+  {
+    Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED);
+    k_update<<<nb, 256, 0, h->stream>>>(l1.x, l1.x32, h->dscal, n);
+  }
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
+// one solve iteration (cycle + normresidual + copy of the ratio to the host)
+int iteration(cfmg_handle* h, int prec, int kind, int norm_kind) {
+  if (prec == CFMG_MIXED) TRY(mixed_iteration(h, kind));
+  else TRY(cycle_t<double>(h, kind));
+  TRY(normresidual_dev(h, norm_kind));
+  CUDA_OK(h, cudaMemcpyAsync(h->hscal, h->dscal, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return CFMG_OK;
+}
+
+int get_graph(cfmg_handle* h, int prec, int kind, int norm_kind, cudaGraphExec_t* out) {
+  cudaGraphExec_t& ge = h->graph[prec][kind];
+  if (!ge) {
+    cudaGraph_t g = nullptr;
+    CUDA_OK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const long long before = h->launches;
+    h->capturing = true;
+    int rc = iteration(h, prec, kind, norm_kind);
+    h->capturing = false;
+    h->graph_launches[prec][kind] = h->launches - before;
+    h->launches = before;
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (rc != CFMG_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return fail(h, CFMG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      ge = nullptr;
+      return fail(h, CFMG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    }
+  }
+  *out = ge;
+  return CFMG_OK;
+}
+
+void drop_graphs(cfmg_handle* h) {
+  for (auto& row : h->graph)
+    for (auto& g : row)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+}
+
+// ----------------------------------------------------------- allocation
+std::vector<Level> create_levels(const cfmg_desc& d) {  // src/gmg_setup.jl:40-64
+  std::vector<Level> out;
+  int nx = d.nx, ny = d.ny, nz = d.nz;
+  const bool t3 = d.kase == CFMG_THREED;
+  const int maxlevs = d.nlevels > 0 ? d.nlevels : 29;
+  auto mk = [&](int a, int b, int c) {
+    Level l;
+    std::memset(&l, 0, sizeof(l));
+    l.nx = a; l.ny = b; l.nz = c; l.nh = d.nh;
+    l.tx = a + 2 * d.nh;
+    l.ty = b + 2 * d.nh;
+    l.tz = t3 ? c + 2 * d.nh : c;
+    l.threed = t3;
+    l.len = (size_t)l.tx * l.ty * l.tz;
+    l.ic0 = d.nh + 1; l.ic1 = a + d.nh;
+    l.jc0 = d.nh + 1; l.jc1 = b + d.nh;
+    l.kc0 = t3 ? d.nh + 1 : 1; l.kc1 = t3 ? c + d.nh : c;
+    return l;
+  };
+  out.push_back(mk(nx, ny, nz));
+  int lev = 1;
+  while (((long long)nx * ny > 8) && (nx > 2) && (ny > 2) && (lev < maxlevs)) {
+    nx /= 2;
+    ny /= 2;
+    if (t3) nz /= 2;
+    out.push_back(mk(nx, ny, nz));
+    lev += 1;
+  }
+  return out;
+}
+
+int validate(const cfmg_desc* d) {
+  if (!d) return fail(nullptr, CFMG_ERR_ARG, "null descriptor");
+  if (d->kase != CFMG_TWOD && d->kase != CFMG_THREED) return fail(nullptr, CFMG_ERR_ARG, "grid must be :twod or :threed");
+  if (d->location != CFMG_CENTERS && d->location != CFMG_VERTICES)
+    return fail(nullptr, CFMG_ERR_ARG, "location must be :centers or :vertices");
+  if (d->op < CFMG_LAPLACIAN || d->op > CFMG_VARCOEF) return fail(nullptr, CFMG_ERR_ARG, "unknown operator");
+  if (d->op == CFMG_VARCOEF && (d->kase != CFMG_TWOD || d->location != CFMG_CENTERS))
+    return fail(nullptr, CFMG_ERR_UNSUPPORTED, "the variable-coefficient operator is 2D cell-centred only");
+  if (d->topology != CFMG_CLOSED && d->topology != CFMG_XPERIO)
+    return fail(nullptr, CFMG_ERR_ARG, "topology is not implemented");
+  if (d->cycle < 0 || d->cycle > CFMG_CYCLE_VREC) return fail(nullptr, CFMG_ERR_ARG, "unknown cycle");
+  if (d->nx < 1 || d->ny < 1 || d->nz < 1) return fail(nullptr, CFMG_ERR_ARG, "nx, ny, nz must be >= 1");
+  if (d->nh < 2 || d->nh > 8) return fail(nullptr, CFMG_ERR_ARG, "nh must be in 2..8");
+  if (d->npre < 0 || d->npost < 0 || d->ndeepest < 0 || d->maxite < 0 || d->nlevels < 0)
+    return fail(nullptr, CFMG_ERR_ARG, "negative count");
+  if (d->precision != CFMG_FP64 && d->precision != CFMG_MIXED) return fail(nullptr, CFMG_ERR_ARG, "unknown precision");
+  if (d->norm_kind != CFMG_NORM_REF_SQUARED && d->norm_kind != CFMG_NORM_L2)
+    return fail(nullptr, CFMG_ERR_ARG, "unknown norm kind");
+  if (!(d->omega > 0.0 && d->omega < 2.0)) return fail(nullptr, CFMG_ERR_ARG, "omega must be in (0, 2)");
+  long long cells = (long long)(d->nx + 2 * d->nh) * (d->ny + 2 * d->nh) *
+                    (d->kase == CFMG_THREED ? d->nz + 2 * d->nh : d->nz);
+  if (cells > (1LL << 40)) return fail(nullptr, CFMG_ERR_ARG, "grid too large");
+  return CFMG_OK;
+}
+
+}  // namespace
+
+// ===================================================================== ABI
+extern "C" {
+
+int cfmg_desc_default(cfmg_desc* d) {
+  if (!d) return CFMG_ERR_ARG;
+  std::memset(d, 0, sizeof(*d));
+  d->kase = CFMG_THREED;
+  d->location = CFMG_CENTERS;
+  d->op = CFMG_LAPLACIAN;
+  d->topology = CFMG_CLOSED;
+  d->cycle = CFMG_CYCLE_V;
+  d->nx = d->ny = d->nz = 64;
+  d->nh = 3;
+  d->nlevels = 0;
+  d->npre = d->npost = 1;
+  d->ndeepest = 20;
+  d->maxite = 15;
+  d->omega = 0.9;
+  d->tol = 1e-10;
+  d->precision = CFMG_FP64;
+  d->norm_kind = CFMG_NORM_REF_SQUARED;
+  return CFMG_OK;
+}
+
+int cfmg_create(const cfmg_desc* d, cfmg_handle** out) {
+  if (!out) return fail(nullptr, CFMG_ERR_ARG, "null output pointer");
+  *out = nullptr;
+  TRY(validate(d));
+  cfmg_handle* h = new cfmg_handle();
+  h->d = *d;
+  h->lv = create_levels(*d);
+  if (cudaGetDevice(&h->device) != cudaSuccess) {
+    delete h;
+    return fail(nullptr, CFMG_ERR_CUDA, "no CUDA device");
+  }
+  // arena: all level arrays, 256-byte aligned
+  const bool mixed = d->precision == CFMG_MIXED;
+  const bool vc = d->op == CFMG_VARCOEF;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  size_t total = al(kNormParts * sizeof(double)) + al(S_COUNT * sizeof(double));
+  for (const Level& l : h->lv) {
+    size_t n = l.len;
+    total += 8 * al(n * 8) + al(n);           // x y r b diag idiag widiag Rcoef Pcoef + msk (Pcoef counted below)
+    total += al(n * 8);                       // Pcoef
+    total += (vc ? 3 : 0) * al(n * 8);        // kappa cE cN
+    total += (mixed ? 8 : 0) * al(n * 4);     // x32 y32 r32 b32 widiag32 diag32 Rcoef32 Pcoef32
+    total += (mixed && vc ? 2 : 0) * al(n * 4);
+  }
+  if (cudaMalloc(&h->arena, total) != cudaSuccess) {
+    cudaGetLastError();
+    delete h;
+    return fail(nullptr, CFMG_ERR_ALLOC, "device allocation of " + std::to_string(total) + " bytes failed");
+  }
+  h->arena_bytes = total;
+  char* p = (char*)h->arena;
+  auto take = [&](size_t b) {
+    void* q = p;
+    p += al(b);
+    return q;
+  };
+  h->partials = (double*)take(kNormParts * sizeof(double));
+  h->dscal = (double*)take(S_COUNT * sizeof(double));
+  for (Level& l : h->lv) {
+    size_t n = l.len;
+    l.x = (double*)take(n * 8); l.y = (double*)take(n * 8); l.r = (double*)take(n * 8); l.b = (double*)take(n * 8);
+    l.diag = (double*)take(n * 8); l.idiag = (double*)take(n * 8); l.widiag = (double*)take(n * 8);
+    l.Rcoef = (double*)take(n * 8); l.Pcoef = (double*)take(n * 8);
+    l.msk = (uint8_t*)take(n);
+    if (vc) { l.kappa = (double*)take(n * 8); l.cE = (double*)take(n * 8); l.cN = (double*)take(n * 8); }
+    if (mixed) {
+      l.x32 = (float*)take(n * 4); l.y32 = (float*)take(n * 4); l.r32 = (float*)take(n * 4); l.b32 = (float*)take(n * 4);
+      l.widiag32 = (float*)take(n * 4); l.diag32 = (float*)take(n * 4);
+      l.Rcoef32 = (float*)take(n * 4); l.Pcoef32 = (float*)take(n * 4);
+      if (vc) { l.cE32 = (float*)take(n * 4); l.cN32 = (float*)take(n * 4); }
+    }
+  }
+  if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaHostAlloc((void**)&h->hscal, S_COUNT * sizeof(double), cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    cfmg_destroy(h);
+    return fail(nullptr, CFMG_ERR_ALLOC, "stream or pinned allocation failed");
+  }
+  h->stream = h->own_stream;
+  if (cudaMemsetAsync(h->arena, 0, total, h->stream) != cudaSuccess) {
+    cfmg_destroy(h);
+    return fail(nullptr, CFMG_ERR_CUDA, "arena clear failed");
+  }
+  if (vc)
+    for (Level& l : h->lv) launch_fill_f64(l.kappa, 1.0, l.len, h->stream);
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+    cfmg_destroy(h);
+    return fail(nullptr, CFMG_ERR_CUDA, "initialisation kernels failed (is this an sm_103 GPU?)");
+  }
+  *out = h;
+  return CFMG_OK;
+}
+
+int cfmg_destroy(cfmg_handle* h) {
+  if (!h) return CFMG_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  drop_graphs(h);
+  harvest(h);
+  for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+  if (h->arena) cudaFree(h->arena);
+  if (h->hscal) cudaFreeHost(h->hscal);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  delete h;
+  return CFMG_OK;
+}
+
+const char* cfmg_last_error(const cfmg_handle* h) {
+  if (h) return h->err.c_str();
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  return g_create_err.c_str();
+}
+
+int cfmg_nlevels(const cfmg_handle* h, int* n) {
+  if (!h || !n) return CFMG_ERR_ARG;
+  *n = L(h);
+  return CFMG_OK;
+}
+
+int cfmg_level_dims(const cfmg_handle* h, int lev, int* dims) {
+  if (!h || !dims || lev < 1 || lev > L(h)) return CFMG_ERR_ARG;
+  const Level& l = h->lv[lev - 1];
+  dims[0] = l.nx; dims[1] = l.ny; dims[2] = l.nz; dims[3] = l.nh; dims[4] = l.tx; dims[5] = l.ty; dims[6] = l.tz;
+  return CFMG_OK;
+}
+
+int cfmg_set_stream(cfmg_handle* h, void* stream) {
+  if (!h) return CFMG_ERR_ARG;
+  CUDA_OK(h, cudaStreamSynchronize(h->stream));
+  h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+  return CFMG_OK;
+}
+
+int cfmg_synchronize(cfmg_handle* h) {
+  if (!h) return CFMG_ERR_ARG;
+  return sync(h);
+}
+
+static void* field_any(const Level& l, int f, size_t* elt) {
+  *elt = 8;
+  switch (f) {
+    case CFMG_X: return l.x;
+    case CFMG_R: return l.r;
+    case CFMG_B: return l.b;
+    case CFMG_Y: return l.y;
+    case CFMG_DIAG: return l.diag;
+    case CFMG_IDIAG: return l.idiag;
+    case CFMG_RCOEF: return l.Rcoef;
+    case CFMG_PCOEF: return l.Pcoef;
+    case CFMG_KAPPA: return l.kappa;
+    case CFMG_MSK: *elt = 1; return l.msk;
+    default: return nullptr;
+  }
+}
+
+int cfmg_field_ptr(cfmg_handle* h, int lev, int field, void** dptr) {
+  TRY(check_lev(h, lev));
+  size_t elt;
+  void* p = field_any(h->lv[lev - 1], field, &elt);
+  if (!p || !dptr) return fail(h, CFMG_ERR_ARG, "unknown field (kappa exists only for the varcoef operator)");
+  *dptr = p;
+  return CFMG_OK;
+}
+
+static int refresh_derived(cfmg_handle* h, int lev, int field) {
+  Level& l = h->lv[lev - 1];
+  if (field == CFMG_IDIAG) launch_widiag(l.idiag, l.widiag, h->d.omega, l.len, h->stream);
+  if (h->d.op == CFMG_VARCOEF && (field == CFMG_KAPPA || field == CFMG_MSK))
+    launch_face_coef(l.kappa, l.msk, l.cE, l.cN, geom(l), h->stream);
+  if (field >= CFMG_DIAG) h->mixed_dirty = true;
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
+int cfmg_upload(cfmg_handle* h, int lev, int field, const void* src) {
+  TRY(check_lev(h, lev));
+  size_t elt;
+  Level& l = h->lv[lev - 1];
+  void* p = field_any(l, field, &elt);
+  if (!p || !src) return fail(h, CFMG_ERR_ARG, "unknown field or null source");
+  CUDA_OK(h, cudaMemcpyAsync(p, src, l.len * elt, cudaMemcpyDefault, h->stream));
+  TRY(refresh_derived(h, lev, field));
+  return sync(h);
+}
+
+int cfmg_download(cfmg_handle* h, int lev, int field, void* dst) {
+  TRY(check_lev(h, lev));
+  size_t elt;
+  Level& l = h->lv[lev - 1];
+  void* p = field_any(l, field, &elt);
+  if (!p || !dst) return fail(h, CFMG_ERR_ARG, "unknown field or null destination");
+  CUDA_OK(h, cudaMemcpyAsync(dst, p, l.len * elt, cudaMemcpyDefault, h->stream));
+  return sync(h);
+}
+
+int cfmg_bind_level(cfmg_handle* h, int lev, const double* diag, const double* idiag, const double* Rcoef,
+                    const double* Pcoef, const uint8_t* msk) {
+  TRY(check_lev(h, lev));
+  Level& l = h->lv[lev - 1];
+  cudaStream_t s = h->stream;
+  if (diag) CUDA_OK(h, cudaMemcpyAsync(l.diag, diag, l.len * 8, cudaMemcpyDefault, s));
+  if (idiag) CUDA_OK(h, cudaMemcpyAsync(l.idiag, idiag, l.len * 8, cudaMemcpyDefault, s));
+  if (Rcoef) CUDA_OK(h, cudaMemcpyAsync(l.Rcoef, Rcoef, l.len * 8, cudaMemcpyDefault, s));
+  if (Pcoef) CUDA_OK(h, cudaMemcpyAsync(l.Pcoef, Pcoef, l.len * 8, cudaMemcpyDefault, s));
+  if (msk) CUDA_OK(h, cudaMemcpyAsync(l.msk, msk, l.len, cudaMemcpyDefault, s));
+  TRY(refresh_derived(h, lev, CFMG_IDIAG));
+  if (msk) TRY(refresh_derived(h, lev, CFMG_MSK));
+  h->mixed_dirty = true;
+  return sync(h);
+}
+
+int cfmg_set_default_msk(cfmg_handle* h) {
+  if (!h) return CFMG_ERR_ARG;
+  Level& l = h->lv[0];
+  launch_default_msk(DEFMSK_SET, l.msk, nullptr, 0.0, l, vertices(h), threed(h), xperio(h), h->stream);
+  LAUNCH_OK(h);
+  return sync(h);
+}
+
+int cfmg_setup_operators(cfmg_handle* h) {
+  if (!h) return CFMG_ERR_ARG;
+  TRY(setup_operators(h));
+  return sync(h);
+}
+
+int cfmg_smooth(cfmg_handle* h, int lev, int nite) {
+  TRY(check_lev(h, lev));
+  if (nite < 0) return fail(h, CFMG_ERR_ARG, "nite must be >= 0");
+  return smooth_t<double>(h, lev, nite);
+}
+
+int cfmg_residual(cfmg_handle* h, int lev) {
+  TRY(check_lev(h, lev));
+  return residual_t<double>(h, lev);
+}
+
+int cfmg_restrict(cfmg_handle* h, int lev, int field) {
+  TRY(check_lev(h, lev, 1));
+  if (field != CFMG_X && field != CFMG_R && field != CFMG_B && field != CFMG_Y)
+    return fail(h, CFMG_ERR_ARG, "restriction field must be x, r, b or y");
+  return restrict_t<double>(h, lev, field);
+}
+
+int cfmg_prolong(cfmg_handle* h, int lev) {
+  TRY(check_lev(h, lev, 1));
+  return prolong_t<double>(h, lev);
+}
+
+int cfmg_zero(cfmg_handle* h, int lev, int field) {
+  TRY(check_lev(h, lev));
+  size_t elt;
+  Level& l = h->lv[lev - 1];
+  void* p = field_any(l, field, &elt);
+  if (!p) return fail(h, CFMG_ERR_ARG, "unknown field");
+  CUDA_OK(h, cudaMemsetAsync(p, 0, l.len * elt, h->stream));
+  if (field >= CFMG_DIAG) TRY(refresh_derived(h, lev, field));
+  return CFMG_OK;
+}
+
+int cfmg_fill(cfmg_handle* h, int lev, int field) {
+  TRY(check_lev(h, lev));
+  size_t elt;
+  Level& l = h->lv[lev - 1];
+  void* p = field_any(l, field, &elt);
+  if (!p) return fail(h, CFMG_ERR_ARG, "unknown field");
+  if (!xperio(h)) return CFMG_OK;
+  if (elt == 1) launch_fill_xperio<uint8_t>((uint8_t*)p, geom(l), h->stream);
+  else launch_fill_xperio<double>((double*)p, geom(l), h->stream);
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
+int cfmg_norm(cfmg_handle* h, int lev, int field, double* out) {
+  TRY(check_lev(h, lev));
+  size_t elt;
+  Level& l = h->lv[lev - 1];
+  void* p = field_any(l, field, &elt);
+  if (!p || elt != 8 || !out) return fail(h, CFMG_ERR_ARG, "norm needs an FP64 field and an output");
+  TRY(norm_dev(h, lev, (const double*)p, nullptr, CFMG_NORM_REF_SQUARED));
+  CUDA_OK(h, cudaMemcpyAsync(h->hscal, h->dscal, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  *out = h->hscal[0];
+  return CFMG_OK;
+}
+
+int cfmg_normresidual(cfmg_handle* h, double normb, double* out) {
+  if (!h || !out) return CFMG_ERR_ARG;
+  if (!(normb > 0.0)) {
+    *out = 0.0;
+    return CFMG_OK;
+  }
+  TRY(residual_t<double>(h, 1));
+  double nr;
+  TRY(cfmg_norm(h, 1, CFMG_R, &nr));
+  *out = nr / normb;
+  return CFMG_OK;
+}
+
+int cfmg_cycle(cfmg_handle* h, int kind) {
+  if (!h) return CFMG_ERR_ARG;
+  return cycle_t<double>(h, kind);
+}
+
+int cfmg_solve(cfmg_handle* h, double* res_out, int* nite_out, double* history) {
+  if (!h || !res_out || !nite_out) return CFMG_ERR_ARG;
+  const cfmg_desc& d = h->d;
+  int prec = d.precision;
+  if (prec == CFMG_MIXED && L(h) == 1) prec = CFMG_FP64;  // no coarse level to correct with
+  if (prec == CFMG_MIXED && d.cycle != CFMG_CYCLE_V && d.cycle != CFMG_CYCLE_F && d.cycle != CFMG_CYCLE_VREC)
+    return fail(h, CFMG_ERR_UNSUPPORTED, "the mixed-precision form runs V and F cycles");
+  if (prec == CFMG_MIXED) TRY(prepare_mixed(h));
+  // normb = norm(mg, 1, :b) (src/gmg_solver.jl:22)
+  const Level& l1 = h->lv[0];
+  {
+    Launch k(h, CFMG_K_NORM, 1, CFMG_FP64, 2);
+    launch_norm<double>(l1.b, l1.msk, l1.len, h->partials, h->dscal + S_NORMB, nullptr, d.norm_kind, h->stream);
+  }
+  LAUNCH_OK(h);
+  TRY(normresidual_dev(h, d.norm_kind));
+  CUDA_OK(h, cudaMemcpyAsync(h->hscal, h->dscal, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  double res = h->hscal[S_RES];
+  if (history) history[0] = res;
+  int nite = 0;
+  cudaGraphExec_t ge = nullptr;
+  while ((res > d.tol) && (nite < d.maxite)) {  // src/gmg_solver.jl:29-39
+    nite += 1;
+    if (h->prof_cls >= 0) {
+      TRY(iteration(h, prec, d.cycle, d.norm_kind));  // eager, so launches can be bracketed
+    } else {
+      if (!ge) TRY(get_graph(h, prec, d.cycle, d.norm_kind, &ge));
+      CUDA_OK(h, cudaGraphLaunch(ge, h->stream));
+      h->launches += h->graph_launches[prec][d.cycle];
+    }
+    TRY(sync(h));
+    res = h->hscal[S_RES];
+    if (history) history[nite] = res;
+  }
+  *res_out = res;
+  *nite_out = nite;
+  return CFMG_OK;
+}
+
+int cfmg_launch_count(const cfmg_handle* h, long long* n) {
+  if (!h || !n) return CFMG_ERR_ARG;
+  *n = h->launches;
+  return CFMG_OK;
+}
+
+int cfmg_profile(cfmg_handle* h, int cls, int lev, int precision) {
+  if (!h) return CFMG_ERR_ARG;
+  TRY(sync(h));
+  h->prof_cls = cls;
+  h->prof_lev = lev;
+  h->prof_prec = precision;
+  h->prof_launches = 0;
+  h->prof_ms = 0.0;
+  return CFMG_OK;
+}
+
+int cfmg_profile_read(cfmg_handle* h, long long* launches, double* total_ms) {
+  if (!h || !launches || !total_ms) return CFMG_ERR_ARG;
+  TRY(sync(h));
+  *launches = h->prof_launches;
+  *total_ms = h->prof_ms;
+  return CFMG_OK;
+}
+
+}  // extern "C"

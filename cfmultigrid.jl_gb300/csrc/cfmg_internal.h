@@ -1,0 +1,121 @@
+// Internal declarations shared by the libcfmg translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/cfmg.h"
+
+namespace cfmg {
+
+// One level of the hierarchy on the device. Reference layout: column-major
+// tx*ty*tz arrays (src/gmg_types.jl:68-118), plus the derived arrays the
+// kernels stream instead of recomputing:
+//   widiag = omega*idiag (bit-identical to the reference's omega*idiag[I])
+//   the FP32 copies used by the mixed-precision cycles.
+struct Level {
+  int nx, ny, nz, nh, tx, ty, tz;
+  bool threed;
+  size_t len;
+  double *x, *y, *r, *b, *diag, *idiag, *widiag, *Rcoef, *Pcoef, *kappa;
+  double *cE, *cN;  // face coefficients of the variable-coefficient operator
+  uint8_t* msk;
+  // mixed precision copies (used by CFMG_MIXED)
+  float *x32, *y32, *r32, *b32, *widiag32, *diag32, *Rcoef32, *Pcoef32, *cE32, *cN32;
+  int ic0, ic1, jc0, jc1, kc0, kc1;  // interior box (1-based inclusive)
+};
+
+struct Box {  // 1-based inclusive index box
+  int i0, i1, j0, j1, k0, k1;
+};
+
+// Geometry passed by value to kernels.
+struct Geom {
+  int tx, ty, tz, nh;
+  long long len, n1, n2;  // n1 = tx, n2 = tx*ty
+};
+
+inline Geom geom(const Level& l) {
+  Geom g;
+  g.tx = l.tx; g.ty = l.ty; g.tz = l.tz; g.nh = l.nh;
+  g.len = (long long)l.len;
+  g.n1 = l.tx;
+  g.n2 = (long long)l.tx * l.ty;
+  return g;
+}
+
+// ---- per-level operators (k_ops.cu), templated on the field type T
+// (double: bit-exact parity form; float: the mixed-precision cycles).
+template <class T>
+void launch_sweep5_2d(const T* x, T* y, const T* b, const T* widiag, T cff, const Geom& g, cudaStream_t s);
+template <class T>
+void launch_sweep7_3d(const T* x, T* y, const T* b, const T* widiag, T cff, const Geom& g, cudaStream_t s);
+template <class T>
+void launch_sweep9_2d(const T* x, T* y, const T* b, const T* widiag, T cff, const Geom& g, const Box& bx,
+                      cudaStream_t s);
+template <class T>
+void launch_sweep19_3d(const T* x, T* y, const T* b, const T* widiag, T cff, const Geom& g, const Box& bx,
+                       cudaStream_t s);
+// variable coefficient: cE[I] / cN[I] are the face coefficients between I
+// and I+1 / I+n1 (0 across a dry cell)
+template <class T>
+void launch_sweep_vc_2d(const T* x, T* y, const T* b, const T* widiag, const T* cE, const T* cN, T cff,
+                        const Geom& g, cudaStream_t s);
+template <class T>
+void launch_resid5_2d(T* r, const T* x, const T* b, const T* diag, const uint8_t* msk, const Geom& g,
+                      cudaStream_t s);
+template <class T>
+void launch_resid7_3d(T* r, const T* x, const T* b, const T* diag, const uint8_t* msk, const Geom& g,
+                      const Box& bx, cudaStream_t s);
+template <class T>
+void launch_resid9_2d(T* r, const T* x, const T* b, const T* diag, const uint8_t* msk, const Geom& g,
+                      const Box& bx, cudaStream_t s);
+template <class T>
+void launch_resid19_3d(T* r, const T* x, const T* b, const T* diag, const uint8_t* msk, const Geom& g,
+                       const Box& bx, cudaStream_t s);
+template <class T>
+void launch_resid_vc_2d(T* r, const T* x, const T* b, const T* diag, const T* cE, const T* cN,
+                        const uint8_t* msk, const Geom& g, cudaStream_t s);
+// restriction: fine field -> coarse b over the coarse interior box;
+// kind: 0 centres 2D, 1 centres 3D, 2 vertices 2D, 3 vertices 3D
+template <class T>
+void launch_restrict(int kind, const T* xf, T* bc, const T* Rcoef, const Geom& gf, const Geom& gc,
+                     const Box& cbox, cudaStream_t s);
+// prolongation: fine x += Pcoef * P(coarse x); same kinds; (nxf, nyf, nzf)
+// are the fine level's nx, ny, nz and [kf0, kf1] its k-range of parents.
+template <class T>
+void launch_prolong(int kind, T* xf, const T* xc, const T* Pcoef, const Geom& gf, const Geom& gc, int nxf, int nyf,
+                    int nzf, int kf0, int kf1, cudaStream_t s);
+template <class T>
+void launch_fill_xperio(T* x, const Geom& g, cudaStream_t s);
+// norm: deterministic sum of msk*x^2 (FP64 accumulation) over the whole
+// array into out[0], with 0 -> 1 for the reference rule
+// (src/operators_at_level.jl:21-23). When normb != nullptr, out[1] is the
+// residual ratio: sum/normb (CFMG_NORM_REF_SQUARED) or sqrt(sum/normb) (L2).
+template <class T>
+void launch_norm(const T* x, const uint8_t* msk, size_t n, double* partials, double* out, const double* normb,
+                 int norm_kind, cudaStream_t s);
+constexpr int kNormParts = 1024;
+
+// ---- setup kernels (k_setup.cu)
+enum DefMskMode { DEFMSK_SET = 0, DEFMSK_MUL = 1, DEFMSK_SCALE_F64 = 2 };
+void launch_default_msk(int mode, uint8_t* msk, double* f, double coef, const Level& l, bool vertices, bool threed,
+                        bool xperio, cudaStream_t s);
+void launch_fill_f64(double* a, double v, size_t n, cudaStream_t s);
+void launch_u8_to_f64(const uint8_t* m, double* out, size_t n, cudaStream_t s);
+void launch_threshold(const double* b, uint8_t* msk, double thr, size_t n, cudaStream_t s);
+void launch_rcoef(const uint8_t* msk, const double* b, double* Rcoef, bool vertices, double coef, size_t n,
+                  cudaStream_t s);
+void launch_pcoef(const uint8_t* msk, const double* x, double* Pcoef, size_t n, cudaStream_t s);
+void launch_diag(const uint8_t* msk, const double* r, double* diag, double* idiag, size_t n, cudaStream_t s);
+void launch_widiag(const double* idiag, double* widiag, double omega, size_t n, cudaStream_t s);
+void launch_restrict_kappa(const double* kf, const uint8_t* mf, double* kc, const Geom& gf, const Geom& gc,
+                           const Box& cbox, cudaStream_t s);
+void launch_face_coef(const double* kappa, const uint8_t* msk, double* cE, double* cN, const Geom& g,
+                      cudaStream_t s);
+void launch_to_f32(const double* a, float* out, size_t n, cudaStream_t s);
+
+}  // namespace cfmg

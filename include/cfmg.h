@@ -1,0 +1,183 @@
+/*
+ * libcfmg: GB300-native (sm_103a) geometric multigrid for CFMultigrid.jl.
+ *
+ * A C ABI: plain pointers, sizes and ints, no CUDA or torch types. Every
+ * function returns an int status (CFMG_OK = 0); cfmg_last_error() gives
+ * the message of the last failure. A handle is not thread-safe; calls on
+ * one handle are issued in order on the handle's CUDA stream. Distinct
+ * handles are independent.
+ *
+ * The reference (ClimFlows/CFMultigrid.jl) is pure Julia. Its hot path is
+ * called through four per-level function tables
+ *   mg.smoother[lev](mg, lev, nite), mg.residual[lev](mg, lev),
+ *   mg.restriction[lev](mg, lev, field), mg.prolongation[lev](mg, lev)
+ * (src/gmg_types.jl:128-131, bound in src/gmg_setup.jl:86-101), plus
+ * solve!, norm, set_to_zero! and fill!. Each entry point below names the
+ * Julia function it replaces. The Julia glue that binds them with ccall
+ * is shown in INTEGRATION.md.
+ *
+ * Arrays crossing the ABI use the reference layout: one column-major
+ * (i fastest) array of tx*ty*tz entries per level and field, with
+ * tx = nx+2nh, ty = ny+2nh, tz = nz (2D) or nz+2nh (3D)
+ * (src/gmg_types.jl:68-118). FP64 fields are double, the mask is uint8_t.
+ * Pointers passed to upload/download/bind may be host or device memory.
+ */
+#ifndef CFMG_H
+#define CFMG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define CFMG_API __attribute__((visibility("default")))
+#else
+#define CFMG_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define CFMG_OK 0
+#define CFMG_ERR_ARG 1         /* invalid argument (the reference's AssertionError) */
+#define CFMG_ERR_CUDA 2        /* a CUDA call failed */
+#define CFMG_ERR_ALLOC 3       /* device or pinned allocation failed */
+#define CFMG_ERR_STATE 4       /* call out of order (e.g. solve before setup) */
+#define CFMG_ERR_NONFINITE 5   /* NaN/Inf met in a residual norm */
+#define CFMG_ERR_UNSUPPORTED 6 /* combination not implemented */
+
+/* Param symbols (src/gmg_types.jl:41-59) */
+#define CFMG_TWOD 0
+#define CFMG_THREED 1
+#define CFMG_CENTERS 0
+#define CFMG_VERTICES 1
+#define CFMG_LAPLACIAN 0  /* 5-point (2D) / 7-point (3D) */
+#define CFMG_LAPLACIAN9 1 /* 19-point (3D, src/laplacian9.jl) / in-plane 9-point (2D) */
+#define CFMG_VARCOEF 2    /* 2D cell-centred div(kappa grad x), face kappa = mean of the two cells */
+#define CFMG_CLOSED 0
+#define CFMG_XPERIO 1
+/* cycles of solve!'s table (src/gmg_solver.jl:11-16) */
+#define CFMG_CYCLE_V 0
+#define CFMG_CYCLE_F 1
+#define CFMG_CYCLE_ONELEV 2
+#define CFMG_CYCLE_TWOLEV 3
+#define CFMG_CYCLE_NLEV 4
+#define CFMG_CYCLE_VREC 5
+/* arithmetic of solve */
+#define CFMG_FP64 0  /* plain FP64 drop-in, bit-identical pointwise to the reference */
+#define CFMG_MIXED 1 /* FP32 cycles inside FP64 defect correction */
+/* stopping rule */
+#define CFMG_NORM_REF_SQUARED 0 /* the reference's sum(msk r^2)/sum(msk b^2) <= tol */
+#define CFMG_NORM_L2 1          /* ||r||_2/||b||_2 <= tol */
+
+/* field ids (src/gmg_types.jl:86-118) */
+#define CFMG_X 0
+#define CFMG_R 1
+#define CFMG_B 2
+#define CFMG_Y 3
+#define CFMG_DIAG 4
+#define CFMG_IDIAG 5
+#define CFMG_RCOEF 6
+#define CFMG_PCOEF 7
+#define CFMG_KAPPA 8
+#define CFMG_MSK 9
+
+/* kernel classes for cfmg_profile */
+#define CFMG_K_SWEEP 0    /* one Jacobi sweep (or a fused block of sweeps) */
+#define CFMG_K_RESIDUAL 1
+#define CFMG_K_RESTRICT 2
+#define CFMG_K_PROLONG 3
+#define CFMG_K_NORM 4
+#define CFMG_K_FILL 5
+#define CFMG_K_CONVERT 6  /* FP64 <-> FP32 transfers of the mixed form */
+
+typedef struct cfmg_desc {
+  int kase;     /* CFMG_TWOD / CFMG_THREED            (Param.case) */
+  int location; /* CFMG_CENTERS / CFMG_VERTICES       (Param.location) */
+  int op;       /* CFMG_LAPLACIAN / _LAPLACIAN9 / _VARCOEF (Param.operator) */
+  int topology; /* CFMG_CLOSED / CFMG_XPERIO          (Param.topology) */
+  int cycle;    /* CFMG_CYCLE_*                       (Param.cycle) */
+  int nx, ny, nz, nh;
+  int nlevels;  /* 0: the reference's hierarchy (src/gmg_setup.jl:40-64); else a cap */
+  int npre, npost, ndeepest, maxite;
+  double omega, tol;
+  int precision; /* CFMG_FP64 / CFMG_MIXED */
+  int norm_kind; /* CFMG_NORM_REF_SQUARED / CFMG_NORM_L2 */
+} cfmg_desc;
+
+typedef struct cfmg_handle cfmg_handle;
+
+/* Fill `d` with the defaults of Param() (src/gmg_types.jl:41-59). */
+CFMG_API int cfmg_desc_default(cfmg_desc* d);
+
+/* get_gmg's allocation part (src/gmg_setup.jl:26-35, create_levels :40-64,
+ * allocate_mg :77-104): builds the level hierarchy and allocates every
+ * level's fields on the current CUDA device, all zero. The default mask and
+ * operator setup are separate calls (cfmg_set_default_msk,
+ * cfmg_setup_operators) or come from the caller (cfmg_bind_level). */
+CFMG_API int cfmg_create(const cfmg_desc* d, cfmg_handle** out);
+CFMG_API int cfmg_destroy(cfmg_handle* h);
+/* Message of the last failure on `h` (or of the last failed cfmg_create when h is NULL). */
+CFMG_API const char* cfmg_last_error(const cfmg_handle* h);
+
+CFMG_API int cfmg_nlevels(const cfmg_handle* h, int* n);
+/* dims = {nx, ny, nz, nh, tx, ty, tz} of level lev (1-based). */
+CFMG_API int cfmg_level_dims(const cfmg_handle* h, int lev, int* dims);
+/* Issue all work of `h` on `stream` (a cudaStream_t, NULL = the handle's own stream). */
+CFMG_API int cfmg_set_stream(cfmg_handle* h, void* stream);
+CFMG_API int cfmg_synchronize(cfmg_handle* h);
+
+/* Copy a whole field of one level in or out (replaces reading/writing
+ * mg.data[lev].x/b/... and mg.oper[lev].* in Julia). */
+CFMG_API int cfmg_upload(cfmg_handle* h, int lev, int field, const void* src);
+CFMG_API int cfmg_download(cfmg_handle* h, int lev, int field, void* dst);
+/* Device address of a field (for zero-copy interop). */
+CFMG_API int cfmg_field_ptr(cfmg_handle* h, int lev, int field, void** dptr);
+
+/* Bind operator coefficients computed by the caller's own setup
+ * (setup_operators!, src/gmg_setup.jl:264-287). Any pointer may be NULL to
+ * keep the current array. */
+CFMG_API int cfmg_bind_level(cfmg_handle* h, int lev, const double* diag, const double* idiag, const double* Rcoef,
+                    const double* Pcoef, const uint8_t* msk);
+/* set_default_msk! (src/gmg_setup.jl:106-122) on the device. */
+CFMG_API int cfmg_set_default_msk(cfmg_handle* h);
+/* setup_operators! (src/gmg_setup.jl:264-287) on the device: coarse masks
+ * (compute_msk_dev), Rcoef, Pcoef, diag/idiag, from the level-1 mask. */
+CFMG_API int cfmg_setup_operators(cfmg_handle* h);
+
+/* Per-level operators: the function tables' entries. */
+CFMG_API int cfmg_smooth(cfmg_handle* h, int lev, int nite);        /* mg.smoother[lev]    (src/laplacian.jl:24-41,95-112; src/laplacian9.jl:2-47) */
+CFMG_API int cfmg_residual(cfmg_handle* h, int lev);                /* mg.residual[lev]    (src/laplacian.jl:53-64,114-128; src/laplacian9.jl:49-73) */
+CFMG_API int cfmg_restrict(cfmg_handle* h, int lev, int field);     /* mg.restriction[lev] (src/RP_on_centers.jl:73-82,135-144; src/RP_on_vertices.jl:1-32,140-150) */
+CFMG_API int cfmg_prolong(cfmg_handle* h, int lev);                 /* mg.prolongation[lev](src/RP_on_centers.jl:106-114,165-175; src/RP_on_vertices.jl:34-72,152-162) */
+CFMG_API int cfmg_zero(cfmg_handle* h, int lev, int field);         /* set_to_zero!        (src/operators_at_level.jl:7-10) */
+CFMG_API int cfmg_fill(cfmg_handle* h, int lev, int field);         /* fill!               (src/halo.jl:1-15) */
+CFMG_API int cfmg_norm(cfmg_handle* h, int lev, int field, double* out); /* norm       (src/operators_at_level.jl:12-27) */
+CFMG_API int cfmg_normresidual(cfmg_handle* h, double normb, double* out); /* normresidual! (src/operators_at_level.jl:29-36) */
+
+/* One cycle of solve!'s table (src/gmg_cycles.jl): kind = CFMG_CYCLE_*. */
+CFMG_API int cfmg_cycle(cfmg_handle* h, int kind);
+
+/* solve!(mg) (src/gmg_solver.jl:9-42) on the fields already on the device
+ * (b and the x warm start of level 1), with desc.tol, desc.maxite,
+ * desc.norm_kind and desc.precision. `history` (may be NULL) receives
+ * maxite+1 entries: the residual after 0..nite cycles. */
+CFMG_API int cfmg_solve(cfmg_handle* h, double* res, int* nite, double* history);
+
+/* Instrumentation (no counterpart in the reference, which has none).
+ * cfmg_launch_count: kernels this handle has launched so far; a replay of a
+ * captured solve iteration counts every kernel node in it.
+ * cfmg_profile: from now on, bracket every launch of kernel class `cls`
+ * (CFMG_K_*) on level `lev` in arithmetic `precision` with CUDA events on
+ * the handle's stream (cls < 0 turns it off). While it is on, cfmg_solve
+ * launches eagerly instead of replaying its graph. cfmg_profile_read
+ * returns the number of bracketed launches and their summed device time. */
+CFMG_API int cfmg_launch_count(const cfmg_handle* h, long long* n);
+CFMG_API int cfmg_profile(cfmg_handle* h, int cls, int lev, int precision);
+CFMG_API int cfmg_profile_read(cfmg_handle* h, long long* launches, double* total_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CFMG_H */

@@ -104,12 +104,17 @@ void fill_halo(orc_gmg* g, int lev, std::vector<T>& x) {
   if (g->p.topology == 0) return;
   const Grid& gr = g->L(lev).g;
   int nh = gr.nh, tx = gr.tx;
+  // Julia evaluates each right-hand slice before assigning it, which
+  // matters when nx < nh (source and destination columns overlap).
+  std::vector<T> tmp(nh);
   for (int k = 1; k <= gr.tz; ++k)
     for (int j = 1; j <= gr.ty; ++j) {
       // x[1:nh,:,:] = x[end+1-2nh:end-nh,:,:]
-      for (int i = 1; i <= nh; ++i) x[gr.at(i, j, k)] = x[gr.at(tx - 2 * nh + i, j, k)];
+      for (int i = 1; i <= nh; ++i) tmp[i - 1] = x[gr.at(tx - 2 * nh + i, j, k)];
+      for (int i = 1; i <= nh; ++i) x[gr.at(i, j, k)] = tmp[i - 1];
       // x[end+1-nh:end,:,:] = x[nh+1:2nh,:,:]
-      for (int i = 1; i <= nh; ++i) x[gr.at(tx - nh + i, j, k)] = x[gr.at(nh + i, j, k)];
+      for (int i = 1; i <= nh; ++i) tmp[i - 1] = x[gr.at(nh + i, j, k)];
+      for (int i = 1; i <= nh; ++i) x[gr.at(tx - nh + i, j, k)] = tmp[i - 1];
     }
 }
 
@@ -117,6 +122,7 @@ void fill_halo(orc_gmg* g, int lev, std::vector<T>& x) {
 // sloop2d! (src/laplacian.jl:66-73): linear range 1+n1 .. length-n1.
 void sloop2d(const A& x, A& y, const A& b, const A& idiag, const Grid& g, double omega) {
   const size_t n1 = g.tx, len = g.len();
+  #pragma omp parallel for schedule(static)
   for (size_t I = n1; I < len - n1; ++I) {  // 0-based I for 1-based 1+n1..len-n1
     double s = ((x[I - 1] + x[I + 1]) + x[I - n1]) + x[I + n1];
     y[I] = (1.0 - omega) * x[I] - (omega * idiag[I]) * (b[I] - s);
@@ -126,6 +132,7 @@ void sloop2d(const A& x, A& y, const A& b, const A& idiag, const Grid& g, double
 // rloop2d! (src/laplacian.jl:87-93)
 void rloop2d(A& r, const A& x, const A& b, const A& diag, const M& msk, const Grid& g) {
   const size_t n1 = g.tx, len = g.len();
+  #pragma omp parallel for schedule(static)
   for (size_t I = n1; I < len - n1; ++I) {
     double s = ((x[I - 1] + x[I + 1]) + x[I - n1]) + x[I + n1];
     r[I] = (double)msk[I] * (((diag[I] * x[I]) + b[I]) - s);
@@ -152,6 +159,7 @@ void residual_laplacian2d(orc_gmg* g, int lev) {
 // sloop3d_v1! (src/laplacian.jl:11-20): linear range 1+n2 .. length-n2.
 void sloop3d(const A& x, A& y, const A& b, const A& idiag, const Grid& g, double omega) {
   const size_t n1 = g.tx, n2 = (size_t)g.tx * g.ty, len = g.len();
+  #pragma omp parallel for schedule(static)
   for (size_t I = n2; I < len - n2; ++I) {
     double s = ((((x[I - 1] + x[I + 1]) + x[I - n1]) + x[I + n1]) + x[I - n2]) + x[I + n2];
     y[I] = (1.0 - omega) * x[I] - (omega * idiag[I]) * (b[I] - s);
@@ -173,6 +181,7 @@ void residual_laplacian3d(orc_gmg* g, int lev) {
   Level& l = g->L(lev);
   const Grid& gr = l.g;
   const size_t n1 = gr.tx, n2 = (size_t)gr.tx * gr.ty;
+  #pragma omp parallel for schedule(static)
   for (int k = gr.kc0(); k <= gr.kc1(); ++k)
     for (int j = gr.jc0(); j <= gr.jc1(); ++j)
       for (int i = gr.ic0(); i <= gr.ic1(); ++i) {
@@ -211,6 +220,7 @@ void smooth_laplacian9_3d(orc_gmg* g, int lev, int /*nite*/) {
   const Grid& gr = l.g;
   const size_t n1 = gr.tx, n2 = (size_t)gr.tx * gr.ty;
   const double omega = g->p.omega, cff = 1.0 - omega;
+  #pragma omp parallel for schedule(static)
   for (int k = gr.nh; k <= gr.nz + gr.nh + 1; ++k)
     for (int j = gr.nh; j <= gr.ny + gr.nh + 1; ++j)
       for (int i = gr.nh; i <= gr.nx + gr.nh + 1; ++i) {
@@ -218,6 +228,7 @@ void smooth_laplacian9_3d(orc_gmg* g, int lev, int /*nite*/) {
         l.y[I] = cff * l.x[I] - (omega * l.idiag[I]) *
                                     ((l.b[I] - faces19(l.x, I, n1, n2) / 2) - edges19(l.x, I, n1, n2) / 4);
       }
+  #pragma omp parallel for schedule(static)
   for (int k = gr.kc0(); k <= gr.kc1(); ++k)
     for (int j = gr.jc0(); j <= gr.jc1(); ++j)
       for (int i = gr.ic0(); i <= gr.ic1(); ++i) {
@@ -232,6 +243,7 @@ void residual_laplacian9_3d(orc_gmg* g, int lev) {
   Level& l = g->L(lev);
   const Grid& gr = l.g;
   const size_t n1 = gr.tx, n2 = (size_t)gr.tx * gr.ty;
+  #pragma omp parallel for schedule(static)
   for (int k = gr.kc0(); k <= gr.kc1(); ++k)
     for (int j = gr.jc0(); j <= gr.jc1(); ++j)
       for (int i = gr.ic0(); i <= gr.ic1(); ++i) {
@@ -259,12 +271,14 @@ void smooth_laplacian9_2d(orc_gmg* g, int lev, int nite) {
   const size_t n1 = gr.tx;
   const double omega = g->p.omega, cff = 1.0 - omega;
   for (int kt = 0; kt < nite; ++kt) {
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= gr.nz; ++k)
       for (int j = gr.nh; j <= gr.ny + gr.nh + 1; ++j)
         for (int i = gr.nh; i <= gr.nx + gr.nh + 1; ++i) {
           size_t I = gr.at(i, j, k);
           l.y[I] = cff * l.x[I] - (omega * l.idiag[I]) * ((l.b[I] - faces9(l.x, I, n1) / 2) - diags9(l.x, I, n1) / 4);
         }
+    #pragma omp parallel for schedule(static)
     for (int k = 1; k <= gr.nz; ++k)
       for (int j = gr.jc0(); j <= gr.jc1(); ++j)
         for (int i = gr.ic0(); i <= gr.ic1(); ++i) {
@@ -279,6 +293,7 @@ void residual_laplacian9_2d(orc_gmg* g, int lev) {
   Level& l = g->L(lev);
   const Grid& gr = l.g;
   const size_t n1 = gr.tx;
+  #pragma omp parallel for schedule(static)
   for (int k = 1; k <= gr.nz; ++k)
     for (int j = gr.jc0(); j <= gr.jc1(); ++j)
       for (int i = gr.ic0(); i <= gr.ic1(); ++i) {
@@ -311,6 +326,7 @@ void smooth_varcoef2d(orc_gmg* g, int lev, int nite) {
     for (int pass = 0; pass < 2; ++pass) {
       const A& x = pass == 0 ? l.x : l.y;
       A& y = pass == 0 ? l.y : l.x;
+#pragma omp parallel for schedule(static)
       for (size_t I = n1; I < len - n1; ++I) {
         double s = vc_sum(x, l.kappa, l.msk, I, n1);
         y[I] = (1.0 - omega) * x[I] - (omega * l.idiag[I]) * (l.b[I] - s);
@@ -323,6 +339,7 @@ void smooth_varcoef2d(orc_gmg* g, int lev, int nite) {
 void residual_varcoef2d(orc_gmg* g, int lev) {
   Level& l = g->L(lev);
   const size_t n1 = l.g.tx, len = l.g.len();
+#pragma omp parallel for schedule(static)
   for (size_t I = n1; I < len - n1; ++I) {
     double s = vc_sum(l.x, l.kappa, l.msk, I, n1);
     l.r[I] = (double)l.msk[I] * (((l.diag[I] * l.x[I]) + l.b[I]) - s);
@@ -346,6 +363,7 @@ void restriction_centers2d(orc_gmg* g, int lev, int f) {
   int nh = gc.nh;
   for (int kk = gc.kc0(); kk <= gc.kc1(); ++kk) {
     int k = kk;
+    #pragma omp parallel for schedule(static)
     for (int jj = gc.jc0(); jj <= gc.jc1(); ++jj) {
       int j = c2f(jj, nh);
       for (int ii = gc.ic0(); ii <= gc.ic1(); ++ii) {
@@ -369,6 +387,7 @@ void prolongation_centers2d(orc_gmg* g, int lev) {
   int nh = gf.nh;
   for (int k = gf.kc0(); k <= gf.kc1(); ++k) {
     int kc = k;
+    #pragma omp parallel for schedule(static)
     for (int j = nh + 1; j <= gf.ny + nh; j += 2) {
       int jc = f2c(j, nh);
       for (int i = nh + 1; i <= gf.nx + nh; i += 2) {
@@ -396,6 +415,7 @@ void restriction_centers3d(orc_gmg* g, int lev, int f) {
   int nh = gc.nh;
   for (int kk = gc.kc0(); kk <= gc.kc1(); ++kk) {
     int k = c2f(kk, nh);
+    #pragma omp parallel for schedule(static)
     for (int jj = gc.jc0(); jj <= gc.jc1(); ++jj) {
       int j = c2f(jj, nh);
       for (int ii = gc.ic0(); ii <= gc.ic1(); ++ii) {
@@ -425,6 +445,7 @@ void prolongation_centers3d(orc_gmg* g, int lev) {
   int nh = gf.nh;
   for (int k = nh + 1; k <= gf.nz + nh; k += 2) {
     int kc = f2c(k, nh);
+    #pragma omp parallel for schedule(static)
     for (int j = nh + 1; j <= gf.ny + nh; j += 2) {
       int jc = f2c(j, nh);
       for (int i = nh + 1; i <= gf.nx + nh; i += 2) {
@@ -457,6 +478,7 @@ void restriction_vertices3d(orc_gmg* g, int lev, int f) {
   int nh = gc.nh;
   for (int kk = gc.kc0(); kk <= gc.kc1(); ++kk) {
     int k = c2f(kk, nh);
+    #pragma omp parallel for schedule(static)
     for (int jj = gc.jc0(); jj <= gc.jc1(); ++jj) {
       int j = c2f(jj, nh);
       for (int ii = gc.ic0(); ii <= gc.ic1(); ++ii) {
@@ -489,6 +511,7 @@ void prolongation_vertices3d(orc_gmg* g, int lev) {
   int nh = gf.nh;
   for (int k = nh + 1; k <= gf.nz + nh; k += 2) {
     int kc = f2c(k, nh);
+    #pragma omp parallel for schedule(static)
     for (int j = nh + 1; j <= gf.ny + nh; j += 2) {
       int jc = f2c(j, nh);
       for (int i = nh + 1; i <= gf.nx + nh; i += 2) {
@@ -529,6 +552,7 @@ void restriction_vertices2d(orc_gmg* g, int lev, int f) {
   int nh = gc.nh;
   for (int kk = gc.kc0(); kk <= gc.kc1(); ++kk) {
     int k = kk;
+    #pragma omp parallel for schedule(static)
     for (int j = nh + 1; j <= 2 * gc.ny + nh; j += 2) {
       int jc = f2c(j, nh);
       for (int i = nh + 1; i <= 2 * gc.nx + nh; i += 2) {
@@ -559,6 +583,7 @@ void prolongation_vertices2d(orc_gmg* g, int lev) {
   int nh = gf.nh;
   for (int k = gf.kc0(); k <= gf.kc1(); ++k) {
     int kc = k;
+    #pragma omp parallel for schedule(static)
     for (int j = nh + 1; j <= gf.ny + nh; j += 2) {
       int jc = f2c(j, nh);
       for (int i = nh + 1; i <= gf.nx + nh; i += 2) {
@@ -636,6 +661,7 @@ M default_msk(orc_gmg* g, int lev) {
       for (int j = nh + 2; j <= gr.ny + nh; ++j)
         for (int i = nh + 2; i <= gr.nx + nh; ++i) msk[gr.at(i, j, k)] = 1;
   } else {
+    #pragma omp parallel for schedule(static)
     for (int k = gr.kc0(); k <= gr.kc1(); ++k)
       for (int j = gr.jc0(); j <= gr.jc1(); ++j)
         for (int i = gr.ic0(); i <= gr.ic1(); ++i) msk[gr.at(i, j, k)] = 1;
@@ -730,6 +756,7 @@ void restrict_kappa(orc_gmg* g, int lev) {
   int nh = gc.nh;
   std::fill(kc.begin(), kc.end(), 1.0);
   for (int kk = gc.kc0(); kk <= gc.kc1(); ++kk)
+    #pragma omp parallel for schedule(static)
     for (int jj = gc.jc0(); jj <= gc.jc1(); ++jj)
       for (int ii = gc.ic0(); ii <= gc.ic1(); ++ii) {
         int i = c2f(ii, nh), j = c2f(jj, nh);

@@ -19,6 +19,9 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libcfmg_oracle.so")
+# OpenMP build of the same source (identical results, element-wise loops
+# split over threads); selected with CFMG_ORACLE_THREADS > 1 before import.
+_LIB_OMP_PATH = os.path.join(_HERE, "_build", "libcfmg_oracle_omp.so")
 
 LOCATIONS = {"centers": 0, "vertices": 1}
 CASES = {"twod": 0, "threed": 1}
@@ -50,9 +53,10 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(_LIB_PATH):
+        path = _LIB_OMP_PATH if int(os.environ.get("CFMG_ORACLE_THREADS", "1")) > 1 else _LIB_PATH
+        if not os.path.exists(path):
             build()
-        L = ctypes.CDLL(_LIB_PATH)
+        L = ctypes.CDLL(path)
         vp = ctypes.c_void_p
         L.orc_get_gmg.restype = vp
         L.orc_get_gmg.argtypes = [ctypes.POINTER(_Param)]

@@ -1,0 +1,98 @@
+"""Mixed-precision form: FP32 V/F-cycles inside FP64 defect correction.
+
+Its result is checked against the CPU oracle's FP64 solve of the same
+problem: the true FP64 residual must meet the tolerance, and the solution
+(wet mean removed for the singular cell-centred case) must agree with the
+oracle's FP64 solution to the accuracy the tolerance implies.
+"""
+import numpy as np
+import pytest
+
+import fixtures as F
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+cfmg = pytest.importorskip("cfmg")
+
+CASES = {
+    "config1_256_centers_v": (dict(nx=256, ny=256, nz=1, case="twod", cycle="v", npre=2, npost=2, omega=0.8,
+                                   nlevels=6), "disk"),
+    "config2_512_vertices_lap9_f": (dict(nx=512, ny=512, nz=1, case="twod", location="vertices",
+                                         operator="laplacian9", cycle="f", npre=3, npost=3, omega=0.8,
+                                         nlevels=7), "disk"),
+    "3d_48_centers_v": (dict(nx=48, ny=48, nz=48, case="threed", cycle="v", npre=2, npost=2, omega=0.8), None),
+    "2d_xperio_vertices_v": (dict(nx=64, ny=64, nz=1, case="twod", location="vertices", topology="xperio",
+                                  cycle="v", npre=2, npost=2, omega=0.9, ndeepest=60), None),
+}
+
+
+def _mask(p, shape, kind):
+    if kind is None:
+        return None
+    m = F.get_circular_domain(shape, radius=0.45)
+    return F.get_mask_at_corners(m) if p.get("location") == "vertices" else m
+
+
+def _wet_mean_removed(x, m):
+    w = m.astype(bool)
+    y = x.copy()
+    y[w] -= y[w].mean()
+    y[~w] = 0
+    return y
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_mixed_matches_fp64_oracle(name):
+    base, mkind = CASES[name]
+    tol = 1e-10
+    p = dict(base, tol=tol * tol, maxite=40)  # oracle: squared rule, same threshold
+    og = O.OracleGmg(p)
+    shape = og.shape(1)
+    custom = _mask(base, shape, mkind)
+    if custom is not None:
+        og.field(1, "msk")[...] = custom
+        og.setup_operators()
+    for lev in range(1, og.nlevels + 1):
+        for f in ("x", "y", "r", "b"):
+            og.field(lev, f)[...] = 0.0
+    msk = og.field(1, "msk").copy()
+    b = np.asfortranarray(np.random.default_rng(5).standard_normal(shape)) * msk
+    F.subtract_mean(b, msk.astype(np.float64))
+    og.field(1, "b")[...] = b
+    res0, n0, _ = og.solve()
+
+    mg = cfmg.get_gmg(cfmg.Param(**base, tol=tol, maxite=40, residual_norm="l2", precision="mixed", verbose=False))
+    if custom is not None:
+        mg.oper[1].msk = custom
+        cfmg.setup_operators(mg)
+        for lev in range(1, mg.nlevels + 1):
+            for f in ("x", "y", "r", "b"):
+                cfmg.set_to_zero(mg, lev, f)
+    assert np.array_equal(mg.download(1, "msk"), msk)
+    mg.data[1].b = b
+    res1, n1, hist = cfmg.solve(mg, history=True)
+    assert res1 <= tol, (res1, hist)
+    # the reported residual is the true FP64 one: recompute it on the oracle
+    x = mg.data[1].x
+    og.field(1, "x")[...] = x
+    nb = og.norm(1, "b")
+    true_res = og.normresidual(nb) ** 0.5
+    assert true_res <= tol * 1.0001, true_res
+    assert abs(true_res - res1) <= 1e-6 * res1 + 1e-16
+    # iteration count within one of the FP64 form's
+    assert abs(n1 - n0) <= 1, (n1, n0)
+    # solution agreement with the FP64 oracle
+    xo = O.OracleGmg(p)  # fresh solve for x (og.x was overwritten)
+    if custom is not None:
+        xo.field(1, "msk")[...] = custom
+        xo.setup_operators()
+    for lev in range(1, xo.nlevels + 1):
+        for f in ("x", "y", "r", "b"):
+            xo.field(lev, f)[...] = 0.0
+    xo.field(1, "b")[...] = b
+    xo.solve()
+    singular = base.get("location", "centers") == "centers"
+    a = _wet_mean_removed(x, msk) if singular else x * msk
+    c = _wet_mean_removed(xo.x.copy(), msk) if singular else xo.x * msk
+    err = np.linalg.norm(a - c) / np.linalg.norm(c)
+    assert err <= 1e-6, err

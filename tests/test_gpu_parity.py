@@ -1,0 +1,212 @@
+"""CUDA path (libcfmg through its C ABI) against the CPU oracle.
+
+The FP64 form is required to be bit-identical to the oracle pointwise:
+every operator (sweep, residual, restriction, prolongation, halo fill) and
+the device-side setup coefficients are compared with ``array_equal``, and a
+whole solve must reproduce the oracle's iteration count, final x bit for bit
+and its residual history to 1e-12 relative (the norms' summation order is
+the only difference).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import fixtures as F
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+cfmg = pytest.importorskip("cfmg")
+
+HIST_RTOL = 1e-12
+# history entries against the oracle's sequential FP64 norm sums: the
+# oracle's own summation error on ~1e6 cells reaches ~3e-12
+HIST_RTOL_SEQ = 1e-11
+
+
+class GpuAdapter:
+    def __init__(self, mg):
+        self.mg = mg
+        self.nlevels = mg.nlevels
+
+    def shape(self, lev):
+        return self.mg.shape(lev)
+
+    def get(self, lev, name):
+        return self.mg.download(lev, name)
+
+    def set(self, lev, name, arr):
+        self.mg.upload(lev, name, arr)
+
+    def setup_operators(self):
+        cfmg.setup_operators(self.mg)
+
+
+def gpu_param(p, **kw):
+    d = dict(p)
+    d.update(kw)
+    d.setdefault("verbose", False)
+    d["verbose"] = False
+    return cfmg.Param(**d)
+
+
+def both(param_dict, **kw):
+    og = O.OracleGmg(dict(param_dict, **kw))
+    mg = cfmg.get_gmg(gpu_param(param_dict, **kw))
+    return og, mg
+
+
+CONFIGS = {
+    "2d_centers": dict(nx=48, ny=40, nz=1, case="twod"),
+    "2d_vertices": dict(nx=48, ny=40, nz=1, case="twod", location="vertices"),
+    "2d_centers_xperio": dict(nx=32, ny=24, nz=1, case="twod", topology="xperio"),
+    "2d_vertices_xperio": dict(nx=32, ny=24, nz=1, case="twod", location="vertices", topology="xperio"),
+    "2d_twolayer": dict(nx=32, ny=32, nz=2, case="twod"),
+    "3d_centers": dict(nx=24, ny=16, nz=16, case="threed"),
+    "3d_vertices": dict(nx=24, ny=16, nz=16, case="threed", location="vertices"),
+    "3d_centers_xperio": dict(nx=16, ny=16, nz=16, case="threed", topology="xperio"),
+    "3d_lap9": dict(nx=16, ny=16, nz=16, case="threed", operator="laplacian9"),
+    "3d_lap9_vertices": dict(nx=16, ny=16, nz=16, case="threed", operator="laplacian9", location="vertices"),
+    "2d_lap9_vertices": dict(nx=64, ny=48, nz=1, case="twod", operator="laplacian9", location="vertices"),
+    "2d_lap9_centers": dict(nx=64, ny=48, nz=1, case="twod", operator="laplacian9"),
+    "2d_varcoef": dict(nx=48, ny=40, nz=1, case="twod", operator="varcoef"),
+    "2d_odd": dict(nx=50, ny=38, nz=1, case="twod", nh=3),
+}
+
+
+def _disk(shape, location):
+    msk = F.get_circular_domain(shape, radius=0.45)
+    return F.get_mask_at_corners(msk) if location == "vertices" else msk
+
+
+def _setup_pair(name, custom_mask=True, seed=0):
+    p = CONFIGS[name]
+    og, mg = both(p)
+    if custom_mask and p.get("case") == "twod":
+        m = _disk(og.shape(1), p.get("location", "centers"))
+        if p.get("operator") == "varcoef":
+            rng = np.random.default_rng(seed + 7)
+            kap = np.exp(0.5 * rng.standard_normal(og.shape(1))).astype(np.float64)
+            kap = np.asfortranarray(kap)
+            og.field(1, "kappa")[...] = kap
+            mg.upload(1, "kappa", kap)
+        og.field(1, "msk")[...] = m
+        og.setup_operators()
+        mg.upload(1, "msk", m)
+        cfmg.setup_operators(mg)
+    return og, mg
+
+
+@pytest.mark.parametrize("name", sorted(CONFIGS))
+def test_setup_coefficients_bitwise(name):
+    og, mg = _setup_pair(name)
+    assert og.nlevels == mg.nlevels
+    for lev in range(1, og.nlevels + 1):
+        for f in ("msk", "diag", "idiag", "Rcoef", "Pcoef", "x", "b", "r"):
+            a, b = og.field(lev, f), mg.download(lev, f)
+            assert np.array_equal(a, b), (lev, f, np.abs(a.astype(float) - b).max())
+
+
+def _random_state(og, mg, rng):
+    for lev in range(1, og.nlevels + 1):
+        shape = og.shape(lev)
+        for f in ("x", "b", "y", "r"):
+            a = np.asfortranarray(rng.standard_normal(shape))
+            og.field(lev, f)[...] = a
+            mg.upload(lev, f, a)
+
+
+def _compare_all(og, mg, what):
+    for lev in range(1, og.nlevels + 1):
+        for f in ("x", "y", "r", "b"):
+            a, b = og.field(lev, f), mg.download(lev, f)
+            assert np.array_equal(a, b), (what, lev, f, np.nanmax(np.abs(a - b)))
+
+
+@pytest.mark.parametrize("name", sorted(CONFIGS))
+def test_operators_bitwise(name):
+    og, mg = _setup_pair(name)
+    rng = np.random.default_rng(1)
+    _random_state(og, mg, rng)
+    L = og.nlevels
+    for lev in (1, min(2, L), L):
+        og.smooth(lev, 2)
+        mg.smoother[lev](mg, lev, 2)
+        _compare_all(og, mg, f"smooth{lev}")
+        og.residual(lev)
+        mg.residual[lev](mg, lev)
+        _compare_all(og, mg, f"residual{lev}")
+    for lev in range(1, L):
+        for field in ("r", "b"):
+            og.restrict(lev, field)
+            mg.restriction[lev](mg, lev, field)
+            _compare_all(og, mg, f"restrict{lev}{field}")
+        og.prolong(lev)
+        mg.prolongation[lev](mg, lev)
+        _compare_all(og, mg, f"prolong{lev}")
+    for f in ("x", "r"):
+        og.fill(1, f)
+        cfmg.fill(mg, 1, f)
+    _compare_all(og, mg, "fill")
+    for f in ("x", "b", "r"):
+        a, b = og.norm(1, f), cfmg.norm(mg, 1, f)
+        assert abs(a - b) <= 1e-13 * abs(a), (f, a, b)
+
+
+@pytest.mark.parametrize("kind", ["v", "f", "onelev", "twolev", "nlev", "vrec"])
+def test_cycles_bitwise(kind):
+    og, mg = _setup_pair("2d_centers")
+    rng = np.random.default_rng(2)
+    _random_state(og, mg, rng)
+    og.cycle(kind)
+    cfmg.cycle(mg, kind)
+    _compare_all(og, mg, kind)
+
+
+def _solve_pair(sc, **gpu_kw):
+    og = O.OracleGmg(sc.param)
+    F.prepare(F.OracleAdapter(og), sc)
+    r0 = og.solve()
+    mg = cfmg.get_gmg(gpu_param(sc.param, **gpu_kw))
+    F.prepare(GpuAdapter(mg), sc)
+    r1 = cfmg.solve(mg, history=True)
+    return og, mg, r0, r1
+
+
+def _exact_ratio(mg):
+    """sum(msk r^2)/sum(msk b^2) of the device's final fields, summed exactly."""
+    m = mg.download(1, "msk").astype(np.float64).ravel()
+    r = mg.download(1, "r").ravel()
+    b = mg.download(1, "b").ravel()
+    nr = math.fsum(m * r * r) or 1.0
+    nb = math.fsum(m * b * b) or 1.0
+    return nr / nb
+
+
+def _check_solve(sc, og, mg, r0, r1):
+    (res0, n0, h0), (res1, n1, h1) = r0, r1
+    assert n1 == n0
+    # pointwise arithmetic is bit-identical: same final solution and residual
+    assert np.array_equal(og.x, mg.data[1].x)
+    assert np.array_equal(og.field(1, "r"), mg.download(1, "r"))
+    # the device norm is a tree sum: within 1e-13 of the exactly rounded
+    # ratio; the oracle (like the reference) sums sequentially, which on
+    # ~1e6 cells is itself off by up to a few 1e-12
+    assert abs(res1 - _exact_ratio(mg)) <= 1e-13 * res1
+    np.testing.assert_allclose(h1, h0, rtol=HIST_RTOL_SEQ, atol=0)
+
+
+@pytest.mark.parametrize("sc", F.KNOWN_ANSWERS + F.RECTANGULAR, ids=lambda s: s.name)
+def test_known_answer_solve(sc):
+    og, mg, r0, r1 = _solve_pair(sc)
+    assert r1[1] == sc.expect_ite
+    assert abs(r1[0] - sc.expect_res) <= sc.atol
+    _check_solve(sc, og, mg, r0, r1)
+
+
+@pytest.mark.parametrize("sc", F.ITERATION_ONLY[:3], ids=lambda s: s.name)
+def test_iteration_only_solve(sc):
+    og, mg, r0, r1 = _solve_pair(sc)
+    assert r1[1] == sc.expect_ite
+    _check_solve(sc, og, mg, r0, r1)
