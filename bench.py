@@ -141,7 +141,7 @@ def make_gmg(cfmg, param, vmsk, noise, precision, stream_ptr):
     p = cfmg.Param(**param, tol=TOL, maxite=MAXITE, residual_norm="l2", precision=precision, verbose=False)
     mg = cfmg.get_gmg(p)
     mg.set_stream(stream_ptr)
-    mg.data[1].msk = vmsk
+    mg.oper[1].msk = vmsk
     cfmg.setup_operators(mg)
     for lev in range(1, mg.nlevels + 1):
         for f in ("b", "x", "y", "r"):

@@ -232,6 +232,11 @@ class Gmg:
     def synchronize(self):
         self._check(self._L.cfmg_synchronize(self._h))
 
+    def set_option(self, name: str, value: int) -> None:
+        """Tuning knobs (``engine_cells``: levels of at most this many cells
+        run in the coarse-level program engine; 0 turns it off)."""
+        self._check(self._L.cfmg_set_option(self._h, _lib.OPTIONS[name], int(value)))
+
     def set_stream(self, stream_ptr: Optional[int]):
         self._check(self._L.cfmg_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
 

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <unordered_map>
 
 #include "cfmg_internal.h"
 
@@ -40,7 +41,16 @@ struct cfmg_handle {
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pending;
   long long prof_launches = 0;
   double prof_ms = 0.0;
+  // coarse-level program engine
+  bool engine_on = true;
+  long long engine_cells = 80000;  // levels of at most this many cells run in the engine
+  std::vector<cfmg::Op> pending;
+  cfmg::Op* prog_pool = nullptr;   // device program store
+  int pool_cap = 0, pool_used = 0;
+  std::unordered_map<std::string, int> prog_cache;
 };
+
+constexpr int kProgPoolOps = 8192;  // device store of engine programs (~1.9 MB)
 
 enum Scal { S_NORM = 0, S_RES = 1, S_NORMB = 2, S_NWET = 3, S_SCALE = 4, S_MEAN = 5, S_TMP0 = 6, S_ISCALE = 7,
             S_COUNT = 16 };
@@ -98,7 +108,10 @@ int harvest(cfmg_handle* h) {
   return CFMG_OK;
 }
 
+int flush(cfmg_handle* h);
+
 int sync(cfmg_handle* h) {
+  TRY(flush(h));
   CUDA_OK(h, cudaStreamSynchronize(h->stream));
   return harvest(h);
 }
@@ -167,49 +180,134 @@ T* field_ptr(const Level& l, int f) {
   }
 }
 
+// ----------------------------------------------------------- op emission
+// Every operator is an Op. emit() runs fine-level Ops as standalone kernels
+// and gathers consecutive coarse-level Ops (level length <= engine_cells)
+// into a pending program; flush() runs the pending program as one
+// cluster-launched engine kernel. Programs are cached on the device by
+// content, so a captured graph and later replays reuse the same copy.
+Op mkop(int kind, int prec, int lev, int cls, const Level& l) {
+  Op op;
+  std::memset(&op, 0, sizeof(op));
+  op.kind = kind;
+  op.prec = prec;
+  op.lev = lev;
+  op.cls = cls;
+  op.g = geom(l);
+  return op;
+}
+
+long long box_count(const Box& b) {
+  if (b.i1 < b.i0 || b.j1 < b.j0 || b.k1 < b.k0) return 0;
+  return (long long)(b.i1 - b.i0 + 1) * (b.j1 - b.j0 + 1) * (b.k1 - b.k0 + 1);
+}
+
+int flush(cfmg_handle* h) {
+  if (h->pending.empty()) return CFMG_OK;
+  const int n = (int)h->pending.size();
+  std::string key((const char*)h->pending.data(), (size_t)n * sizeof(Op));
+  auto it = h->prog_cache.find(key);
+  int off = -1;
+  if (it != h->prog_cache.end()) {
+    off = it->second;
+  } else if (h->pool_used + n <= h->pool_cap) {
+    // synchronous upload; allowed while the stream is being captured in
+    // relaxed mode, and never overwrites a program a graph refers to
+    CUDA_OK(h, cudaMemcpy(h->prog_pool + h->pool_used, h->pending.data(), (size_t)n * sizeof(Op),
+                          cudaMemcpyHostToDevice));
+    off = h->pool_used;
+    h->pool_used += n;
+    h->prog_cache.emplace(std::move(key), off);
+  }
+  if (off >= 0) {
+    Launch k(h, CFMG_K_ENGINE, 0, h->pending[0].prec ? CFMG_MIXED : CFMG_FP64);
+    launch_program(h->prog_pool + off, n, h->stream);
+  } else {  // pool full: run the Ops one by one
+    for (const Op& op : h->pending) {
+      Launch k(h, op.cls, op.lev, op.prec ? CFMG_MIXED : CFMG_FP64);
+      launch_op(op, h->stream);
+    }
+  }
+  h->pending.clear();
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
+int emit(cfmg_handle* h, const Op& op) {
+  if (op.n <= 0) return CFMG_OK;
+  const Level& l = h->lv[op.lev - 1];
+  if (h->engine_on && (long long)l.len <= h->engine_cells) {
+    h->pending.push_back(op);
+    return CFMG_OK;
+  }
+  TRY(flush(h));
+  Launch k(h, op.cls, op.lev, op.prec ? CFMG_MIXED : CFMG_FP64);
+  launch_op(op, h->stream);
+  return CFMG_OK;
+}
+
 template <class T>
-void fill_if(cfmg_handle* h, int lev, T* x) {
-  if (!xperio(h)) return;
-  Launch k(h, CFMG_K_FILL, lev, prec_of<T>());
-  launch_fill_xperio<T>(x, geom(h->lv[lev - 1]), h->stream);
+int fill_if(cfmg_handle* h, int lev, T* x) {
+  if (!xperio(h)) return CFMG_OK;
+  const Level& l = h->lv[lev - 1];
+  Op op = mkop(OPK_FILL, prec_of<T>() == CFMG_FP64 ? 0 : 1, lev, CFMG_K_FILL, l);
+  op.y = x;
+  op.n = (long long)l.ty * l.tz;
+  return emit(h, op);
+}
+
+template <class T>
+constexpr int pc() {
+  return sizeof(T) == 8 ? 0 : 1;
 }
 
 // ------------------------------------------------------- per-level operators
+template <class T>
+int sweep(cfmg_handle* h, int lev, int kind, const T* x, T* y, const Box* bx) {
+  const Level& l = h->lv[lev - 1];
+  View<T> v = view<T>(l);
+  Op op = mkop(kind, pc<T>(), lev, CFMG_K_SWEEP, l);
+  op.x = x; op.y = y; op.b = v.b; op.w = v.widiag; op.cE = v.cE; op.cN = v.cN;
+  op.cff = 1.0 - h->d.omega;
+  if (bx) {
+    op.box = *bx;
+    op.n = box_count(*bx);
+  } else {
+    const long long off = (kind == OPK_SWEEP7) ? op.g.n2 : op.g.n1;
+    op.lo = off;
+    op.n = op.g.len - 2 * off;
+  }
+  return emit(h, op);
+}
+
 // mg.smoother[lev] (src/gmg_setup.jl:124-139 selects among these)
 template <class T>
 int smooth_t(cfmg_handle* h, int lev, int nite) {
   const Level& l = h->lv[lev - 1];
   View<T> v = view<T>(l);
-  const Geom g = geom(l);
-  const T cff = (T)(1.0 - h->d.omega);
-  cudaStream_t s = h->stream;
   if (h->d.op == CFMG_LAPLACIAN9 && threed(h)) {
     // smooth_laplacian9! (src/laplacian9.jl:2-47): one pair whatever nite
     // is; sweep 1 over icp x jcp x kcp, sweep 2 over the interior; no fill!
     Box ext{l.nh, l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, l.nh, l.nz + l.nh + 1};
-    { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep19_3d<T>(v.x, v.y, v.b, v.widiag, cff, g, ext, s); }
-    { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep19_3d<T>(v.y, v.x, v.b, v.widiag, cff, g, interior(l), s); }
-    LAUNCH_OK(h);
-    return CFMG_OK;
+    Box in = interior(l);
+    TRY(sweep<T>(h, lev, OPK_SWEEP19, v.x, v.y, &ext));
+    return sweep<T>(h, lev, OPK_SWEEP19, v.y, v.x, &in);
   }
   for (int kt = 0; kt < nite; ++kt) {
     if (h->d.op == CFMG_LAPLACIAN9) {  // 2D 9-point extension
       Box ext{l.nh, l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, 1, l.nz};
-      { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep9_2d<T>(v.x, v.y, v.b, v.widiag, cff, g, ext, s); }
-      { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep9_2d<T>(v.y, v.x, v.b, v.widiag, cff, g, interior(l), s); }
-    } else if (h->d.op == CFMG_VARCOEF) {
-      { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep_vc_2d<T>(v.x, v.y, v.b, v.widiag, v.cE, v.cN, cff, g, s); }
-      { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep_vc_2d<T>(v.y, v.x, v.b, v.widiag, v.cE, v.cN, cff, g, s); }
-    } else if (threed(h)) {  // smooth_laplacian! (src/laplacian.jl:24-41)
-      { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep7_3d<T>(v.x, v.y, v.b, v.widiag, cff, g, s); }
-      { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep7_3d<T>(v.y, v.x, v.b, v.widiag, cff, g, s); }
-    } else {  // smooth_laplacian2d! (src/laplacian.jl:95-112)
-      { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep5_2d<T>(v.x, v.y, v.b, v.widiag, cff, g, s); }
-      { Launch k(h, CFMG_K_SWEEP, lev, prec_of<T>()); launch_sweep5_2d<T>(v.y, v.x, v.b, v.widiag, cff, g, s); }
+      Box in = interior(l);
+      TRY(sweep<T>(h, lev, OPK_SWEEP9, v.x, v.y, &ext));
+      TRY(sweep<T>(h, lev, OPK_SWEEP9, v.y, v.x, &in));
+    } else {
+      // smooth_laplacian2d! (src/laplacian.jl:95-112), smooth_laplacian!
+      // (src/laplacian.jl:24-41), variable coefficient
+      const int k = h->d.op == CFMG_VARCOEF ? OPK_SWEEPVC : (threed(h) ? OPK_SWEEP7 : OPK_SWEEP5);
+      TRY(sweep<T>(h, lev, k, v.x, v.y, nullptr));
+      TRY(sweep<T>(h, lev, k, v.y, v.x, nullptr));
     }
-    fill_if<T>(h, lev, v.x);
+    TRY(fill_if<T>(h, lev, v.x));
   }
-  LAUNCH_OK(h);
   return CFMG_OK;
 }
 
@@ -218,20 +316,25 @@ template <class T>
 int residual_t(cfmg_handle* h, int lev) {
   const Level& l = h->lv[lev - 1];
   View<T> v = view<T>(l);
-  const Geom g = geom(l);
-  cudaStream_t s = h->stream;
-  if (h->d.op == CFMG_LAPLACIAN9 && threed(h)) {  // residual_laplacian9!: interior, no fill!
-    { Launch k(h, CFMG_K_RESIDUAL, lev, prec_of<T>()); launch_resid19_3d<T>(v.r, v.x, v.b, v.diag, v.msk, g, interior(l), s); }
-    LAUNCH_OK(h);
-    return CFMG_OK;
+  Op op = mkop(OPK_RESID5, pc<T>(), lev, CFMG_K_RESIDUAL, l);
+  op.x = v.x; op.y = v.r; op.b = v.b; op.d = v.diag; op.m = v.msk; op.cE = v.cE; op.cN = v.cN;
+  Box in = interior(l);
+  if (h->d.op == CFMG_LAPLACIAN9) {
+    op.kind = threed(h) ? OPK_RESID19 : OPK_RESID9;  // interior box
+    op.box = in;
+    op.n = box_count(in);
+  } else if (threed(h)) {
+    op.kind = OPK_RESID7;  // rloop3d!: interior box
+    op.box = in;
+    op.n = box_count(in);
+  } else {
+    op.kind = h->d.op == CFMG_VARCOEF ? OPK_RESIDVC : OPK_RESID5;  // linear range 1+n1 .. len-n1
+    op.lo = op.g.n1;
+    op.n = op.g.len - 2 * op.g.n1;
   }
-  if (h->d.op == CFMG_LAPLACIAN9) { Launch k(h, CFMG_K_RESIDUAL, lev, prec_of<T>()); launch_resid9_2d<T>(v.r, v.x, v.b, v.diag, v.msk, g, interior(l), s); }
-  else if (h->d.op == CFMG_VARCOEF) { Launch k(h, CFMG_K_RESIDUAL, lev, prec_of<T>()); launch_resid_vc_2d<T>(v.r, v.x, v.b, v.diag, v.cE, v.cN, v.msk, g, s); }
-  else if (threed(h)) { Launch k(h, CFMG_K_RESIDUAL, lev, prec_of<T>()); launch_resid7_3d<T>(v.r, v.x, v.b, v.diag, v.msk, g, interior(l), s); }
-  else { Launch k(h, CFMG_K_RESIDUAL, lev, prec_of<T>()); launch_resid5_2d<T>(v.r, v.x, v.b, v.diag, v.msk, g, s); }
-  fill_if<T>(h, lev, v.r);
-  LAUNCH_OK(h);
-  return CFMG_OK;
+  TRY(emit(h, op));
+  if (h->d.op == CFMG_LAPLACIAN9 && threed(h)) return CFMG_OK;  // residual_laplacian9!: no fill!
+  return fill_if<T>(h, lev, v.r);
 }
 
 int rp_kind(const cfmg_handle* h) { return (vertices(h) ? 2 : 0) + (threed(h) ? 1 : 0); }
@@ -242,14 +345,15 @@ int restrict_t(cfmg_handle* h, int lev, int field) {
   const Level& f = h->lv[lev - 1];
   const Level& c = h->lv[lev];
   View<T> vc = view<T>(c);
-  const T* src = field_ptr<T>(f, field);
-  {
-    Launch k(h, CFMG_K_RESTRICT, lev, prec_of<T>());
-    launch_restrict<T>(rp_kind(h), src, vc.b, vc.Rcoef, geom(f), geom(c), interior(c), h->stream);
-  }
-  fill_if<T>(h, lev + 1, vc.b);
-  LAUNCH_OK(h);
-  return CFMG_OK;
+  Op op = mkop(OPK_RESTRICT0 + rp_kind(h), pc<T>(), lev, CFMG_K_RESTRICT, f);
+  op.gc = geom(c);
+  op.x = field_ptr<T>(f, field);
+  op.y = vc.b;
+  op.coef = vc.Rcoef;
+  op.box = interior(c);
+  op.n = box_count(op.box);
+  TRY(emit(h, op));
+  return fill_if<T>(h, lev + 1, vc.b);
 }
 
 // mg.prolongation[lev]: x of lev += Pcoef * P(x of lev+1), then fill!
@@ -259,34 +363,41 @@ int prolong_t(cfmg_handle* h, int lev) {
   const Level& c = h->lv[lev];
   View<T> vf = view<T>(f);
   View<T> vc = view<T>(c);
-  {
-    Launch k(h, CFMG_K_PROLONG, lev, prec_of<T>());
-    launch_prolong<T>(rp_kind(h), vf.x, vc.x, vf.Pcoef, geom(f), geom(c), f.nx, f.ny, f.nz, f.kc0, f.kc1, h->stream);
+  const int kind = rp_kind(h);
+  Op op = mkop(OPK_PROLONG0 + kind, pc<T>(), lev, CFMG_K_PROLONG, f);
+  op.gc = geom(c);
+  op.x = vc.x;
+  op.y = vf.x;
+  op.coef = vf.Pcoef;
+  // parents i = nh+1 : 2 : nx+nh (likewise j, and k in 3D)
+  op.np_i = (f.nx + 1) / 2;
+  op.np_j = (f.ny + 1) / 2;
+  int np_k;
+  if (kind == 1 || kind == 3) {
+    np_k = (f.nz + 1) / 2;
+    op.kf0 = 0;
+    op.kf1 = np_k - 1;
+  } else {
+    op.kf0 = f.kc0;
+    op.kf1 = f.kc1;
+    np_k = f.kc1 - f.kc0 + 1;
   }
-  fill_if<T>(h, lev, vf.x);
-  LAUNCH_OK(h);
-  return CFMG_OK;
+  op.n = (long long)op.np_i * op.np_j * np_k;
+  TRY(emit(h, op));
+  return fill_if<T>(h, lev, vf.x);
 }
 
 template <class T>
 int zero_t(cfmg_handle* h, int lev, int field) {
   const Level& l = h->lv[lev - 1];
-  T* p = field_ptr<T>(l, field);
-  CUDA_OK(h, cudaMemsetAsync(p, 0, l.len * sizeof(T), h->stream));
-  return CFMG_OK;
+  Op op = mkop(OPK_ZERO, pc<T>(), lev, CFMG_K_FILL, l);
+  op.y = field_ptr<T>(l, field);
+  op.n = (long long)l.len;
+  return emit(h, op);
 }
 
 // Mixed form: the coarsest level is solved in FP64 (FP32 b -> FP64 b,
 // ndeepest FP64 pairs, FP64 x -> FP32 x).
-__global__ void k_f32_to_f64(const float* a, double* out, long long n) {
-  long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (I < n) out[I] = (double)a[I];
-}
-__global__ void k_f64_to_f32(const double* a, float* out, long long n) {
-  long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (I < n) out[I] = (float)a[I];
-}
-
 template <class T>
 int coarsest_t(cfmg_handle* h, int nite);
 template <>
@@ -296,21 +407,18 @@ int coarsest_t<double>(cfmg_handle* h, int nite) {
 template <>
 int coarsest_t<float>(cfmg_handle* h, int nite) {
   if (L(h) == 1) return smooth_t<float>(h, 1, nite);
-  const Level& c = h->lv[L(h) - 1];
-  long long n = (long long)c.len;
-  unsigned nb = (unsigned)((n + 255) / 256);
-  {
-    Launch k(h, CFMG_K_CONVERT, L(h), CFMG_MIXED, 2);
-    k_f32_to_f64<<<nb, 256, 0, h->stream>>>(c.b32, c.b, n);
-    k_f32_to_f64<<<nb, 256, 0, h->stream>>>(c.x32, c.x, n);
-  }
-  TRY(smooth_t<double>(h, L(h), nite));
-  {
-    Launch k(h, CFMG_K_CONVERT, L(h), CFMG_MIXED);
-    k_f64_to_f32<<<nb, 256, 0, h->stream>>>(c.x, c.x32, n);
-  }
-  LAUNCH_OK(h);
-  return CFMG_OK;
+  const int lev = L(h);
+  const Level& c = h->lv[lev - 1];
+  Op op = mkop(OPK_F32TO64, 1, lev, CFMG_K_CONVERT, c);
+  op.n = (long long)c.len;
+  op.x = c.b32; op.y = c.b;
+  TRY(emit(h, op));
+  op.x = c.x32; op.y = c.x;
+  TRY(emit(h, op));
+  TRY(smooth_t<double>(h, lev, nite));
+  op.kind = OPK_F64TO32;
+  op.x = c.x; op.y = c.x32;
+  return emit(h, op);
 }
 
 // ------------------------------------------------------------------ cycles
@@ -350,7 +458,7 @@ int fcycle_t(cfmg_handle* h) {
 }
 
 template <class T>
-int cycle_t(cfmg_handle* h, int kind) {
+int cycle_body(cfmg_handle* h, int kind) {
   const cfmg_desc& d = h->d;
   switch (kind) {
     case CFMG_CYCLE_V:
@@ -383,8 +491,15 @@ int cycle_t(cfmg_handle* h, int kind) {
   }
 }
 
+template <class T>
+int cycle_t(cfmg_handle* h, int kind) {
+  TRY(cycle_body<T>(h, kind));
+  return flush(h);
+}
+
 // norm of one FP64 field into dscal[S_NORM] (and dscal[S_RES] when normb given)
 int norm_dev(cfmg_handle* h, int lev, const double* x, const double* normb, int kind) {
+  TRY(flush(h));
   const Level& l = h->lv[lev - 1];
   Launch k(h, CFMG_K_NORM, lev, CFMG_FP64, 2);
   launch_norm<double>(x, l.msk, l.len, h->partials, h->dscal + S_NORM, normb, kind, h->stream);
@@ -408,7 +523,16 @@ int check_lev(cfmg_handle* h, int lev, int lo_off = 0) {
 
 
 // ------------------------------------------------------------------ setup
+int setup_operators_body(cfmg_handle* h);
 int setup_operators(cfmg_handle* h) {
+  TRY(flush(h));
+  const bool on = h->engine_on;
+  h->engine_on = false;  // the setup interleaves element-wise kernels with the operators
+  int rc = setup_operators_body(h);
+  h->engine_on = on;
+  return rc;
+}
+int setup_operators_body(cfmg_handle* h) {
   const int nl = L(h);
   const bool vert = vertices(h), t3 = threed(h), xp = xperio(h);
   cudaStream_t s = h->stream;
@@ -563,13 +687,14 @@ int mixed_iteration(cfmg_handle* h, int kind) {
   const long long n = (long long)l1.len;
   const unsigned nb = (unsigned)((n + 255) / 256);
   const bool remove_mean = !vertices(h);
+  TRY(flush(h));
   {
     Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED, remove_mean ? 3 : 2);
     if (remove_mean) k_mean_partial<<<kNormParts, 256, 0, h->stream>>>(l1.r, l1.msk, n, h->partials);
     k_scale_from_norm<<<1, kNormParts, 0, h->stream>>>(h->dscal, h->partials, kNormParts, remove_mean);
     k_rhs32<<<nb, 256, 0, h->stream>>>(l1.r, l1.msk, h->dscal, l1.b32, l1.r32, n);
   }
-  CUDA_OK(h, cudaMemsetAsync(l1.x32, 0, l1.len * sizeof(float), h->stream));
+  TRY(zero_t<float>(h, 1, CFMG_X));
   LAUNCH_OK(h);
   TRY(cycle_t<float>(h, kind));
   {
@@ -593,7 +718,7 @@ int get_graph(cfmg_handle* h, int prec, int kind, int norm_kind, cudaGraphExec_t
   cudaGraphExec_t& ge = h->graph[prec][kind];
   if (!ge) {
     cudaGraph_t g = nullptr;
-    CUDA_OK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    CUDA_OK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeRelaxed));
     const long long before = h->launches;
     h->capturing = true;
     int rc = iteration(h, prec, kind, norm_kind);
@@ -724,7 +849,7 @@ int cfmg_create(const cfmg_desc* d, cfmg_handle** out) {
   const bool mixed = d->precision == CFMG_MIXED;
   const bool vc = d->op == CFMG_VARCOEF;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  size_t total = al(kNormParts * sizeof(double)) + al(S_COUNT * sizeof(double));
+  size_t total = al(kNormParts * sizeof(double)) + al(S_COUNT * sizeof(double)) + al((size_t)kProgPoolOps * sizeof(Op));
   for (const Level& l : h->lv) {
     size_t n = l.len;
     total += 8 * al(n * 8) + al(n);           // x y r b diag idiag widiag Rcoef Pcoef + msk (Pcoef counted below)
@@ -746,6 +871,8 @@ int cfmg_create(const cfmg_desc* d, cfmg_handle** out) {
     return q;
   };
   h->partials = (double*)take(kNormParts * sizeof(double));
+  h->prog_pool = (Op*)take((size_t)kProgPoolOps * sizeof(Op));
+  h->pool_cap = kProgPoolOps;
   h->dscal = (double*)take(S_COUNT * sizeof(double));
   for (Level& l : h->lv) {
     size_t n = l.len;
@@ -916,28 +1043,33 @@ int cfmg_setup_operators(cfmg_handle* h) {
 int cfmg_smooth(cfmg_handle* h, int lev, int nite) {
   TRY(check_lev(h, lev));
   if (nite < 0) return fail(h, CFMG_ERR_ARG, "nite must be >= 0");
-  return smooth_t<double>(h, lev, nite);
+  TRY(smooth_t<double>(h, lev, nite));
+  return flush(h);
 }
 
 int cfmg_residual(cfmg_handle* h, int lev) {
   TRY(check_lev(h, lev));
-  return residual_t<double>(h, lev);
+  TRY(residual_t<double>(h, lev));
+  return flush(h);
 }
 
 int cfmg_restrict(cfmg_handle* h, int lev, int field) {
   TRY(check_lev(h, lev, 1));
   if (field != CFMG_X && field != CFMG_R && field != CFMG_B && field != CFMG_Y)
     return fail(h, CFMG_ERR_ARG, "restriction field must be x, r, b or y");
-  return restrict_t<double>(h, lev, field);
+  TRY(restrict_t<double>(h, lev, field));
+  return flush(h);
 }
 
 int cfmg_prolong(cfmg_handle* h, int lev) {
   TRY(check_lev(h, lev, 1));
-  return prolong_t<double>(h, lev);
+  TRY(prolong_t<double>(h, lev));
+  return flush(h);
 }
 
 int cfmg_zero(cfmg_handle* h, int lev, int field) {
   TRY(check_lev(h, lev));
+  TRY(flush(h));
   size_t elt;
   Level& l = h->lv[lev - 1];
   void* p = field_any(l, field, &elt);
@@ -954,6 +1086,7 @@ int cfmg_fill(cfmg_handle* h, int lev, int field) {
   void* p = field_any(l, field, &elt);
   if (!p) return fail(h, CFMG_ERR_ARG, "unknown field");
   if (!xperio(h)) return CFMG_OK;
+  TRY(flush(h));
   if (elt == 1) launch_fill_xperio<uint8_t>((uint8_t*)p, geom(l), h->stream);
   else launch_fill_xperio<double>((double*)p, geom(l), h->stream);
   LAUNCH_OK(h);
@@ -1001,6 +1134,7 @@ int cfmg_solve(cfmg_handle* h, double* res_out, int* nite_out, double* history) 
   if (prec == CFMG_MIXED) TRY(prepare_mixed(h));
   // normb = norm(mg, 1, :b) (src/gmg_solver.jl:22)
   const Level& l1 = h->lv[0];
+  TRY(flush(h));
   {
     Launch k(h, CFMG_K_NORM, 1, CFMG_FP64, 2);
     launch_norm<double>(l1.b, l1.msk, l1.len, h->partials, h->dscal + S_NORMB, nullptr, d.norm_kind, h->stream);
@@ -1035,6 +1169,19 @@ int cfmg_launch_count(const cfmg_handle* h, long long* n) {
   if (!h || !n) return CFMG_ERR_ARG;
   *n = h->launches;
   return CFMG_OK;
+}
+
+int cfmg_set_option(cfmg_handle* h, int option, long long value) {
+  if (!h) return CFMG_ERR_ARG;
+  TRY(sync(h));
+  if (option == CFMG_OPT_ENGINE_CELLS) {
+    if (value < 0) return fail(h, CFMG_ERR_ARG, "engine_cells must be >= 0");
+    h->engine_cells = value;
+    h->engine_on = value > 0;
+    drop_graphs(h);  // captured graphs embed the old split
+    return CFMG_OK;
+  }
+  return fail(h, CFMG_ERR_ARG, "unknown option");
 }
 
 int cfmg_profile(cfmg_handle* h, int cls, int lev, int precision) {

@@ -100,6 +100,36 @@ void launch_norm(const T* x, const uint8_t* msk, size_t n, double* partials, dou
                  int norm_kind, cudaStream_t s);
 constexpr int kNormParts = 1024;
 
+// ---- operator descriptors and the coarse-level program engine (k_coarse.cu)
+// One Op describes one launch-worth of work on one level: its kind, the
+// arithmetic (prec 0 = double, 1 = float), its operands and its index space
+// of n work items. Fine levels run an Op as a standalone kernel; consecutive
+// Ops on coarse levels are gathered into a program that one cluster-launched
+// kernel executes, with a cluster barrier between Ops.
+enum OpKind : int {
+  OPK_SWEEP5 = 0, OPK_SWEEP7, OPK_SWEEP9, OPK_SWEEP19, OPK_SWEEPVC,
+  OPK_RESID5, OPK_RESID7, OPK_RESID9, OPK_RESID19, OPK_RESIDVC,
+  OPK_RESTRICT0, OPK_RESTRICT1, OPK_RESTRICT2, OPK_RESTRICT3,
+  OPK_PROLONG0, OPK_PROLONG1, OPK_PROLONG2, OPK_PROLONG3,
+  OPK_FILL, OPK_ZERO, OPK_F32TO64, OPK_F64TO32,
+};
+struct Op {
+  int kind, prec, lev, cls;  // cls: CFMG_K_* class for accounting
+  long long n;               // work items
+  long long lo;              // linear ops: first index
+  Box box;                   // box ops: index box
+  Geom g, gc;                // level (and coarse level for R/P)
+  int np_i, np_j, kf0, kf1;  // prolongation parents
+  double cff;
+  const void *x, *b, *w, *d, *cE, *cN, *coef;
+  void* y;  // the written field: sweep y, residual r, coarse b, fine x, filled/zeroed field
+  const uint8_t* m;
+};
+constexpr int kEngineCtas = 8;      // cluster size (portable)
+constexpr int kEngineThreads = 1024;
+void launch_op(const Op& op, cudaStream_t s);                   // one Op as a standalone kernel
+void launch_program(const Op* prog, int nops, cudaStream_t s);  // a device-resident program
+
 // ---- setup kernels (k_setup.cu)
 enum DefMskMode { DEFMSK_SET = 0, DEFMSK_MUL = 1, DEFMSK_SCALE_F64 = 2 };
 void launch_default_msk(int mode, uint8_t* msk, double* f, double coef, const Level& l, bool vertices, bool threed,

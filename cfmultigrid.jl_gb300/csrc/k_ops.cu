@@ -12,40 +12,9 @@
 // These kernels are single-pass and keep the reference's own loop ranges,
 // halo cells included; they are FP64-issue bound on GB300 (the FP64 pipe
 // runs at 1/64 of the FP32 rate), so their memory traffic is not the limit.
-#include "cfmg_internal.h"
+#include "ops_dev.cuh"
 
 namespace cfmg {
-
-template <class T>
-struct Ar;
-template <>
-struct Ar<double> {
-  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
-  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
-  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
-  // a*w + c with w a power of two (exact product): one rounding, same value
-  static __device__ __forceinline__ double fmx(double a, double w, double c) { return __fma_rn(a, w, c); }
-};
-template <>
-struct Ar<float> {
-  static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
-  static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
-  static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
-  static __device__ __forceinline__ float fmx(float a, float w, float c) { return __fmaf_rn(a, w, c); }
-};
-
-// msk*v for a UInt8 mask, as the reference's promote-and-multiply: 1 -> v,
-// 0 -> a zero carrying v's sign, other values -> (double)m*v.
-template <class T>
-__device__ __forceinline__ T mask_mul(uint8_t m, T v) {
-  if (m == 1) return v;
-  if (m == 0) return copysign(T(0), v);
-  return Ar<T>::mul(T(m), v);
-}
-
-__device__ __forceinline__ long long lin(const Geom& g, int i, int j, int k) {
-  return (long long)(i - 1) + g.n1 * ((long long)(j - 1) + (long long)g.ty * (k - 1));
-}
 
 constexpr int kThreads = 256;
 
@@ -59,10 +28,7 @@ __global__ void __launch_bounds__(kThreads) k_sweep5_2d(const T* __restrict__ x,
                                                         const T* __restrict__ b, const T* __restrict__ w, T cff,
                                                         long long n1, long long lo, long long hi) {
   long long I = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (I >= hi) return;
-  typedef Ar<T> A;
-  T s = A::add(A::add(A::add(x[I - 1], x[I + 1]), x[I - n1]), x[I + n1]);
-  y[I] = A::sub(A::mul(cff, x[I]), A::mul(w[I], A::sub(b[I], s)));
+  if (I < hi) d_sweep5(x, y, b, w, cff, n1, I);
 }
 
 // sloop3d_v1! (src/laplacian.jl:11-20): 7-point, linear range 1+n2 .. length-n2.
@@ -71,10 +37,7 @@ __global__ void __launch_bounds__(kThreads) k_sweep7_3d(const T* __restrict__ x,
                                                         const T* __restrict__ b, const T* __restrict__ w, T cff,
                                                         long long n1, long long n2, long long lo, long long hi) {
   long long I = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (I >= hi) return;
-  typedef Ar<T> A;
-  T s = A::add(A::add(A::add(A::add(A::add(x[I - 1], x[I + 1]), x[I - n1]), x[I + n1]), x[I - n2]), x[I + n2]);
-  y[I] = A::sub(A::mul(cff, x[I]), A::mul(w[I], A::sub(b[I], s)));
+  if (I < hi) d_sweep7(x, y, b, w, cff, n1, n2, I);
 }
 
 // Thread mapping of a box kernel: x over i, y over j, z over k.
@@ -97,52 +60,12 @@ inline dim3 box_grid(const Box& bx, dim3 blk) {
 inline bool box_empty(const Box& bx) { return bx.i1 < bx.i0 || bx.j1 < bx.j0 || bx.k1 < bx.k0; }
 static const dim3 kBoxBlk(64, 4, 1);
 
-// In-plane part of laplacian9 (2D 9-point extension): faces/2, diagonals/4.
-template <class T>
-__device__ __forceinline__ T faces4(const T* x, long long I, long long n1) {
-  typedef Ar<T> A;
-  return A::add(A::add(A::add(x[I - 1], x[I + 1]), x[I - n1]), x[I + n1]);
-}
-template <class T>
-__device__ __forceinline__ T diags4(const T* x, long long I, long long n1) {
-  typedef Ar<T> A;
-  return A::add(A::add(A::add(x[I - 1 - n1], x[I + 1 - n1]), x[I - 1 + n1]), x[I + 1 + n1]);
-}
-
 template <class T>
 __global__ void __launch_bounds__(kThreads) k_sweep9_2d(const T* __restrict__ x, T* __restrict__ y,
                                                         const T* __restrict__ b, const T* __restrict__ w, T cff,
                                                         Geom g, Box bx) {
   BoxIdx q = box_idx(bx);
-  if (!q.ok) return;
-  typedef Ar<T> A;
-  long long I = lin(g, q.i, q.j, q.k);
-  T t = A::fmx(faces4(x, I, g.n1), T(-0.5), b[I]);   // b - faces/2
-  t = A::fmx(diags4(x, I, g.n1), T(-0.25), t);      // - diagonals/4
-  y[I] = A::sub(A::mul(cff, x[I]), A::mul(w[I], t));
-}
-
-// 19-point stencil of smooth_laplacian9! (src/laplacian9.jl:14-44).
-template <class T>
-__device__ __forceinline__ T faces6(const T* x, long long I, long long n1, long long n2) {
-  typedef Ar<T> A;
-  return A::add(A::add(A::add(A::add(A::add(x[I - 1], x[I + 1]), x[I - n1]), x[I + n1]), x[I - n2]), x[I + n2]);
-}
-template <class T>
-__device__ __forceinline__ T edges12(const T* x, long long I, long long n1, long long n2) {
-  typedef Ar<T> A;
-  T e = A::add(x[I - 1 - n1], x[I + 1 - n1]);
-  e = A::add(e, x[I - 1 + n1]);
-  e = A::add(e, x[I + 1 + n1]);
-  e = A::add(e, x[I - 1 - n2]);
-  e = A::add(e, x[I + 1 - n2]);
-  e = A::add(e, x[I - 1 + n2]);
-  e = A::add(e, x[I + 1 + n2]);
-  e = A::add(e, x[I - n1 - n2]);
-  e = A::add(e, x[I + n1 - n2]);
-  e = A::add(e, x[I - n1 + n2]);
-  e = A::add(e, x[I + n1 + n2]);
-  return e;
+  if (q.ok) d_sweep9(x, y, b, w, cff, g.n1, lin(g, q.i, q.j, q.k));
 }
 
 template <class T>
@@ -150,21 +73,7 @@ __global__ void __launch_bounds__(kThreads) k_sweep19_3d(const T* __restrict__ x
                                                          const T* __restrict__ b, const T* __restrict__ w, T cff,
                                                          Geom g, Box bx) {
   BoxIdx q = box_idx(bx);
-  if (!q.ok) return;
-  typedef Ar<T> A;
-  long long I = lin(g, q.i, q.j, q.k);
-  T t = A::fmx(faces6(x, I, g.n1, g.n2), T(-0.5), b[I]);
-  t = A::fmx(edges12(x, I, g.n1, g.n2), T(-0.25), t);
-  y[I] = A::sub(A::mul(cff, x[I]), A::mul(w[I], t));
-}
-
-// Variable-coefficient 5-point sweep over sloop2d!'s linear range.
-template <class T>
-__device__ __forceinline__ T vc_sum(const T* x, const T* cE, const T* cN, long long I, long long n1) {
-  typedef Ar<T> A;
-  T s = A::add(A::mul(cE[I - 1], x[I - 1]), A::mul(cE[I], x[I + 1]));
-  s = A::add(s, A::mul(cN[I - n1], x[I - n1]));
-  return A::add(s, A::mul(cN[I], x[I + n1]));
+  if (q.ok) d_sweep19(x, y, b, w, cff, g.n1, g.n2, lin(g, q.i, q.j, q.k));
 }
 
 template <class T>
@@ -173,10 +82,7 @@ __global__ void __launch_bounds__(kThreads) k_sweep_vc_2d(const T* __restrict__ 
                                                           const T* __restrict__ cE, const T* __restrict__ cN, T cff,
                                                           long long n1, long long lo, long long hi) {
   long long I = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (I >= hi) return;
-  typedef Ar<T> A;
-  T s = vc_sum(x, cE, cN, I, n1);
-  y[I] = A::sub(A::mul(cff, x[I]), A::mul(w[I], A::sub(b[I], s)));
+  if (I < hi) d_sweepvc(x, y, b, w, cE, cN, cff, n1, I);
 }
 
 // -------------------------------------------------------------- residuals
@@ -187,10 +93,7 @@ __global__ void __launch_bounds__(kThreads) k_resid5_2d(T* __restrict__ r, const
                                                         const uint8_t* __restrict__ m, long long n1, long long lo,
                                                         long long hi) {
   long long I = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (I >= hi) return;
-  typedef Ar<T> A;
-  T s = A::add(A::add(A::add(x[I - 1], x[I + 1]), x[I - n1]), x[I + n1]);
-  r[I] = mask_mul(m[I], A::sub(A::add(A::mul(d[I], x[I]), b[I]), s));
+  if (I < hi) d_resid5(r, x, b, d, m, n1, I);
 }
 
 // rloop3d! (src/laplacian.jl:43-51): interior box only.
@@ -199,11 +102,7 @@ __global__ void __launch_bounds__(kThreads) k_resid7_3d(T* __restrict__ r, const
                                                         const T* __restrict__ b, const T* __restrict__ d,
                                                         const uint8_t* __restrict__ m, Geom g, Box bx) {
   BoxIdx q = box_idx(bx);
-  if (!q.ok) return;
-  typedef Ar<T> A;
-  long long I = lin(g, q.i, q.j, q.k);
-  T s = faces6(x, I, g.n1, g.n2);
-  r[I] = mask_mul(m[I], A::sub(A::add(A::mul(d[I], x[I]), b[I]), s));
+  if (q.ok) d_resid7(r, x, b, d, m, g.n1, g.n2, lin(g, q.i, q.j, q.k));
 }
 
 // residual of the 2D 9-point extension, interior box.
@@ -212,13 +111,7 @@ __global__ void __launch_bounds__(kThreads) k_resid9_2d(T* __restrict__ r, const
                                                         const T* __restrict__ b, const T* __restrict__ d,
                                                         const uint8_t* __restrict__ m, Geom g, Box bx) {
   BoxIdx q = box_idx(bx);
-  if (!q.ok) return;
-  typedef Ar<T> A;
-  long long I = lin(g, q.i, q.j, q.k);
-  T v = A::add(A::mul(d[I], x[I]), b[I]);
-  v = A::fmx(faces4(x, I, g.n1), T(-0.5), v);
-  v = A::fmx(diags4(x, I, g.n1), T(-0.25), v);
-  r[I] = mask_mul(m[I], v);
+  if (q.ok) d_resid9(r, x, b, d, m, g.n1, lin(g, q.i, q.j, q.k));
 }
 
 // residual_laplacian9! (src/laplacian9.jl:49-73), interior box.
@@ -227,13 +120,7 @@ __global__ void __launch_bounds__(kThreads) k_resid19_3d(T* __restrict__ r, cons
                                                          const T* __restrict__ b, const T* __restrict__ d,
                                                          const uint8_t* __restrict__ m, Geom g, Box bx) {
   BoxIdx q = box_idx(bx);
-  if (!q.ok) return;
-  typedef Ar<T> A;
-  long long I = lin(g, q.i, q.j, q.k);
-  T v = A::add(A::mul(d[I], x[I]), b[I]);
-  v = A::fmx(faces6(x, I, g.n1, g.n2), T(-0.5), v);
-  v = A::fmx(edges12(x, I, g.n1, g.n2), T(-0.25), v);
-  r[I] = mask_mul(m[I], v);
+  if (q.ok) d_resid19(r, x, b, d, m, g.n1, g.n2, lin(g, q.i, q.j, q.k));
 }
 
 template <class T>
@@ -243,81 +130,20 @@ __global__ void __launch_bounds__(kThreads) k_resid_vc_2d(T* __restrict__ r, con
                                                           const uint8_t* __restrict__ m, long long n1, long long lo,
                                                           long long hi) {
   long long I = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (I >= hi) return;
-  typedef Ar<T> A;
-  T s = vc_sum(x, cE, cN, I, n1);
-  r[I] = mask_mul(m[I], A::sub(A::add(A::mul(d[I], x[I]), b[I]), s));
+  if (I < hi) d_residvc(r, x, b, d, cE, cN, m, n1, I);
 }
 
 // ------------------------------------------------------------ restriction
-__device__ __forceinline__ int c2f(int i, int nh) { return (i - nh - 1) * 2 + nh + 1; }  // src/gmg_types.jl:25
 
 // Thread per coarse interior cell (ii, jj, kk); the coarse b is written.
 template <class T, int KIND>
 __global__ void __launch_bounds__(kThreads) k_restrict(const T* __restrict__ x, T* __restrict__ xc,
                                                        const T* __restrict__ coef, Geom gf, Geom gc, Box cb) {
   BoxIdx q = box_idx(cb);
-  if (!q.ok) return;
-  typedef Ar<T> A;
-  const int nh = gc.nh;
-  const int i = c2f(q.i, nh), j = c2f(q.j, nh);
-  const long long n1 = gf.n1, n2 = gf.n2;
-  T s;
-  if (KIND == 0) {  // rcloop2d! (src/RP_on_centers.jl:117-133)
-    long long F = lin(gf, i, j, q.k);
-    s = A::add(A::add(A::add(x[F], x[F + 1]), x[F + n1]), x[F + 1 + n1]);
-  } else if (KIND == 1) {  // rcloop3d! (src/RP_on_centers.jl:5-23)
-    long long F = lin(gf, i, j, c2f(q.k, nh));
-    s = A::add(x[F], x[F + 1]);
-    s = A::add(s, x[F + n1]);
-    s = A::add(s, x[F + 1 + n1]);
-    s = A::add(s, x[F + n2]);
-    s = A::add(s, x[F + 1 + n2]);
-    s = A::add(s, x[F + n1 + n2]);
-    s = A::add(s, x[F + 1 + n1 + n2]);
-  } else if (KIND == 2) {  // rvloop2d! (src/RP_on_vertices.jl:96-115): 1-2-1 x 1-2-1
-    long long F = lin(gf, i, j, q.k);
-    s = A::fmx(x[F - n1], T(2), x[F - 1 - n1]);
-    s = A::add(s, x[F + 1 - n1]);
-    s = A::fmx(x[F - 1], T(2), s);
-    s = A::fmx(x[F], T(4), s);
-    s = A::fmx(x[F + 1], T(2), s);
-    s = A::add(s, x[F - 1 + n1]);
-    s = A::fmx(x[F + n1], T(2), s);
-    s = A::add(s, x[F + 1 + n1]);
-  } else {  // restriction_vertices! (src/RP_on_vertices.jl:1-32): 27 points, 1-2-4-8
-    long long F = lin(gf, i, j, c2f(q.k, nh));
-    bool first = true;
-    s = T(0);
-#pragma unroll
-    for (int dk = -1; dk <= 1; ++dk)
-#pragma unroll
-      for (int dj = -1; dj <= 1; ++dj)
-#pragma unroll
-        for (int di = -1; di <= 1; ++di) {
-          const int w = (2 - (di < 0 ? -di : di)) * (2 - (dj < 0 ? -dj : dj)) * (2 - (dk < 0 ? -dk : dk));
-          T v = x[F + di + dj * n1 + dk * n2];
-          if (first) {
-            s = (w == 1) ? v : A::mul(T(w), v);
-            first = false;
-          } else {
-            s = (w == 1) ? A::add(s, v) : A::fmx(v, T(w), s);
-          }
-        }
-  }
-  long long C = lin(gc, q.i, q.j, q.k);
-  xc[C] = A::mul(coef[C], s);
+  if (q.ok) d_restrict<T, KIND>(x, xc, coef, gf, gc, q.i, q.j, q.k);
 }
 
 // ----------------------------------------------------------- prolongation
-__device__ __forceinline__ int f2c(int i, int nh) { return (i - nh - 1) / 2 + nh + 1; }  // src/gmg_types.jl:26
-
-// square (src/RP_on_centers.jl:1-3): 3*(x[i+di,j,k+dk]+x[i,j+dj,k+dk]) + x[i+di,j+dj,k+dk]
-template <class T>
-__device__ __forceinline__ T square3(const T* x, long long C, long long di, long long dj, long long dk) {
-  typedef Ar<T> A;
-  return A::add(A::mul(T(3), A::add(x[C + di + dk], x[C + dj + dk])), x[C + di + dj + dk]);
-}
 
 // Thread per fine parent (i, j, k) = (nh+1+2p, nh+1+2q, ...); each parent
 // updates its 4 (2D) or 8 (3D) children, which no other thread touches.
@@ -328,101 +154,17 @@ __global__ void __launch_bounds__(kThreads) k_prolong(T* __restrict__ xf, const 
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const int qj = blockIdx.y * blockDim.y + threadIdx.y;
   const int qk = blockIdx.z;
-  if (p >= np_i || qj >= np_j) return;
-  typedef Ar<T> A;
-  const int nh = gf.nh;
-  const int i = nh + 1 + 2 * p, j = nh + 1 + 2 * qj;
-  const int ic = f2c(i, nh), jc = f2c(j, nh);
-  const long long c1 = gc.n1, c2 = gc.n2, f1 = gf.n1, f2 = gf.n2;
-  if (KIND == 0) {  // pcloop2d! (src/RP_on_centers.jl:146-163)
-    const int k = kf0 + qk;
-    if (k > kf1) return;
-    const long long C = lin(gc, ic, jc, k), F = lin(gf, i, j, k);
-    const T x9 = A::mul(x[C], T(9));
-#pragma unroll
-    for (int dj = 0; dj <= 1; ++dj)
-#pragma unroll
-      for (int di = 0; di <= 1; ++di) {
-        T bb = square3(x, C, (long long)(2 * di - 1), (2 * dj - 1) * c1, 0LL);
-        long long Fi = F + di + dj * f1;
-        xf[Fi] = A::add(xf[Fi], A::mul(coef[Fi], A::add(bb, x9)));
-      }
-  } else if (KIND == 1) {  // pcloop3d! (src/RP_on_centers.jl:84-104)
-    if (qk >= np_k) return;
-    const int k = nh + 1 + 2 * qk;
-    const int kc = f2c(k, nh);
-    const long long C = lin(gc, ic, jc, kc), F = lin(gf, i, j, k);
-    const T x28 = A::mul(x[C], T(28));
-#pragma unroll
-    for (int dj = 0; dj <= 1; ++dj)
-#pragma unroll
-      for (int di = 0; di <= 1; ++di) {
-        const long long ddi = 2 * di - 1, ddj = (2 * dj - 1) * c1;
-        T a = square3(x, C, ddi, ddj, -c2);
-        T bb = A::mul(square3(x, C, ddi, ddj, 0LL), T(3));
-        T c = square3(x, C, ddi, ddj, c2);
-        long long F0 = F + di + dj * f1, F1 = F0 + f2;
-        xf[F0] = A::add(xf[F0], A::mul(coef[F0], A::add(A::add(bb, a), x28)));
-        xf[F1] = A::add(xf[F1], A::mul(coef[F1], A::add(A::add(bb, c), x28)));
-      }
-  } else if (KIND == 2) {  // pvloop2d! (src/RP_on_vertices.jl:117-137)
-    const int k = kf0 + qk;
-    if (k > kf1) return;
-    const long long C = lin(gc, ic, jc, k), F = lin(gf, i, j, k);
-    const T x00 = x[C], x10 = x[C + 1], x01 = x[C + c1], x11 = x[C + 1 + c1];
-    xf[F] = A::add(xf[F], A::mul(coef[F], x00));
-    xf[F + 1] = A::add(xf[F + 1], A::mul(coef[F + 1], A::add(x00, x10)));
-    xf[F + f1] = A::add(xf[F + f1], A::mul(coef[F + f1], A::add(x00, x01)));
-    xf[F + 1 + f1] = A::add(xf[F + 1 + f1], A::mul(coef[F + 1 + f1], A::add(A::add(A::add(x00, x10), x01), x11)));
-  } else {  // prolongation_vertices! (src/RP_on_vertices.jl:34-72)
-    if (qk >= np_k) return;
-    const int k = nh + 1 + 2 * qk;
-    const int kc = f2c(k, nh);
-    const long long C = lin(gc, ic, jc, kc), F = lin(gf, i, j, k);
-    const T x000 = x[C], x100 = x[C + 1], x010 = x[C + c1], x001 = x[C + c2];
-    const T x110 = x[C + 1 + c1], x101 = x[C + 1 + c2], x011 = x[C + c1 + c2], x111 = x[C + 1 + c1 + c2];
-    auto upd = [&](long long Fi, T v) { xf[Fi] = A::add(xf[Fi], A::mul(coef[Fi], v)); };
-    upd(F, x000);
-    upd(F + 1, A::add(x000, x100));
-    upd(F + f1, A::add(x000, x010));
-    upd(F + f2, A::add(x000, x001));
-    upd(F + 1 + f1, A::add(A::add(A::add(x000, x100), x010), x110));
-    upd(F + 1 + f2, A::add(A::add(A::add(x000, x100), x001), x101));
-    upd(F + f1 + f2, A::add(A::add(A::add(x000, x001), x010), x011));
-    T s = A::add(x000, x100);
-    s = A::add(s, x001);
-    s = A::add(s, x101);
-    s = A::add(s, x010);
-    s = A::add(s, x110);
-    s = A::add(s, x011);
-    s = A::add(s, x111);
-    upd(F + 1 + f1 + f2, s);
-  }
+  if (p < np_i && qj < np_j && qk < np_k) d_prolong<T, KIND>(xf, x, coef, gf, gc, p, qj, qk, kf0);
 }
 
 // ------------------------------------------------------------------- halo
 // fill! for :xperio (src/halo.jl:6-9). One thread per (j,k) line copies the
 // nh columns through registers, so the copies of each statement read
 // before they write, as Julia's sliced assignment does.
-constexpr int kMaxNh = 8;
 template <class T>
 __global__ void __launch_bounds__(kThreads) k_fill_xperio(T* __restrict__ x, int tx, int nh, long long nlines) {
   long long L = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (L >= nlines) return;
-  T* row = x + L * tx;
-  T tmp[kMaxNh];
-#pragma unroll
-  for (int i = 0; i < kMaxNh; ++i)
-    if (i < nh) tmp[i] = row[tx - 2 * nh + i];  // x[end+1-2nh : end-nh]
-#pragma unroll
-  for (int i = 0; i < kMaxNh; ++i)
-    if (i < nh) row[i] = tmp[i];  // -> x[1:nh]
-#pragma unroll
-  for (int i = 0; i < kMaxNh; ++i)
-    if (i < nh) tmp[i] = row[nh + i];  // x[nh+1 : 2nh]
-#pragma unroll
-  for (int i = 0; i < kMaxNh; ++i)
-    if (i < nh) row[tx - nh + i] = tmp[i];  // -> x[end+1-nh : end]
+  if (L < nlines) d_fill_line(x + L * tx, tx, nh);
 }
 
 // ------------------------------------------------------------------- norm
@@ -606,5 +348,74 @@ void launch_norm(const T* x, const uint8_t* m, size_t n, double* partials, doubl
 CFMG_INST(double)
 CFMG_INST(float)
 template void launch_fill_xperio<uint8_t>(uint8_t*, const Geom&, cudaStream_t);
+
+}  // namespace cfmg
+
+namespace cfmg {
+
+__global__ void k_f32_to_f64(const float* a, double* out, long long n) {
+  long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I < n) out[I] = (double)a[I];
+}
+__global__ void k_f64_to_f32(const double* a, float* out, long long n) {
+  long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I < n) out[I] = (float)a[I];
+}
+
+// One Op as a standalone kernel (fine levels).
+template <class T>
+static void launch_op_t(const Op& op, cudaStream_t s) {
+  const T* x = (const T*)op.x;
+  const T* b = (const T*)op.b;
+  const T* w = (const T*)op.w;
+  const T* d = (const T*)op.d;
+  T* y = (T*)op.y;
+  const T cff = (T)op.cff;
+  switch (op.kind) {
+    case OPK_SWEEP5: launch_sweep5_2d<T>(x, y, b, w, cff, op.g, s); break;
+    case OPK_SWEEP7: launch_sweep7_3d<T>(x, y, b, w, cff, op.g, s); break;
+    case OPK_SWEEP9: launch_sweep9_2d<T>(x, y, b, w, cff, op.g, op.box, s); break;
+    case OPK_SWEEP19: launch_sweep19_3d<T>(x, y, b, w, cff, op.g, op.box, s); break;
+    case OPK_SWEEPVC: launch_sweep_vc_2d<T>(x, y, b, w, (const T*)op.cE, (const T*)op.cN, cff, op.g, s); break;
+    case OPK_RESID5: launch_resid5_2d<T>(y, x, b, d, op.m, op.g, s); break;
+    case OPK_RESID7: launch_resid7_3d<T>(y, x, b, d, op.m, op.g, op.box, s); break;
+    case OPK_RESID9: launch_resid9_2d<T>(y, x, b, d, op.m, op.g, op.box, s); break;
+    case OPK_RESID19: launch_resid19_3d<T>(y, x, b, d, op.m, op.g, op.box, s); break;
+    case OPK_RESIDVC: launch_resid_vc_2d<T>(y, x, b, d, (const T*)op.cE, (const T*)op.cN, op.m, op.g, s); break;
+    case OPK_RESTRICT0:
+    case OPK_RESTRICT1:
+    case OPK_RESTRICT2:
+    case OPK_RESTRICT3:
+      launch_restrict<T>(op.kind - OPK_RESTRICT0, x, y, (const T*)op.coef, op.g, op.gc, op.box, s);
+      break;
+    case OPK_PROLONG0:
+    case OPK_PROLONG1:
+    case OPK_PROLONG2:
+    case OPK_PROLONG3: {
+      const int kind = op.kind - OPK_PROLONG0;
+      const bool t3 = (kind == 1 || kind == 3);
+      // launch_prolong derives the parent counts from (nx, ny, nz) of the fine level
+      launch_prolong<T>(kind, y, x, (const T*)op.coef, op.g, op.gc, 2 * op.np_i, 2 * op.np_j,
+                        t3 ? 2 * (op.kf1 - op.kf0 + 1) : 1, op.kf0, op.kf1, s);
+      break;
+    }
+    case OPK_FILL: launch_fill_xperio<T>(y, op.g, s); break;
+    case OPK_ZERO: cudaMemsetAsync(y, 0, op.n * sizeof(T), s); break;
+    default: break;
+  }
+}
+
+void launch_op(const Op& op, cudaStream_t s) {
+  if (op.kind == OPK_F32TO64) {
+    k_f32_to_f64<<<nblocks(op.n), kThreads, 0, s>>>((const float*)op.x, (double*)op.y, op.n);
+    return;
+  }
+  if (op.kind == OPK_F64TO32) {
+    k_f64_to_f32<<<nblocks(op.n), kThreads, 0, s>>>((const double*)op.x, (float*)op.y, op.n);
+    return;
+  }
+  if (op.prec == 0) launch_op_t<double>(op, s);
+  else launch_op_t<float>(op, s);
+}
 
 }  // namespace cfmg

@@ -91,6 +91,11 @@ extern "C" {
 #define CFMG_K_NORM 4
 #define CFMG_K_FILL 5
 #define CFMG_K_CONVERT 6  /* FP64 <-> FP32 transfers of the mixed form */
+#define CFMG_K_ENGINE 7   /* one launch of the coarse-level program engine */
+
+/* options for cfmg_set_option */
+#define CFMG_OPT_ENGINE_CELLS 0 /* levels of at most this many cells (tx*ty*tz) run in the
+                                   coarse-level engine; 0 turns the engine off (default 80000) */
 
 typedef struct cfmg_desc {
   int kase;     /* CFMG_TWOD / CFMG_THREED            (Param.case) */
@@ -174,6 +179,8 @@ CFMG_API int cfmg_solve(cfmg_handle* h, double* res, int* nite, double* history)
  * launches eagerly instead of replaying its graph. cfmg_profile_read
  * returns the number of bracketed launches and their summed device time. */
 CFMG_API int cfmg_launch_count(const cfmg_handle* h, long long* n);
+/* Tuning knobs (CFMG_OPT_*); no counterpart in the reference. */
+CFMG_API int cfmg_set_option(cfmg_handle* h, int option, long long value);
 CFMG_API int cfmg_profile(cfmg_handle* h, int cls, int lev, int precision);
 CFMG_API int cfmg_profile_read(cfmg_handle* h, long long* launches, double* total_ms);
 

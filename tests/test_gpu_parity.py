@@ -124,9 +124,13 @@ def _compare_all(og, mg, what):
             assert np.array_equal(a, b), (what, lev, f, np.nanmax(np.abs(a - b)))
 
 
+@pytest.mark.parametrize("engine", ["engine", "standalone"])
 @pytest.mark.parametrize("name", sorted(CONFIGS))
-def test_operators_bitwise(name):
+def test_operators_bitwise(name, engine):
     og, mg = _setup_pair(name)
+    # small levels run in the coarse-level program engine by default; the
+    # standalone variant launches every operator as its own kernel
+    mg.set_option("engine_cells", 10**9 if engine == "engine" else 0)
     rng = np.random.default_rng(1)
     _random_state(og, mg, rng)
     L = og.nlevels
@@ -154,9 +158,11 @@ def test_operators_bitwise(name):
         assert abs(a - b) <= 1e-13 * abs(a), (f, a, b)
 
 
+@pytest.mark.parametrize("engine_cells", [0, 400, 10**9])
 @pytest.mark.parametrize("kind", ["v", "f", "onelev", "twolev", "nlev", "vrec"])
-def test_cycles_bitwise(kind):
+def test_cycles_bitwise(kind, engine_cells):
     og, mg = _setup_pair("2d_centers")
+    mg.set_option("engine_cells", engine_cells)  # none / the coarsest levels / all levels in the engine
     rng = np.random.default_rng(2)
     _random_state(og, mg, rng)
     og.cycle(kind)
