@@ -60,6 +60,15 @@ namespace {
 std::mutex g_err_mu;
 std::string g_create_err;
 
+}  // namespace
+
+void cfmg::set_global_error(const std::string& msg) {
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_create_err = msg;
+}
+
+namespace {
+
 int fail(cfmg_handle* h, int code, const std::string& msg) {
   if (h) h->err = msg;
   else {

@@ -130,6 +130,9 @@ constexpr int kEngineThreads = 1024;
 void launch_op(const Op& op, cudaStream_t s);                   // one Op as a standalone kernel
 void launch_program(const Op* prog, int nops, cudaStream_t s);  // a device-resident program
 
+// message returned by cfmg_last_error(NULL) (cfmg_api.cu)
+void set_global_error(const std::string& msg);
+
 // ---- setup kernels (k_setup.cu)
 enum DefMskMode { DEFMSK_SET = 0, DEFMSK_MUL = 1, DEFMSK_SCALE_F64 = 2 };
 void launch_default_msk(int mode, uint8_t* msk, double* f, double coef, const Level& l, bool vertices, bool threed,

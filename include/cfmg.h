@@ -184,6 +184,24 @@ CFMG_API int cfmg_set_option(cfmg_handle* h, int option, long long value);
 CFMG_API int cfmg_profile(cfmg_handle* h, int cls, int lev, int precision);
 CFMG_API int cfmg_profile_read(cfmg_handle* h, long long* launches, double* total_ms);
 
+/* Masked norm without allocation. No counterpart in the reference.
+ * For callers that cannot allocate device memory where they need the
+ * reduction: an application whose device pool belongs to another allocator
+ * (a Julia CuArray or PyTorch caching pool), or a deployment with a fixed
+ * device-memory budget. Computes sum(msk[i]*x[i]^2) over n elements of
+ * caller-owned device arrays (0 -> 1, as the reference's norm,
+ * src/operators_at_level.jl:12-27) into out[0], a device or mapped host
+ * address, asynchronously on `stream` (a cudaStream_t; NULL = legacy).
+ * Its scratch is a static device array of 4096 doubles (32 KB) held on every
+ * GPU that loads the library; n is limited to CFMG_NOALLOC_MAX_ELEMS and
+ * larger n is rejected with CFMG_ERR_ARG. The first call on a device looks
+ * up that array's device address; make it before any stream capture.
+ * Calls that overlap on the GPU race on the shared scratch. No cudaMalloc,
+ * cudaFree or allocating library routine is called. Errors:
+ * cfmg_last_error(NULL). */
+#define CFMG_NOALLOC_MAX_ELEMS 268435456LL
+CFMG_API int cfmg_norm_noalloc(const double* x, const uint8_t* msk, long long n, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
