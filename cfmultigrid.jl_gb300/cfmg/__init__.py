@@ -32,7 +32,7 @@ from . import _lib
 from ._lib import CASES, CYCLES, FIELDS, LOCATIONS, NORMS, OPERATORS, PRECISIONS, TOPOLOGIES
 
 __all__ = ["Param", "Gmg", "CfmgError", "get_gmg", "solve", "setup_operators", "vcycle", "fcycle", "fill",
-           "norm", "normresidual", "set_to_zero", "set_default_msk"]
+           "norm", "normresidual", "set_to_zero", "set_default_msk", "adjoint", "loss_and_grad"]
 
 
 class CfmgError(RuntimeError):
@@ -347,3 +347,52 @@ def solve(mg: Gmg, history: bool = False):
     if history:
         return res.value, nite.value, np.array(hist[: nite.value + 1])
     return res.value, nite.value
+
+
+def adjoint(mg: Gmg, g):
+    """Backward pass of ``solve(mg)`` (the body of a ChainRulesCore rrule on a
+    Julia host): with the cotangent g = dL/dx of level 1, returns
+    (dL/db, dL/dkappa); dL/dkappa is None unless the operator is "varcoef".
+    Needs a preceding forward ``solve(mg)``; the forward x and b are kept."""
+    shape = mg.shape(1)
+    ga = np.asfortranarray(np.asarray(g, dtype=np.float64).reshape(shape, order="F"))
+    gb = np.empty(shape, dtype=np.float64, order="F")
+    vc = mg.param.operator == "varcoef"
+    gk = np.empty(shape, dtype=np.float64, order="F") if vc else None
+    res = ctypes.c_double()
+    nite = ctypes.c_int()
+    mg._check(mg._L.cfmg_adjoint(mg._h, ga.ctypes.data_as(ctypes.c_void_p), gb.ctypes.data_as(ctypes.c_void_p),
+                                 gk.ctypes.data_as(ctypes.c_void_p) if vc else None, ctypes.byref(res),
+                                 ctypes.byref(nite)))
+    return gb, gk
+
+
+def _wet_mean_removed(x, msk):
+    w = msk.astype(bool)
+    y = np.where(w, x, 0.0)
+    if w.any():
+        y[w] -= y[w].mean()
+    return y
+
+
+def loss_and_grad(mg: Gmg, b, xstar, kappa=None):
+    """L = 1/2 sum_wet (P x - x*)^2 with A(kappa) x = b and P the wet-mean
+    projection (cell-centred) or the mask (vertex-centred); returns
+    (L, dL/db, dL/dkappa) from one forward and one adjoint solve."""
+    if kappa is not None:
+        mg.oper[1].kappa = kappa
+        setup_operators(mg)
+        for lev in range(1, mg.nlevels + 1):
+            for f in ("x", "y", "r", "b"):
+                set_to_zero(mg, lev, f)
+    msk = mg.download(1, "msk")
+    mg.data[1].b = b
+    set_to_zero(mg, 1, "x")
+    solve(mg)
+    x = mg.data[1].x
+    neumann = mg.param.location == "centers"
+    px = _wet_mean_removed(x, msk) if neumann else x * msk
+    d = (px - xstar) * msk
+    loss = 0.5 * float(np.sum(d * d))
+    gb, gk = adjoint(mg, d)
+    return loss, gb, gk

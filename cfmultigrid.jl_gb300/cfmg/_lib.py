@@ -33,8 +33,9 @@ EXPORTS = (
     "cfmg_set_default_msk", "cfmg_setup_operators", "cfmg_smooth", "cfmg_residual", "cfmg_restrict",
     "cfmg_prolong", "cfmg_zero", "cfmg_fill", "cfmg_norm", "cfmg_normresidual", "cfmg_cycle", "cfmg_solve",
     "cfmg_launch_count", "cfmg_profile", "cfmg_profile_read", "cfmg_set_option", "cfmg_norm_noalloc",
+    "cfmg_adjoint",
 )
-OPTIONS = {"engine_cells": 0}
+OPTIONS = {"engine_cells": 0, "temporal_blocking": 1}
 KERNEL_CLASSES = {"sweep": 0, "residual": 1, "restrict": 2, "prolong": 3, "norm": 4, "fill": 5, "convert": 6,
                   "engine": 7}
 
@@ -95,6 +96,7 @@ def load() -> ctypes.CDLL:
         "cfmg_profile_read": [vp, ctypes.POINTER(ctypes.c_longlong), pd],
         "cfmg_set_option": [vp, i, ctypes.c_longlong],
         "cfmg_norm_noalloc": [vp, vp, ctypes.c_longlong, vp, vp],
+        "cfmg_adjoint": [vp, vp, vp, vp, pd, pi],
     }
     for name, args in sig.items():
         f = getattr(L, name)

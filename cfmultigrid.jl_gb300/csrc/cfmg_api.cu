@@ -48,6 +48,10 @@ struct cfmg_handle {
   cfmg::Op* prog_pool = nullptr;   // device program store
   int pool_cap = 0, pool_used = 0;
   std::unordered_map<std::string, int> prog_cache;
+  bool tb_on = true;  // temporally blocked FP32 smoothing on fine levels
+  // adjoint scratch (level-1 FP64 arrays, allocated on the first cfmg_adjoint)
+  double *adj_x = nullptr, *adj_b = nullptr, *adj_gk = nullptr;
+  bool record = false;  // emit() records every Op (whole-solve programs) instead of running it
 };
 
 constexpr int kProgPoolOps = 8192;  // device store of engine programs (~1.9 MB)
@@ -174,7 +178,9 @@ View<double> view<double>(const Level& l) {
 }
 template <>
 View<float> view<float>(const Level& l) {
-  return View<float>{l.x32, l.y32, l.r32, l.b32, l.diag32, l.widiag32, l.Rcoef32, l.Pcoef32, l.cE32, l.cN32, l.msk};
+  float* xs = l.xswap ? l.y32 : l.x32;  // the FP32 x and its partner buffer
+  float* ys = l.xswap ? l.x32 : l.y32;
+  return View<float>{xs, ys, l.r32, l.b32, l.diag32, l.widiag32, l.Rcoef32, l.Pcoef32, l.cE32, l.cN32, l.msk};
 }
 
 template <class T>
@@ -212,7 +218,7 @@ long long box_count(const Box& b) {
 }
 
 int flush(cfmg_handle* h) {
-  if (h->pending.empty()) return CFMG_OK;
+  if (h->record || h->pending.empty()) return CFMG_OK;
   const int n = (int)h->pending.size();
   std::string key((const char*)h->pending.data(), (size_t)n * sizeof(Op));
   auto it = h->prog_cache.find(key);
@@ -230,7 +236,7 @@ int flush(cfmg_handle* h) {
   }
   if (off >= 0) {
     Launch k(h, CFMG_K_ENGINE, 0, h->pending[0].prec ? CFMG_MIXED : CFMG_FP64);
-    launch_program(h->prog_pool + off, n, h->stream);
+    launch_program(h->prog_pool + off, n, h->partials, h->stream);
   } else {  // pool full: run the Ops one by one
     for (const Op& op : h->pending) {
       Launch k(h, op.cls, op.lev, op.prec ? CFMG_MIXED : CFMG_FP64);
@@ -242,10 +248,18 @@ int flush(cfmg_handle* h) {
   return CFMG_OK;
 }
 
+// The engine's 8 SMs give about 1/19 of the GPU's FP64 rate, which suits
+// only small FP64 levels; FP32 levels up to engine_cells cells go there.
+long long engine_limit(const cfmg_handle* h, int prec) { return prec == 0 ? h->engine_cells / 16 : h->engine_cells; }
+
 int emit(cfmg_handle* h, const Op& op) {
   if (op.n <= 0) return CFMG_OK;
+  if (h->record) {
+    h->pending.push_back(op);
+    return CFMG_OK;
+  }
   const Level& l = h->lv[op.lev - 1];
-  if (h->engine_on && (long long)l.len <= h->engine_cells) {
+  if (h->engine_on && (long long)l.len <= engine_limit(h, op.prec)) {
     h->pending.push_back(op);
     return CFMG_OK;
   }
@@ -289,9 +303,39 @@ int sweep(cfmg_handle* h, int lev, int kind, const T* x, T* y, const Box* bx) {
   return emit(h, op);
 }
 
+// FP32 smoothing of a fine level in temporally blocked passes (closed
+// topology, 2D 5- and 9-point): the result goes to the partner buffer.
+template <class T>
+bool tb_eligible(const cfmg_handle* h, int lev) {
+  if (sizeof(T) != 4 || !h->tb_on || h->record || xperio(h) || threed(h)) return false;
+  if (h->d.op != CFMG_LAPLACIAN && h->d.op != CFMG_LAPLACIAN9) return false;
+  const Level& l = h->lv[lev - 1];
+  return !(h->engine_on && (long long)l.len <= engine_limit(h, CFMG_MIXED));
+}
+
+int smooth_tb(cfmg_handle* h, int lev, int nite) {
+  Level& l = h->lv[lev - 1];
+  const int stencil = h->d.op == CFMG_LAPLACIAN9 ? 9 : 5;
+  TRY(flush(h));
+  for (int left = nite; left > 0;) {
+    const int n = left > 3 ? 3 : left;
+    View<float> v = view<float>(l);
+    {
+      Launch k(h, CFMG_K_SWEEP, lev, CFMG_MIXED);
+      launch_smooth_tb(stencil, n, v.x, v.y, v.b, v.widiag, (float)(1.0 - h->d.omega), l.tx, l.ty, l.tz, l.nh,
+                       l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, h->stream);
+    }
+    l.xswap ^= 1;
+    left -= n;
+  }
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
 // mg.smoother[lev] (src/gmg_setup.jl:124-139 selects among these)
 template <class T>
 int smooth_t(cfmg_handle* h, int lev, int nite) {
+  if (tb_eligible<T>(h, lev)) return smooth_tb(h, lev, nite);
   const Level& l = h->lv[lev - 1];
   View<T> v = view<T>(l);
   if (h->d.op == CFMG_LAPLACIAN9 && threed(h)) {
@@ -418,15 +462,16 @@ int coarsest_t<float>(cfmg_handle* h, int nite) {
   if (L(h) == 1) return smooth_t<float>(h, 1, nite);
   const int lev = L(h);
   const Level& c = h->lv[lev - 1];
+  View<float> v = view<float>(c);
   Op op = mkop(OPK_F32TO64, 1, lev, CFMG_K_CONVERT, c);
   op.n = (long long)c.len;
-  op.x = c.b32; op.y = c.b;
+  op.x = v.b; op.y = c.b;
   TRY(emit(h, op));
-  op.x = c.x32; op.y = c.x;
+  op.x = v.x; op.y = c.x;
   TRY(emit(h, op));
   TRY(smooth_t<double>(h, lev, nite));
   op.kind = OPK_F64TO32;
-  op.x = c.x; op.y = c.x32;
+  op.x = c.x; op.y = v.x;
   return emit(h, op);
 }
 
@@ -691,7 +736,68 @@ __global__ void k_update(double* x, const float* e, const double* dscal, long lo
   x[I] = __fma_rn((double)e[I], dscal[S_ISCALE], x[I]);
 }
 
+// ------------------------------------------------------------- adjoint
+// wet-mean removal: x -= (sum msk x)/(sum msk) on wet cells, the sum in
+// Neumaier-compensated FP64 (k_mean_partial above) with a fixed-order final
+__global__ void k_mean_final(const double* partials, int nparts, double* dscal) {
+  __shared__ double sh[kNormParts];
+  sh[threadIdx.x] = (int)threadIdx.x < nparts ? partials[threadIdx.x] : 0.0;
+  __syncthreads();
+  for (int w = kNormParts / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) dscal[S_MEAN] = dscal[S_NWET] > 0 ? sh[0] / dscal[S_NWET] : 0.0;
+}
+__global__ void k_sub_mean(double* x, const uint8_t* m, const double* dscal, long long n) {
+  long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= n) return;
+  x[I] = m[I] ? x[I] - dscal[S_MEAN] : 0.0;
+}
+
+// dL/dkappa_k = sum over the faces of k with both cells wet of
+// 1/2 (lam_k - lam_nb)(x_k - x_nb): the face coefficient (kappa_k+kappa_nb)/2
+// enters A as c_f (x_nb - x_k) in both rows, so dL/dc_f = (lam_i-lam_j)(x_i-x_j).
+__global__ void k_kappa_grad(const double* lam, const double* x, const uint8_t* m, double* gk, long long n1,
+                             long long n) {
+  long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= n) return;
+  double s = 0.0;
+  if (m[I]) {
+    const long long nb[4] = {I - 1, I + 1, I - n1, I + n1};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const long long J = nb[q];
+      if (J >= 0 && J < n && m[J]) s += 0.5 * (lam[I] - lam[J]) * (x[I] - x[J]);
+    }
+  }
+  gk[I] = s;
+}
+
+int count_wet(cfmg_handle* h) {
+  const Level& l1 = h->lv[0];
+  launch_fill_f64(l1.y, 1.0, l1.len, h->stream);
+  launch_norm<double>(l1.y, l1.msk, l1.len, h->partials, h->dscal + S_TMP0, nullptr, CFMG_NORM_L2, h->stream);
+  CUDA_OK(h, cudaMemcpyAsync(h->dscal + S_NWET, h->dscal + S_TMP0, sizeof(double), cudaMemcpyDeviceToDevice,
+                             h->stream));
+  CUDA_OK(h, cudaMemsetAsync(l1.y, 0, l1.len * sizeof(double), h->stream));
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
+int remove_wet_mean(cfmg_handle* h, double* x) {
+  const Level& l1 = h->lv[0];
+  const long long n = (long long)l1.len;
+  k_mean_partial<<<kNormParts, 256, 0, h->stream>>>(x, l1.msk, n, h->partials);
+  k_mean_final<<<1, kNormParts, 0, h->stream>>>(h->partials, kNormParts, h->dscal);
+  k_sub_mean<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(x, l1.msk, h->dscal, n);
+  h->launches += 3;
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
 int mixed_iteration(cfmg_handle* h, int kind) {
+  for (Level& l : h->lv) l.xswap = 0;  // every FP32 x is zeroed before use in the cycle
   const Level& l1 = h->lv[0];
   const long long n = (long long)l1.len;
   const unsigned nb = (unsigned)((n + 255) / 256);
@@ -708,7 +814,7 @@ int mixed_iteration(cfmg_handle* h, int kind) {
   TRY(cycle_t<float>(h, kind));
   {
     Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED);
-    k_update<<<nb, 256, 0, h->stream>>>(l1.x, l1.x32, h->dscal, n);
+    k_update<<<nb, 256, 0, h->stream>>>(l1.x, view<float>(l1).x, h->dscal, n);
   }
   LAUNCH_OK(h);
   return CFMG_OK;
@@ -843,10 +949,15 @@ int cfmg_desc_default(cfmg_desc* d) {
   return CFMG_OK;
 }
 
-int cfmg_create(const cfmg_desc* d, cfmg_handle** out) {
+}  // extern "C"
+
+// A handle. `shared` (batch instances) puts it on a caller's stream without
+// a program store of its own.
+static int create_handle(const cfmg_desc* d, cudaStream_t shared, cfmg_handle** out) {
   if (!out) return fail(nullptr, CFMG_ERR_ARG, "null output pointer");
   *out = nullptr;
   TRY(validate(d));
+  const int pool_ops = shared ? 0 : kProgPoolOps;
   cfmg_handle* h = new cfmg_handle();
   h->d = *d;
   h->lv = create_levels(*d);
@@ -858,7 +969,7 @@ int cfmg_create(const cfmg_desc* d, cfmg_handle** out) {
   const bool mixed = d->precision == CFMG_MIXED;
   const bool vc = d->op == CFMG_VARCOEF;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  size_t total = al(kNormParts * sizeof(double)) + al(S_COUNT * sizeof(double)) + al((size_t)kProgPoolOps * sizeof(Op));
+  size_t total = al(kNormParts * sizeof(double)) + al(S_COUNT * sizeof(double)) + al((size_t)pool_ops * sizeof(Op));
   for (const Level& l : h->lv) {
     size_t n = l.len;
     total += 8 * al(n * 8) + al(n);           // x y r b diag idiag widiag Rcoef Pcoef + msk (Pcoef counted below)
@@ -880,8 +991,8 @@ int cfmg_create(const cfmg_desc* d, cfmg_handle** out) {
     return q;
   };
   h->partials = (double*)take(kNormParts * sizeof(double));
-  h->prog_pool = (Op*)take((size_t)kProgPoolOps * sizeof(Op));
-  h->pool_cap = kProgPoolOps;
+  h->prog_pool = (Op*)take((size_t)pool_ops * sizeof(Op));
+  h->pool_cap = pool_ops;
   h->dscal = (double*)take(S_COUNT * sizeof(double));
   for (Level& l : h->lv) {
     size_t n = l.len;
@@ -897,13 +1008,13 @@ int cfmg_create(const cfmg_desc* d, cfmg_handle** out) {
       if (vc) { l.cE32 = (float*)take(n * 4); l.cN32 = (float*)take(n * 4); }
     }
   }
-  if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+  if ((!shared && cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess) ||
       cudaHostAlloc((void**)&h->hscal, S_COUNT * sizeof(double), cudaHostAllocDefault) != cudaSuccess) {
     cudaGetLastError();
     cfmg_destroy(h);
     return fail(nullptr, CFMG_ERR_ALLOC, "stream or pinned allocation failed");
   }
-  h->stream = h->own_stream;
+  h->stream = shared ? shared : h->own_stream;
   if (cudaMemsetAsync(h->arena, 0, total, h->stream) != cudaSuccess) {
     cfmg_destroy(h);
     return fail(nullptr, CFMG_ERR_CUDA, "arena clear failed");
@@ -918,12 +1029,18 @@ int cfmg_create(const cfmg_desc* d, cfmg_handle** out) {
   return CFMG_OK;
 }
 
+extern "C" {
+
+int cfmg_create(const cfmg_desc* d, cfmg_handle** out) { return create_handle(d, nullptr, out); }
+
 int cfmg_destroy(cfmg_handle* h) {
   if (!h) return CFMG_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
   drop_graphs(h);
   harvest(h);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+  for (double* p : {h->adj_x, h->adj_b, h->adj_gk})
+    if (p) cudaFree(p);
   if (h->arena) cudaFree(h->arena);
   if (h->hscal) cudaFreeHost(h->hscal);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -1174,6 +1291,49 @@ int cfmg_solve(cfmg_handle* h, double* res_out, int* nite_out, double* history) 
   return CFMG_OK;
 }
 
+int cfmg_adjoint(cfmg_handle* h, const double* g, double* grad_b, double* grad_kappa, double* res, int* nite) {
+  if (!h || !g || !grad_b || !res || !nite) return CFMG_ERR_ARG;
+  if (grad_kappa && h->d.op != CFMG_VARCOEF)
+    return fail(h, CFMG_ERR_ARG, "grad_kappa needs the variable-coefficient operator");
+  TRY(sync(h));
+  Level& l1 = h->lv[0];
+  const size_t bytes = l1.len * sizeof(double);
+  for (double** p : {&h->adj_x, &h->adj_b, &h->adj_gk})
+    if (!*p && cudaMalloc((void**)p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(h, CFMG_ERR_ALLOC, "adjoint scratch allocation failed");
+    }
+  cudaStream_t s = h->stream;
+  const bool neumann = !vertices(h);
+  // keep the forward state
+  CUDA_OK(h, cudaMemcpyAsync(h->adj_x, l1.x, bytes, cudaMemcpyDeviceToDevice, s));
+  CUDA_OK(h, cudaMemcpyAsync(h->adj_b, l1.b, bytes, cudaMemcpyDeviceToDevice, s));
+  // A lam = P g (A symmetric), from lam = 0, with the forward's cycle and rule
+  CUDA_OK(h, cudaMemcpyAsync(l1.b, g, bytes, cudaMemcpyDefault, s));
+  if (neumann) {
+    TRY(count_wet(h));
+    TRY(remove_wet_mean(h, l1.b));
+  }
+  CUDA_OK(h, cudaMemsetAsync(l1.x, 0, bytes, s));
+  TRY(cfmg_solve(h, res, nite, nullptr));
+  if (neumann) {
+    TRY(count_wet(h));
+    TRY(remove_wet_mean(h, l1.x));
+  }
+  CUDA_OK(h, cudaMemcpyAsync(grad_b, l1.x, bytes, cudaMemcpyDefault, s));
+  if (grad_kappa) {
+    const long long n = (long long)l1.len;
+    k_kappa_grad<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(l1.x, h->adj_x, l1.msk, h->adj_gk, l1.tx, n);
+    h->launches += 1;
+    LAUNCH_OK(h);
+    CUDA_OK(h, cudaMemcpyAsync(grad_kappa, h->adj_gk, bytes, cudaMemcpyDefault, s));
+  }
+  // restore the forward solution and right-hand side
+  CUDA_OK(h, cudaMemcpyAsync(l1.x, h->adj_x, bytes, cudaMemcpyDeviceToDevice, s));
+  CUDA_OK(h, cudaMemcpyAsync(l1.b, h->adj_b, bytes, cudaMemcpyDeviceToDevice, s));
+  return sync(h);
+}
+
 int cfmg_launch_count(const cfmg_handle* h, long long* n) {
   if (!h || !n) return CFMG_ERR_ARG;
   *n = h->launches;
@@ -1183,6 +1343,11 @@ int cfmg_launch_count(const cfmg_handle* h, long long* n) {
 int cfmg_set_option(cfmg_handle* h, int option, long long value) {
   if (!h) return CFMG_ERR_ARG;
   TRY(sync(h));
+  if (option == CFMG_OPT_TEMPORAL_BLOCKING) {
+    h->tb_on = value != 0;
+    drop_graphs(h);
+    return CFMG_OK;
+  }
   if (option == CFMG_OPT_ENGINE_CELLS) {
     if (value < 0) return fail(h, CFMG_ERR_ARG, "engine_cells must be >= 0");
     h->engine_cells = value;

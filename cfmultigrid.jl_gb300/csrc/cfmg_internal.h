@@ -25,6 +25,7 @@ struct Level {
   uint8_t* msk;
   // mixed precision copies (used by CFMG_MIXED)
   float *x32, *y32, *r32, *b32, *widiag32, *diag32, *Rcoef32, *Pcoef32, *cE32, *cN32;
+  int xswap;  // 1: the FP32 x currently lives in y32 (after a temporally blocked smoothing)
   int ic0, ic1, jc0, jc1, kc0, kc1;  // interior box (1-based inclusive)
 };
 
@@ -112,6 +113,18 @@ enum OpKind : int {
   OPK_RESTRICT0, OPK_RESTRICT1, OPK_RESTRICT2, OPK_RESTRICT3,
   OPK_PROLONG0, OPK_PROLONG1, OPK_PROLONG2, OPK_PROLONG3,
   OPK_FILL, OPK_ZERO, OPK_F32TO64, OPK_F64TO32,
+  // solve-loop ops of whole-solve programs (the batched engine): they act
+  // on the program's scalar block sc[] (see SolveSlot)
+  OPK_NORM64,    // sc[s0] = sum msk*x^2 (0 -> 1 when s1 != 0)
+  OPK_MEAN64,    // sc[s0] = (sum msk*x) / sc[s1]
+  OPK_RATIO,     // sc[s0] = sc[s1]/sc[s2] (norm_kind REF) or sqrt of it (L2); 0 when sc[s2] <= 0
+  OPK_SCALE,     // sc[s0] = 1/rms, sc[s0+1] = rms with rms = sqrt(sc[s1]/sc[s2])
+  OPK_RHS32,     // y (b32) = y2 (r32) = msk ? (x - sc[s1]) * sc[s0] : 0
+  OPK_UPDATE,    // y (x64) += (double) x (e32) * sc[s0]
+  OPK_BRANCH,    // continue while sc[s0] > tol && sc[s1] < maxite (then sc[s1] += 1), else jump to s2
+  OPK_JUMP,      // jump to s2
+  OPK_STAMP,     // sc[s0] = %globaltimer (ns)
+  OPK_HIST,      // sc[s0 + sc[s1]] = sc[s2]
 };
 struct Op {
   int kind, prec, lev, cls;  // cls: CFMG_K_* class for accounting
@@ -124,11 +137,27 @@ struct Op {
   const void *x, *b, *w, *d, *cE, *cN, *coef;
   void* y;  // the written field: sweep y, residual r, coarse b, fine x, filled/zeroed field
   const uint8_t* m;
+  // solve-loop ops
+  double* sc;
+  void* y2;
+  double tol;
+  int s0, s1, s2, maxite, norm_kind, pad;
 };
+// scalar block of a whole-solve program
+enum SolveSlot { SS_NORMB = 0, SS_NR, SS_RES, SS_NITE, SS_NWET, SS_MEAN, SS_SCALE, SS_ISCALE, SS_T0, SS_T1,
+                 SS_HIST, SS_COUNT_BASE = SS_HIST };
+void launch_batch(const Op* const* progs, const int* nops, int ninst, int* counter, double* red, int nclusters,
+                  cudaStream_t s);
+int engine_max_clusters();
 constexpr int kEngineCtas = 8;      // cluster size (portable)
 constexpr int kEngineThreads = 1024;
 void launch_op(const Op& op, cudaStream_t s);                   // one Op as a standalone kernel
-void launch_program(const Op* prog, int nops, cudaStream_t s);  // a device-resident program
+void launch_program(const Op* prog, int nops, double* red, cudaStream_t s);  // a device-resident program
+
+// temporally blocked FP32 smoother (k_tb.cu): nite pairs of 5- or 9-point
+// sweeps over the box U in one pass, x -> xo; false if nite is not 1..4
+bool launch_smooth_tb(int stencil, int nite, const float* x, float* xo, const float* b, const float* w, float cff,
+                      int tx, int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s);
 
 // message returned by cfmg_last_error(NULL) (cfmg_api.cu)
 void set_global_error(const std::string& msg);

@@ -94,8 +94,11 @@ extern "C" {
 #define CFMG_K_ENGINE 7   /* one launch of the coarse-level program engine */
 
 /* options for cfmg_set_option */
-#define CFMG_OPT_ENGINE_CELLS 0 /* levels of at most this many cells (tx*ty*tz) run in the
-                                   coarse-level engine; 0 turns the engine off (default 80000) */
+#define CFMG_OPT_ENGINE_CELLS 0 /* FP32 levels of at most this many cells (tx*ty*tz), FP64
+                                   levels of at most 1/16 of it, run in the coarse-level
+                                   engine; 0 turns the engine off (default 80000) */
+#define CFMG_OPT_TEMPORAL_BLOCKING 1 /* 1 (default): FP32 smoothing of fine 2D levels runs all
+                                        sweeps of a call in one shared-memory pass; 0: one kernel per sweep */
 
 typedef struct cfmg_desc {
   int kase;     /* CFMG_TWOD / CFMG_THREED            (Param.case) */
@@ -169,6 +172,20 @@ CFMG_API int cfmg_cycle(cfmg_handle* h, int kind);
  * desc.norm_kind and desc.precision. `history` (may be NULL) receives
  * maxite+1 entries: the residual after 0..nite cycles. */
 CFMG_API int cfmg_solve(cfmg_handle* h, double* res, int* nite, double* history);
+
+/* Adjoint solve: the backward pass of solve! (no counterpart in the
+ * reference; a Julia host exposes it as a ChainRulesCore rrule, see
+ * INTEGRATION.md). After a forward cfmg_solve, with the cotangent
+ * g = dL/dx of level 1 (reference layout, host or device pointer), solves
+ * A lam = g with the same cycle, arithmetic and stopping rule (A is
+ * symmetric) and writes dL/db = lam to grad_b and, for CFMG_VARCOEF,
+ * dL/dkappa to grad_kappa (may be NULL): the sum over the cell's faces to
+ * wet neighbours of (lam_k - lam_nb)(x_k - x_nb)/2. For the cell-centred
+ * (Neumann) operator g and lam are projected to zero wet mean. The forward
+ * x and b are restored. res/nite report the adjoint solve. The first call
+ * allocates three level-1 FP64 scratch arrays. */
+CFMG_API int cfmg_adjoint(cfmg_handle* h, const double* g, double* grad_b, double* grad_kappa, double* res,
+                          int* nite);
 
 /* Instrumentation (no counterpart in the reference, which has none).
  * cfmg_launch_count: kernels this handle has launched so far; a replay of a

@@ -96,3 +96,32 @@ def test_mixed_matches_fp64_oracle(name):
     c = _wet_mean_removed(xo.x.copy(), msk) if singular else xo.x * msk
     err = np.linalg.norm(a - c) / np.linalg.norm(c)
     assert err <= 1e-6, err
+
+
+@pytest.mark.parametrize("name", ["config1_256_centers_v", "config2_512_vertices_lap9_f"])
+def test_temporal_blocking_is_bit_identical(name):
+    """The temporally blocked FP32 smoother (all sweeps of a call in one
+    shared-memory pass) must give the same FP32 fields as one kernel per
+    sweep, hence the same solve bit for bit."""
+    base, mkind = CASES[name]
+    out = []
+    for tb in (1, 0):
+        mg = cfmg.get_gmg(cfmg.Param(**base, tol=1e-10, maxite=40, residual_norm="l2", precision="mixed",
+                                     verbose=False))
+        mg.set_option("engine_cells", 2000)  # keep the fine levels out of the engine
+        mg.set_option("temporal_blocking", tb)
+        shape = mg.shape(1)
+        custom = _mask(base, shape, mkind)
+        mg.oper[1].msk = custom
+        cfmg.setup_operators(mg)
+        for lev in range(1, mg.nlevels + 1):
+            for f in ("x", "y", "r", "b"):
+                cfmg.set_to_zero(mg, lev, f)
+        msk = mg.download(1, "msk").astype(np.float64)
+        b = np.asfortranarray(np.random.default_rng(9).standard_normal(shape)) * msk
+        F.subtract_mean(b, msk)
+        mg.data[1].b = b
+        res, n, hist = cfmg.solve(mg, history=True)
+        out.append((hist, mg.data[1].x))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])

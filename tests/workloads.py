@@ -29,7 +29,17 @@ def coastline_cells(n: int, seed: int, sigma: float, land: float):
     return sm > thr, rng
 
 
-def config2(n: int = 4096, nh: int = 3, seed: int = 1, sigma: float = 32.0, land: float = 0.30):
+# Deepest hierarchy of the reference's algorithm that converges on the
+# config-2 coastline. The coverage-thresholded coarse masks
+# (compute_msk_dev, src/gmg_setup.jl:322-366) split the connected ocean
+# into many pieces once a coarse cell spans more than ~16 fine cells; with
+# 6 levels the F-cycle diverges (x1.18 per cycle), with 10 levels (the
+# configuration's own count) by x11 per cycle (CPU oracle, 4096^2).
+CONFIG2_LEVELS = 5
+
+
+def config2(n: int = 4096, nh: int = 3, seed: int = 1, sigma: float = 32.0, land: float = 0.30,
+            nlevels: int = CONFIG2_LEVELS):
     """Returns (param dict, level-1 vertex mask, raw RHS noise) for config 2;
     the RHS is masked and mean-removed with the post-setup mask by ``rhs``."""
     wet, rng = coastline_cells(n, seed, sigma * n / 4096.0, land)
@@ -39,7 +49,7 @@ def config2(n: int = 4096, nh: int = 3, seed: int = 1, sigma: float = 32.0, land
     vmsk = F.get_mask_at_corners(cells)
     noise = np.asfortranarray(rng.standard_normal((t, t, 1)))
     param = dict(nx=n, ny=n, nz=1, nh=nh, case="twod", location="vertices", operator="laplacian9", cycle="f",
-                 nlevels=10, npre=3, npost=3, omega=0.8, ndeepest=20)
+                 nlevels=nlevels, npre=3, npost=3, omega=0.8, ndeepest=20)
     return param, vmsk, noise
 
 
