@@ -32,7 +32,7 @@ from . import _lib
 from ._lib import CASES, CYCLES, FIELDS, LOCATIONS, NORMS, OPERATORS, PRECISIONS, TOPOLOGIES
 
 __all__ = ["Param", "Gmg", "CfmgError", "get_gmg", "solve", "setup_operators", "vcycle", "fcycle", "fill",
-           "norm", "normresidual", "set_to_zero", "set_default_msk", "adjoint", "loss_and_grad"]
+           "norm", "normresidual", "set_to_zero", "set_default_msk", "adjoint", "loss_and_grad", "Batch"]
 
 
 class CfmgError(RuntimeError):
@@ -136,14 +136,18 @@ class _OneBased(list):
 class Gmg:
     """The multigrid object (Gmg, src/gmg_types.jl:121-132) living on the GPU."""
 
-    def __init__(self, param: Param):
+    def __init__(self, param: Param, _handle: Optional[ctypes.c_void_p] = None):
         self._L = _lib.load()
         self.param = param
-        d = param.desc()
-        h = ctypes.c_void_p()
-        rc = self._L.cfmg_create(ctypes.byref(d), ctypes.byref(h))
-        if rc != 0:
-            raise CfmgError(rc, self._L.cfmg_last_error(None).decode())
+        self._owned = _handle is None
+        if _handle is None:
+            d = param.desc()
+            h = ctypes.c_void_p()
+            rc = self._L.cfmg_create(ctypes.byref(d), ctypes.byref(h))
+            if rc != 0:
+                raise CfmgError(rc, self._L.cfmg_last_error(None).decode())
+        else:
+            h = _handle
         self._h = h
         n = ctypes.c_int()
         self._check(self._L.cfmg_nlevels(h, ctypes.byref(n)))
@@ -170,9 +174,9 @@ class Gmg:
 
     def close(self):
         h = getattr(self, "_h", None)
-        if h is not None and h.value:
+        if h is not None and h.value and getattr(self, "_owned", True):
             self._L.cfmg_destroy(h)
-            self._h = None
+        self._h = None
 
     def __del__(self):
         try:
@@ -396,3 +400,65 @@ def loss_and_grad(mg: Gmg, b, xstar, kappa=None):
     loss = 0.5 * float(np.sum(d * d))
     gb, gk = adjoint(mg, d)
     return loss, gb, gk
+
+
+class Batch:
+    """Many independent 2D masked solves of uneven sizes sharing one Param
+    (precision "mixed"), run in one launch of the batched engine.
+
+    ``batch.instance(i)`` is a Gmg for instance i (upload its mask, call
+    setup_operators, upload b, read x back). ``batch.solve()`` returns
+    (res, nite, t_done_ms) arrays; t_done_ms is the time from the batch start
+    until that instance met its tolerance."""
+
+    def __init__(self, param: Param, nx, ny, nlevels=None):
+        self._L = _lib.load()
+        self.param = param
+        n = len(nx)
+        d = param.desc()
+        ax = (ctypes.c_int * n)(*[int(v) for v in nx])
+        ay = (ctypes.c_int * n)(*[int(v) for v in ny])
+        al = (ctypes.c_int * n)(*[int(v) for v in nlevels]) if nlevels is not None else None
+        b = ctypes.c_void_p()
+        rc = self._L.cfmg_batch_create(ctypes.byref(d), n, ax, ay, al, ctypes.byref(b))
+        if rc != 0:
+            raise CfmgError(rc, self._L.cfmg_last_error(None).decode())
+        self._b = b
+        self.n = n
+        self._inst = []
+        for i in range(n):
+            h = ctypes.c_void_p()
+            self._check(self._L.cfmg_batch_instance(b, i, ctypes.byref(h)))
+            p = dataclasses.replace(param, nx=int(nx[i]), ny=int(ny[i]),
+                                    nlevels=int(nlevels[i]) if nlevels is not None else param.nlevels)
+            self._inst.append(Gmg(p, _handle=h))
+
+    def _check(self, rc):
+        if rc != 0:
+            raise CfmgError(rc, self._L.cfmg_batch_last_error(self._b).decode())
+
+    def instance(self, i: int) -> Gmg:
+        return self._inst[i]
+
+    def solve(self, from_zero: bool = True):
+        res = np.zeros(self.n)
+        nite = np.zeros(self.n, dtype=np.int32)
+        t = np.zeros(self.n)
+        self._check(self._L.cfmg_batch_solve(self._b, 1 if from_zero else 0, res.ctypes.data_as(ctypes.c_void_p),
+                                             nite.ctypes.data_as(ctypes.c_void_p),
+                                             t.ctypes.data_as(ctypes.c_void_p)))
+        return res, nite, t
+
+    def close(self):
+        b = getattr(self, "_b", None)
+        if b is not None and b.value:
+            for g in self._inst:
+                g._h = None
+            self._L.cfmg_batch_destroy(b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

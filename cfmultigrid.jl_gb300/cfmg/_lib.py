@@ -33,9 +33,10 @@ EXPORTS = (
     "cfmg_set_default_msk", "cfmg_setup_operators", "cfmg_smooth", "cfmg_residual", "cfmg_restrict",
     "cfmg_prolong", "cfmg_zero", "cfmg_fill", "cfmg_norm", "cfmg_normresidual", "cfmg_cycle", "cfmg_solve",
     "cfmg_launch_count", "cfmg_profile", "cfmg_profile_read", "cfmg_set_option", "cfmg_norm_noalloc",
-    "cfmg_adjoint",
+    "cfmg_adjoint", "cfmg_batch_create", "cfmg_batch_destroy", "cfmg_batch_instance", "cfmg_batch_solve",
+    "cfmg_batch_last_error",
 )
-OPTIONS = {"engine_cells": 0, "temporal_blocking": 1}
+OPTIONS = {"engine_cells": 0, "temporal_blocking": 1, "coarsest_fp64": 2}
 KERNEL_CLASSES = {"sweep": 0, "residual": 1, "restrict": 2, "prolong": 3, "norm": 4, "fill": 5, "convert": 6,
                   "engine": 7}
 
@@ -97,6 +98,10 @@ def load() -> ctypes.CDLL:
         "cfmg_set_option": [vp, i, ctypes.c_longlong],
         "cfmg_norm_noalloc": [vp, vp, ctypes.c_longlong, vp, vp],
         "cfmg_adjoint": [vp, vp, vp, vp, pd, pi],
+        "cfmg_batch_create": [ctypes.POINTER(Desc), i, vp, vp, vp, ctypes.POINTER(vp)],
+        "cfmg_batch_destroy": [vp],
+        "cfmg_batch_instance": [vp, i, ctypes.POINTER(vp)],
+        "cfmg_batch_solve": [vp, i, vp, vp, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -104,5 +109,7 @@ def load() -> ctypes.CDLL:
         f.restype = ctypes.c_int
     L.cfmg_last_error.argtypes = [vp]
     L.cfmg_last_error.restype = ctypes.c_char_p
+    L.cfmg_batch_last_error.argtypes = [vp]
+    L.cfmg_batch_last_error.restype = ctypes.c_char_p
     _lib = L
     return L

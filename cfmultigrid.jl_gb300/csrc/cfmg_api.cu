@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <mutex>
 #include <unordered_map>
 
@@ -49,6 +50,7 @@ struct cfmg_handle {
   int pool_cap = 0, pool_used = 0;
   std::unordered_map<std::string, int> prog_cache;
   bool tb_on = true;  // temporally blocked FP32 smoothing on fine levels
+  int coarsest_fp64 = -1;  // mixed form: -1 FP64 when the coarsest level is small, 0 never, 1 always
   // adjoint scratch (level-1 FP64 arrays, allocated on the first cfmg_adjoint)
   double *adj_x = nullptr, *adj_b = nullptr, *adj_gk = nullptr;
   bool record = false;  // emit() records every Op (whole-solve programs) instead of running it
@@ -56,8 +58,28 @@ struct cfmg_handle {
 
 constexpr int kProgPoolOps = 8192;  // device store of engine programs (~1.9 MB)
 
-enum Scal { S_NORM = 0, S_RES = 1, S_NORMB = 2, S_NWET = 3, S_SCALE = 4, S_MEAN = 5, S_TMP0 = 6, S_ISCALE = 7,
-            S_COUNT = 16 };
+// Batched solves: independent instances (each a full handle on the batch's
+// stream) whose whole mixed-precision solves run as programs of the
+// batched engine, one launch for all of them.
+struct cfmg_batch {
+  cfmg_desc d;
+  std::vector<cfmg_handle*> inst;
+  cudaStream_t stream = nullptr;
+  std::vector<int> order;  // queue order: largest instance first
+  Op* progs = nullptr;     // all programs, concatenated (device)
+  const Op** ptrs = nullptr;
+  int* nops = nullptr;
+  int* counter = nullptr;  // [0]: queue head, [1 + c]: cluster c's current instance
+  double* red = nullptr;   // kEngineCtas reduction slots per cluster
+  double* sc = nullptr;    // scalar blocks, nsc per instance
+  double* nwet = nullptr;  // wet cells per instance
+  int nsc = 0, nclusters = 0;
+  bool built = false;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [zero_x]
+  std::vector<double> hsc;
+  std::string err;
+};
+
 
 namespace {
 
@@ -460,6 +482,9 @@ int coarsest_t<double>(cfmg_handle* h, int nite) {
 template <>
 int coarsest_t<float>(cfmg_handle* h, int nite) {
   if (L(h) == 1) return smooth_t<float>(h, 1, nite);
+  const bool fp64 = h->coarsest_fp64 > 0 ||
+                    (h->coarsest_fp64 < 0 && (long long)h->lv[L(h) - 1].len <= engine_limit(h, CFMG_FP64));
+  if (!fp64) return smooth_t<float>(h, L(h), nite);
   const int lev = L(h);
   const Level& c = h->lv[lev - 1];
   View<float> v = view<float>(c);
@@ -796,8 +821,63 @@ int remove_wet_mean(cfmg_handle* h, double* x) {
   return CFMG_OK;
 }
 
+// Fused path (closed topology): one pass gives the FP64 residual, its
+// norm (and wet sum) and the scaled FP32 right-hand side of the next
+// correction; a Neumann operator adds a mean-removing pass.
+bool fused_ok(const cfmg_handle* h) { return !xperio(h) && h->d.op != CFMG_VARCOEF; }
+
+int fused_residual(cfmg_handle* h) {
+  TRY(flush(h));
+  const Level& l1 = h->lv[0];
+  Geom g = geom(l1);
+  const bool neumann = !vertices(h);
+  int kind;
+  Box bx = interior(l1);
+  long long lo = 0, n;
+  if (h->d.op == CFMG_LAPLACIAN9) kind = threed(h) ? OPK_RESID19 : OPK_RESID9;
+  else kind = threed(h) ? OPK_RESID7 : OPK_RESID5;
+  if (kind == OPK_RESID5) {
+    lo = g.n1;
+    n = g.len - 2 * g.n1;
+  } else {
+    n = box_count(bx);
+  }
+  {
+    Launch k(h, CFMG_K_RESIDUAL, 1, CFMG_FP64, 2);
+    launch_resid_fused(kind, l1.r, l1.x, l1.b, l1.diag, l1.msk, g, bx, lo, n, h->dscal + S_NEXT, l1.b32, l1.r32,
+                       neumann, h->partials, h->stream);
+    launch_fused_final(h->partials, h->dscal, h->dscal + S_NORMB, neumann ? h->dscal + S_NWET : nullptr,
+                       h->d.norm_kind, h->stream);
+  }
+  if (neumann) {
+    Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED);
+    launch_rhs32_mean(l1.r, l1.msk, h->dscal + S_MEAN2, l1.b32, l1.r32, (long long)l1.len, h->stream);
+  }
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
+__global__ void init_scale(double* ds) {
+  const double nw = ds[S_NWET] > 0 ? ds[S_NWET] : 1.0;
+  const double rms = sqrt(ds[S_NORMB] / nw);
+  int e = 0;
+  if (rms > 0 && isfinite(rms)) frexp(rms, &e);
+  ds[S_NEXT] = ldexp(1.0, -e);
+}
+
 int mixed_iteration(cfmg_handle* h, int kind) {
   for (Level& l : h->lv) l.xswap = 0;  // every FP32 x is zeroed before use in the cycle
+  if (fused_ok(h)) {  // the right-hand side was made by the previous fused pass
+    const Level& l1 = h->lv[0];
+    TRY(zero_t<float>(h, 1, CFMG_X));
+    TRY(cycle_t<float>(h, kind));
+    {
+      Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED);
+      launch_update_scaled(l1.x, view<float>(l1).x, h->dscal + S_ICUR, (long long)l1.len, h->stream);
+    }
+    LAUNCH_OK(h);
+    return fused_residual(h);
+  }
   const Level& l1 = h->lv[0];
   const long long n = (long long)l1.len;
   const unsigned nb = (unsigned)((n + 255) / 256);
@@ -822,9 +902,13 @@ int mixed_iteration(cfmg_handle* h, int kind) {
 
 // one solve iteration (cycle + normresidual + copy of the ratio to the host)
 int iteration(cfmg_handle* h, int prec, int kind, int norm_kind) {
-  if (prec == CFMG_MIXED) TRY(mixed_iteration(h, kind));
-  else TRY(cycle_t<double>(h, kind));
-  TRY(normresidual_dev(h, norm_kind));
+  if (prec == CFMG_MIXED) {
+    TRY(mixed_iteration(h, kind));
+    if (!fused_ok(h)) TRY(normresidual_dev(h, norm_kind));
+  } else {
+    TRY(cycle_t<double>(h, kind));
+    TRY(normresidual_dev(h, norm_kind));
+  }
   CUDA_OK(h, cudaMemcpyAsync(h->hscal, h->dscal, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   return CFMG_OK;
 }
@@ -864,6 +948,87 @@ void drop_graphs(cfmg_handle* h) {
         cudaGraphExecDestroy(g);
         g = nullptr;
       }
+}
+
+// ------------------------------------------------ whole-solve programs
+// Records the mixed-precision solve of one handle (the loop of cfmg_solve
+// with mixed_iteration's steps) as a single engine program whose loop,
+// norms and stopping test run on the device; sc is the program's scalar
+// block (SolveSlot), nsc its length.
+int record_solve_program(cfmg_handle* h, double* sc, std::vector<Op>& out) {
+  const Level& l1 = h->lv[0];
+  const long long n = (long long)l1.len;
+  const int nk = h->d.norm_kind;
+  const bool neumann = !vertices(h);
+  h->record = true;
+  h->pending.clear();
+  auto sop = [&](int kind) {
+    Op op = mkop(kind, 0, 1, CFMG_K_NORM, l1);
+    op.sc = sc;
+    op.n = n;
+    op.norm_kind = nk;
+    return op;
+  };
+  auto push = [&](const Op& op) { h->pending.push_back(op); };
+  auto residual_norm = [&]() -> int {
+    TRY(residual_t<double>(h, 1));
+    Op o = sop(OPK_NORM64);
+    o.x = l1.r; o.m = l1.msk; o.s0 = SS_NR; o.s1 = nk == CFMG_NORM_REF_SQUARED;
+    push(o);
+    o = sop(OPK_RATIO);
+    o.s0 = SS_RES; o.s1 = SS_NR; o.s2 = SS_NORMB;
+    push(o);
+    o = sop(OPK_HIST);
+    o.s0 = SS_HIST; o.s1 = SS_NITE; o.s2 = SS_RES;
+    push(o);
+    return CFMG_OK;
+  };
+  int rc = CFMG_OK;
+  do {
+    Op o = sop(OPK_STAMP);
+    o.s0 = SS_T0;
+    push(o);
+    o = sop(OPK_ZERO_IF);  // solve from x = 0 when asked, else from the current x
+    o.y = l1.x; o.s0 = SS_ZEROX;
+    push(o);
+    o = sop(OPK_NORM64);  // normb = norm(mg, 1, :b)
+    o.x = l1.b; o.m = l1.msk; o.s0 = SS_NORMB; o.s1 = nk == CFMG_NORM_REF_SQUARED;
+    push(o);
+    if ((rc = residual_norm()) != CFMG_OK) break;
+    const int branch = (int)h->pending.size();
+    o = sop(OPK_BRANCH);
+    o.s0 = SS_RES; o.s1 = SS_NITE; o.tol = h->d.tol; o.maxite = h->d.maxite;
+    push(o);
+    if (neumann) {
+      o = sop(OPK_MEAN64);
+      o.x = l1.r; o.m = l1.msk; o.s0 = SS_MEAN; o.s1 = SS_NWET;
+      push(o);
+    }
+    o = sop(OPK_SCALE);
+    o.s0 = SS_SCALE; o.s1 = SS_NR; o.s2 = SS_NWET;
+    push(o);
+    for (Level& l : h->lv) l.xswap = 0;
+    o = sop(OPK_RHS32);
+    o.x = l1.r; o.m = l1.msk; o.y = l1.b32; o.y2 = l1.r32; o.s0 = SS_SCALE; o.s1 = SS_MEAN;
+    push(o);
+    if ((rc = zero_t<float>(h, 1, CFMG_X)) != CFMG_OK) break;
+    if ((rc = cycle_body<float>(h, h->d.cycle)) != CFMG_OK) break;
+    o = sop(OPK_UPDATE);
+    o.x = view<float>(l1).x; o.y = l1.x; o.s0 = SS_ISCALE;
+    push(o);
+    if ((rc = residual_norm()) != CFMG_OK) break;
+    o = sop(OPK_JUMP);
+    o.s2 = branch;
+    push(o);
+    h->pending[branch].s2 = (int)h->pending.size();  // the loop exits to the final stamp
+    o = sop(OPK_STAMP);
+    o.s0 = SS_T1;
+    push(o);
+  } while (false);
+  h->record = false;
+  out.swap(h->pending);
+  h->pending.clear();
+  return rc;
 }
 
 // ----------------------------------------------------------- allocation
@@ -1266,7 +1431,12 @@ int cfmg_solve(cfmg_handle* h, double* res_out, int* nite_out, double* history) 
     launch_norm<double>(l1.b, l1.msk, l1.len, h->partials, h->dscal + S_NORMB, nullptr, d.norm_kind, h->stream);
   }
   LAUNCH_OK(h);
-  TRY(normresidual_dev(h, d.norm_kind));
+  if (prec == CFMG_MIXED && fused_ok(h)) {
+    init_scale<<<1, 1, 0, h->stream>>>(h->dscal);  // the first right-hand side is scaled from |b|
+    TRY(fused_residual(h));
+  } else {
+    TRY(normresidual_dev(h, d.norm_kind));
+  }
   CUDA_OK(h, cudaMemcpyAsync(h->hscal, h->dscal, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   TRY(sync(h));
   double res = h->hscal[S_RES];
@@ -1334,6 +1504,179 @@ int cfmg_adjoint(cfmg_handle* h, const double* g, double* grad_b, double* grad_k
   return sync(h);
 }
 
+}  // extern "C"
+
+namespace {
+
+int bfail(cfmg_batch* b, int code, const std::string& msg) {
+  if (b) b->err = msg;
+  return code;
+}
+
+#define BCUDA(b, call)                                                                          \
+  do {                                                                                          \
+    cudaError_t _e = (call);                                                                    \
+    if (_e != cudaSuccess) return bfail((b), CFMG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+__global__ void k_batch_init(double* sc, const double* nwet, int ninst, int nsc, double zero_x) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ninst * nsc) return;
+  const int k = i % nsc;
+  sc[i] = (k == SS_NWET) ? nwet[i / nsc] : (k == SS_ZEROX ? zero_x : 0.0);
+}
+
+int batch_build(cfmg_batch* b) {
+  const int ninst = (int)b->inst.size();
+  b->nsc = SS_HIST + b->d.maxite + 2;
+  // per-instance FP32 coefficients and wet counts
+  BCUDA(b, cudaMalloc((void**)&b->sc, sizeof(double) * (size_t)ninst * b->nsc));
+  BCUDA(b, cudaMalloc((void**)&b->nwet, sizeof(double) * (size_t)ninst));
+  for (int i = 0; i < ninst; ++i) {
+    cfmg_handle* h = b->inst[i];
+    int rc = prepare_mixed(h);
+    if (rc == CFMG_OK) rc = count_wet(h);
+    if (rc != CFMG_OK) return bfail(b, rc, "instance " + std::to_string(i) + ": " + h->err);
+    BCUDA(b, cudaMemcpyAsync(b->nwet + i, h->dscal + S_NWET, sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+  }
+  // programs, in queue order (largest first)
+  b->order.resize(ninst);
+  for (int i = 0; i < ninst; ++i) b->order[i] = i;
+  std::stable_sort(b->order.begin(), b->order.end(),
+                   [&](int a, int c) { return b->inst[a]->lv[0].len > b->inst[c]->lv[0].len; });
+  std::vector<Op> all;
+  std::vector<size_t> off(ninst);
+  std::vector<int> cnt(ninst);
+  for (int q = 0; q < ninst; ++q) {
+    const int i = b->order[q];
+    std::vector<Op> prog;
+    int rc = record_solve_program(b->inst[i], b->sc + (size_t)i * b->nsc, prog);
+    if (rc != CFMG_OK) return bfail(b, rc, "instance " + std::to_string(i) + ": " + b->inst[i]->err);
+    off[q] = all.size();
+    cnt[q] = (int)prog.size();
+    all.insert(all.end(), prog.begin(), prog.end());
+  }
+  BCUDA(b, cudaMalloc((void**)&b->progs, sizeof(Op) * all.size()));
+  BCUDA(b, cudaMemcpy(b->progs, all.data(), sizeof(Op) * all.size(), cudaMemcpyHostToDevice));
+  std::vector<const Op*> ptrs(ninst);
+  for (int q = 0; q < ninst; ++q) ptrs[q] = b->progs + off[q];
+  BCUDA(b, cudaMalloc((void**)&b->ptrs, sizeof(Op*) * (size_t)ninst));
+  BCUDA(b, cudaMemcpy(b->ptrs, ptrs.data(), sizeof(Op*) * (size_t)ninst, cudaMemcpyHostToDevice));
+  BCUDA(b, cudaMalloc((void**)&b->nops, sizeof(int) * (size_t)ninst));
+  BCUDA(b, cudaMemcpy(b->nops, cnt.data(), sizeof(int) * (size_t)ninst, cudaMemcpyHostToDevice));
+  b->nclusters = engine_max_clusters();
+  if (b->nclusters > ninst) b->nclusters = ninst;
+  BCUDA(b, cudaMalloc((void**)&b->counter, sizeof(int) * (size_t)(1 + b->nclusters)));
+  BCUDA(b, cudaMalloc((void**)&b->red, sizeof(double) * (size_t)b->nclusters * kEngineCtas));
+  // one graph per start mode: scalar init, queue reset, the batched engine
+  const int tot = ninst * b->nsc;
+  for (int z = 0; z < 2; ++z) {
+    cudaGraph_t g = nullptr;
+    BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
+    k_batch_init<<<(tot + 255) / 256, 256, 0, b->stream>>>(b->sc, b->nwet, ninst, b->nsc, (double)z);
+    cudaMemsetAsync(b->counter, 0, sizeof(int) * (size_t)(1 + b->nclusters), b->stream);
+    launch_batch(b->ptrs, b->nops, ninst, b->counter, b->red, b->nclusters, b->stream);
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (e != cudaSuccess) return bfail(b, CFMG_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&b->graph[z], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return bfail(b, CFMG_ERR_CUDA, std::string("batch instantiate: ") + cudaGetErrorString(e));
+  }
+  b->hsc.resize((size_t)tot);
+  b->built = true;
+  return CFMG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cfmg_batch_create(const cfmg_desc* d, int ninst, const int* nx, const int* ny, const int* nlevels,
+                      cfmg_batch** out) {
+  if (!out || !d || !nx || !ny || ninst < 1) return fail(nullptr, CFMG_ERR_ARG, "batch: bad arguments");
+  *out = nullptr;
+  if (d->precision != CFMG_MIXED) return fail(nullptr, CFMG_ERR_UNSUPPORTED, "batched solves use the mixed form");
+  if (d->topology != CFMG_CLOSED || d->kase != CFMG_TWOD)
+    return fail(nullptr, CFMG_ERR_UNSUPPORTED, "batched solves are 2D closed-topology");
+  cfmg_batch* b = new cfmg_batch();
+  b->d = *d;
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete b;
+    return fail(nullptr, CFMG_ERR_CUDA, "batch stream creation failed");
+  }
+  for (int i = 0; i < ninst; ++i) {
+    cfmg_desc di = *d;
+    di.nx = nx[i];
+    di.ny = ny[i];
+    if (nlevels) di.nlevels = nlevels[i];
+    cfmg_handle* h = nullptr;
+    int rc = create_handle(&di, b->stream, &h);
+    if (rc != CFMG_OK) {
+      cfmg_batch_destroy(b);
+      return fail(nullptr, rc, "batch instance " + std::to_string(i) + ": " + cfmg_last_error(nullptr));
+    }
+    h->tb_on = false;  // instance handles run through the engine only
+    b->inst.push_back(h);
+  }
+  *out = b;
+  return CFMG_OK;
+}
+
+int cfmg_batch_destroy(cfmg_batch* b) {
+  if (!b) return CFMG_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (cudaGraphExec_t g : b->graph)
+    if (g) cudaGraphExecDestroy(g);
+  for (cfmg_handle* h : b->inst) cfmg_destroy(h);
+  for (void* p : {(void*)b->progs, (void*)b->ptrs, (void*)b->nops, (void*)b->counter, (void*)b->red, (void*)b->sc,
+                  (void*)b->nwet})
+    if (p) cudaFree(p);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return CFMG_OK;
+}
+
+int cfmg_batch_instance(cfmg_batch* b, int i, cfmg_handle** h) {
+  if (!b || !h || i < 0 || i >= (int)b->inst.size()) return CFMG_ERR_ARG;
+  *h = b->inst[i];
+  return CFMG_OK;
+}
+
+const char* cfmg_batch_last_error(const cfmg_batch* b) { return b ? b->err.c_str() : ""; }
+
+int cfmg_batch_solve(cfmg_batch* b, int zero_x, double* res, int* nite, double* t_done_ms) {
+  if (!b) return CFMG_ERR_ARG;
+  for (cfmg_handle* h : b->inst)
+    if (h->mixed_dirty) b->built = false;  // coefficients changed since the programs were made
+  if (!b->built) {
+    for (cudaGraphExec_t& g : b->graph)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+    for (void** p : {(void**)&b->progs, (void**)&b->ptrs, (void**)&b->nops, (void**)&b->counter, (void**)&b->red,
+                     (void**)&b->sc, (void**)&b->nwet})
+      if (*p) {
+        cudaFree(*p);
+        *p = nullptr;
+      }
+    TRY(batch_build(b));
+  }
+  BCUDA(b, cudaGraphLaunch(b->graph[zero_x ? 1 : 0], b->stream));
+  const int ninst = (int)b->inst.size();
+  BCUDA(b, cudaMemcpyAsync(b->hsc.data(), b->sc, sizeof(double) * b->hsc.size(), cudaMemcpyDeviceToHost, b->stream));
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  double t0 = 1e300;
+  for (int i = 0; i < ninst; ++i) t0 = std::min(t0, b->hsc[(size_t)i * b->nsc + SS_T0]);
+  for (int i = 0; i < ninst; ++i) {
+    const double* c = &b->hsc[(size_t)i * b->nsc];
+    if (res) res[i] = c[SS_RES];
+    if (nite) nite[i] = (int)c[SS_NITE];
+    if (t_done_ms) t_done_ms[i] = (c[SS_T1] - t0) * 1e-6;
+  }
+  return CFMG_OK;
+}
+
 int cfmg_launch_count(const cfmg_handle* h, long long* n) {
   if (!h || !n) return CFMG_ERR_ARG;
   *n = h->launches;
@@ -1343,6 +1686,12 @@ int cfmg_launch_count(const cfmg_handle* h, long long* n) {
 int cfmg_set_option(cfmg_handle* h, int option, long long value) {
   if (!h) return CFMG_ERR_ARG;
   TRY(sync(h));
+  if (option == CFMG_OPT_COARSEST_FP64) {
+    if (value < -1 || value > 1) return fail(h, CFMG_ERR_ARG, "coarsest_fp64 must be -1, 0 or 1");
+    h->coarsest_fp64 = (int)value;
+    drop_graphs(h);
+    return CFMG_OK;
+  }
   if (option == CFMG_OPT_TEMPORAL_BLOCKING) {
     h->tb_on = value != 0;
     drop_graphs(h);

@@ -125,6 +125,7 @@ enum OpKind : int {
   OPK_JUMP,      // jump to s2
   OPK_STAMP,     // sc[s0] = %globaltimer (ns)
   OPK_HIST,      // sc[s0 + sc[s1]] = sc[s2]
+  OPK_ZERO_IF,   // y[0..n) = 0 (double) when sc[s0] != 0
 };
 struct Op {
   int kind, prec, lev, cls;  // cls: CFMG_K_* class for accounting
@@ -145,7 +146,7 @@ struct Op {
 };
 // scalar block of a whole-solve program
 enum SolveSlot { SS_NORMB = 0, SS_NR, SS_RES, SS_NITE, SS_NWET, SS_MEAN, SS_SCALE, SS_ISCALE, SS_T0, SS_T1,
-                 SS_HIST, SS_COUNT_BASE = SS_HIST };
+                 SS_ZEROX, SS_HIST };
 void launch_batch(const Op* const* progs, const int* nops, int ninst, int* counter, double* red, int nclusters,
                   cudaStream_t s);
 int engine_max_clusters();
@@ -158,6 +159,20 @@ void launch_program(const Op* prog, int nops, double* red, cudaStream_t s);  // 
 // sweeps over the box U in one pass, x -> xo; false if nite is not 1..4
 bool launch_smooth_tb(int stencil, int nite, const float* x, float* xo, const float* b, const float* w, float cff,
                       int tx, int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s);
+
+// device scalars of a handle (dscal[])
+enum Scal { S_NORM = 0, S_RES = 1, S_NORMB = 2, S_NWET = 3, S_SCALE = 4, S_MEAN = 5, S_TMP0 = 6, S_ISCALE = 7,
+            S_NEXT = 8, S_CUR = 9, S_ICUR = 10, S_MEAN2 = 11, S_COUNT = 16 };
+
+// fused FP64 steps of the mixed loop (k_mixed.cu)
+void launch_resid_fused(int kind, double* r, const double* x, const double* b, const double* d, const uint8_t* m,
+                        const Geom& g, const Box& bx, long long lo, long long n, const double* scale, float* b32,
+                        float* r32, bool neumann, double* partials, cudaStream_t s);
+void launch_fused_final(const double* partials, double* ds, const double* normb, const double* nwet, int norm_kind,
+                        cudaStream_t s);
+void launch_rhs32_mean(const double* r, const uint8_t* m, const double* mean_scale, float* b32, float* r32,
+                       long long n, cudaStream_t s);
+void launch_update_scaled(double* x, const float* e, const double* iscale, long long n, cudaStream_t s);
 
 // message returned by cfmg_last_error(NULL) (cfmg_api.cu)
 void set_global_error(const std::string& msg);

@@ -244,6 +244,10 @@ __device__ void run_program(const Op* __restrict__ prog, int nops, long long t0,
       case OPK_HIST:
         if (cluster_rank() == 0 && threadIdx.x == 0) sc[op.s0 + (int)sc[op.s1]] = sc[op.s2];
         break;
+      case OPK_ZERO_IF:
+        if (sc[op.s0] != 0.0)
+          for (long long t = t0; t < op.n; t += st) ((double*)op.y)[t] = 0.0;
+        break;
       default:
         if (op.prec == 0) exec<double>(op, t0, st);
         else exec<float>(op, t0, st);

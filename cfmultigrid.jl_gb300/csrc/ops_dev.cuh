@@ -127,38 +127,57 @@ __device__ __forceinline__ void d_sweepvc(const T* x, T* y, const T* b, const T*
 }
 
 // ------------------------------------------------------- residuals at I
+// v_* return the residual value, d_* store it.
 // rloop2d! (src/laplacian.jl:87-93): r = msk*((diag*x + b) - s4)
 template <class T>
-__device__ __forceinline__ void d_resid5(T* r, const T* x, const T* b, const T* d, const uint8_t* m, long long n1,
-                                         long long I) {
+__device__ __forceinline__ T v_resid5(const T* x, const T* b, const T* d, const uint8_t* m, long long n1, long long I) {
   typedef Ar<T> A;
-  r[I] = mask_mul(m[I], A::sub(A::add(A::mul(d[I], x[I]), b[I]), sum4(x, I, n1)));
+  return mask_mul(m[I], A::sub(A::add(A::mul(d[I], x[I]), b[I]), sum4(x, I, n1)));
 }
 // rloop3d! (src/laplacian.jl:43-51)
 template <class T>
-__device__ __forceinline__ void d_resid7(T* r, const T* x, const T* b, const T* d, const uint8_t* m, long long n1,
-                                         long long n2, long long I) {
+__device__ __forceinline__ T v_resid7(const T* x, const T* b, const T* d, const uint8_t* m, long long n1, long long n2,
+                                      long long I) {
   typedef Ar<T> A;
-  r[I] = mask_mul(m[I], A::sub(A::add(A::mul(d[I], x[I]), b[I]), faces6(x, I, n1, n2)));
+  return mask_mul(m[I], A::sub(A::add(A::mul(d[I], x[I]), b[I]), faces6(x, I, n1, n2)));
 }
 template <class T>
-__device__ __forceinline__ void d_resid9(T* r, const T* x, const T* b, const T* d, const uint8_t* m, long long n1,
-                                         long long I) {
+__device__ __forceinline__ T v_resid9(const T* x, const T* b, const T* d, const uint8_t* m, long long n1, long long I) {
   typedef Ar<T> A;
   T v = A::add(A::mul(d[I], x[I]), b[I]);
   v = A::fmx(sum4(x, I, n1), T(-0.5), v);
   v = A::fmx(diags4(x, I, n1), T(-0.25), v);
-  r[I] = mask_mul(m[I], v);
+  return mask_mul(m[I], v);
 }
 // residual_laplacian9! (src/laplacian9.jl:49-73)
 template <class T>
-__device__ __forceinline__ void d_resid19(T* r, const T* x, const T* b, const T* d, const uint8_t* m, long long n1,
-                                          long long n2, long long I) {
+__device__ __forceinline__ T v_resid19(const T* x, const T* b, const T* d, const uint8_t* m, long long n1,
+                                       long long n2, long long I) {
   typedef Ar<T> A;
   T v = A::add(A::mul(d[I], x[I]), b[I]);
   v = A::fmx(faces6(x, I, n1, n2), T(-0.5), v);
   v = A::fmx(edges12(x, I, n1, n2), T(-0.25), v);
-  r[I] = mask_mul(m[I], v);
+  return mask_mul(m[I], v);
+}
+template <class T>
+__device__ __forceinline__ void d_resid5(T* r, const T* x, const T* b, const T* d, const uint8_t* m, long long n1,
+                                         long long I) {
+  r[I] = v_resid5(x, b, d, m, n1, I);
+}
+template <class T>
+__device__ __forceinline__ void d_resid7(T* r, const T* x, const T* b, const T* d, const uint8_t* m, long long n1,
+                                         long long n2, long long I) {
+  r[I] = v_resid7(x, b, d, m, n1, n2, I);
+}
+template <class T>
+__device__ __forceinline__ void d_resid9(T* r, const T* x, const T* b, const T* d, const uint8_t* m, long long n1,
+                                         long long I) {
+  r[I] = v_resid9(x, b, d, m, n1, I);
+}
+template <class T>
+__device__ __forceinline__ void d_resid19(T* r, const T* x, const T* b, const T* d, const uint8_t* m, long long n1,
+                                          long long n2, long long I) {
+  r[I] = v_resid19(x, b, d, m, n1, n2, I);
 }
 template <class T>
 __device__ __forceinline__ void d_residvc(T* r, const T* x, const T* b, const T* d, const T* cE, const T* cN,

@@ -97,6 +97,9 @@ extern "C" {
 #define CFMG_OPT_ENGINE_CELLS 0 /* FP32 levels of at most this many cells (tx*ty*tz), FP64
                                    levels of at most 1/16 of it, run in the coarse-level
                                    engine; 0 turns the engine off (default 80000) */
+#define CFMG_OPT_COARSEST_FP64 2 /* mixed form, coarsest-level smoothing in FP64: -1 (default) when the
+                                    coarsest level holds at most 1/16 of CFMG_OPT_ENGINE_CELLS cells,
+                                    0 never (FP32), 1 always */
 #define CFMG_OPT_TEMPORAL_BLOCKING 1 /* 1 (default): FP32 smoothing of fine 2D levels runs all
                                         sweeps of a call in one shared-memory pass; 0: one kernel per sweep */
 
@@ -186,6 +189,27 @@ CFMG_API int cfmg_solve(cfmg_handle* h, double* res, int* nite, double* history)
  * allocates three level-1 FP64 scratch arrays. */
 CFMG_API int cfmg_adjoint(cfmg_handle* h, const double* g, double* grad_b, double* grad_kappa, double* res,
                           int* nite);
+
+/* Batched solves (no counterpart in the reference, which solves one
+ * problem at a time). ninst independent 2D closed-topology problems share
+ * `d` (precision must be CFMG_MIXED) except for their sizes nx[i] x ny[i]
+ * and level counts nlevels[i] (NULL: d->nlevels). Each instance is a full
+ * handle (cfmg_batch_instance): upload its mask, run cfmg_setup_operators,
+ * upload b, and read x back through the usual entry points.
+ * cfmg_batch_solve runs every instance's whole mixed-precision solve in one
+ * launch of the batched engine (a graph of one kernel), from x = 0 when
+ * zero_x is non-zero and else from each instance's current x (as solve!
+ * does); clusters take the
+ * instances largest first from a device queue, and each instance stops at
+ * its own tolerance. res, nite and t_done_ms (time from the batch start to
+ * that instance's convergence) receive ninst entries each; any may be NULL. */
+typedef struct cfmg_batch cfmg_batch;
+CFMG_API int cfmg_batch_create(const cfmg_desc* d, int ninst, const int* nx, const int* ny, const int* nlevels,
+                               cfmg_batch** out);
+CFMG_API int cfmg_batch_destroy(cfmg_batch* b);
+CFMG_API int cfmg_batch_instance(cfmg_batch* b, int i, cfmg_handle** h);
+CFMG_API int cfmg_batch_solve(cfmg_batch* b, int zero_x, double* res, int* nite, double* t_done_ms);
+CFMG_API const char* cfmg_batch_last_error(const cfmg_batch* b);
 
 /* Instrumentation (no counterpart in the reference, which has none).
  * cfmg_launch_count: kernels this handle has launched so far; a replay of a
