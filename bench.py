@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--nlevels", type=int, default=0, help="levels (0: the deepest hierarchy that converges, 5)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the single-thread CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="config2", choices=["config2", "config4"],
+    ap.add_argument("--workload", default="config2", choices=["config2", "config4", "config5"],
                     help="config4: batched solves of uneven sizes (one engine launch per batch)")
     ap.add_argument("--ninst", type=int, default=2048, help="config4 batch size")
     ap.add_argument("--quick", action="store_true",
@@ -303,7 +303,7 @@ def run_ours(args, rank, world, local):
         "ms_per_solve_fp64": ms_fp64, "mixed_speedup_vs_fp64": ms_fp64 / ms_mixed,
         "mixed_coarsest_fp64": {"ms_per_solve": ms_mixed_c64, "cycles": nit_c64, "res": res_c64,
                                 "note": "coarsest-level smoothing in FP64 (the default runs it in FP32 "
-                                        "when the coarsest level exceeds 5000 cells)"},
+                                        "when the coarsest level exceeds 1250 cells)"},
         "mixed_rel_err_vs_fp64": err,
         "e2e": {"value": ms_e2e / world, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "wall_ms_per_step": wall_e2e},
@@ -485,6 +485,64 @@ def run_batch(args, rank, world, local):
             "all_converged": bool(np.all(res <= TOL)), "clocks": clk.summary()}
 
 
+def run_adjoint(args, rank, world, local):
+    """Configuration 5: forward + adjoint solves of variable-coefficient
+    problems (mixed precision, FP64 residuals, to 1e-12), the gradients
+    dL/db and dL/dkappa of L = 1/2 |P x - x*|^2, and a central finite-
+    difference check along random directions at full size."""
+    import numpy as np
+    import torch
+
+    import cfmg
+    import fixtures as F
+    import workloads as W
+
+    torch.cuda.set_device(local)
+    n = args.n if args.n != 4096 else 2048
+    param, probs = W.config5(ninst=args.ninst if args.ninst != 2048 else 16, n=n)
+    mg = cfmg.get_gmg(cfmg.Param(**param, tol=1e-12, maxite=80, residual_norm="l2", precision="mixed",
+                                 verbose=False))
+
+    def loss(msk, kap, b, xs):
+        mg.oper[1].msk = msk
+        mg.oper[1].kappa = kap
+        cfmg.setup_operators(mg)
+        for lev in range(1, mg.nlevels + 1):
+            for f in ("x", "y", "r", "b"):
+                cfmg.set_to_zero(mg, lev, f)
+        m = mg.download(1, "msk").astype(np.float64)
+        bb = b * m
+        F.subtract_mean(bb, m)
+        return cfmg.loss_and_grad(mg, bb, xs * m), m
+
+    times, fd_err = [], []
+    rng = np.random.default_rng(64)
+    for k, (msk, kap, b, xs) in enumerate(probs):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        (L0, gb, gk), m = loss(msk, kap, b, xs)
+        times.append((time.perf_counter() - t) * 1e3)
+        if k < args.steps:  # finite differences on the first instances
+            db = rng.standard_normal(b.shape) * m
+            db -= m * (db.sum() / m.sum())
+            dk = rng.standard_normal(b.shape) * m * 0.1
+            eps = 1e-5
+            lp = loss(msk, kap + eps * dk, b + eps * db, xs)[0][0]
+            lm = loss(msk, kap - eps * dk, b - eps * db, xs)[0][0]
+            fd = (lp - lm) / (2 * eps)
+            an = float(np.sum(gb * db) + np.sum(gk * dk))
+            fd_err.append(abs(fd - an) / abs(an))
+    ms = float(np.median(times))
+    return {"metric": f"ms per forward+adjoint solve ({n}^2 variable-coefficient, mixed, tol 1e-12)",
+            "value": ms, "unit": "ms/instance", "n_gpus": world, "steps": len(probs), "warmup": 0,
+            "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32-in-f64", "data": "synthetic (kappa = exp(0.5 smoothed N(0,1)), disk mask, seed 4)",
+            "config": {"workload": f"config5: {len(probs)} x {n}^2 div(kappa grad x) = b, forward + adjoint + "
+                                   f"dL/dkappa", "levels": mg.nlevels},
+            "fd_check": {"directions": len(fd_err), "max_rel_err": max(fd_err) if fd_err else None,
+                         "bound": 1e-6}}
+
+
 def dataclasses_asdict(p):
     import dataclasses
 
@@ -498,6 +556,8 @@ def main():
         out = run_reference(args, rank, world)
     elif args.workload == "config4":
         out = run_batch(args, rank, world, local)
+    elif args.workload == "config5":
+        out = run_adjoint(args, rank, world, local)
     else:
         out = run_ours(args, rank, world, local)
     if rank == 0 and out is not None:

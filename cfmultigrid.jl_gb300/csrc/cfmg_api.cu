@@ -26,7 +26,7 @@ struct cfmg_handle {
   cudaStream_t stream = nullptr;
   void* arena = nullptr;
   size_t arena_bytes = 0;
-  double* partials = nullptr;  // kNormParts FP64 partial sums
+  double* partials = nullptr;  // kPartials FP64 partial sums
   double* dscal = nullptr;     // device scalars, see enum Scal
   double* hscal = nullptr;     // pinned host mirror of dscal
   std::string err;
@@ -44,7 +44,7 @@ struct cfmg_handle {
   double prof_ms = 0.0;
   // coarse-level program engine
   bool engine_on = true;
-  long long engine_cells = 80000;  // levels of at most this many cells run in the engine
+  long long engine_cells = 20000;  // FP32 levels of at most this many cells run in the engine (FP64: 1/16)
   std::vector<cfmg::Op> pending;
   cfmg::Op* prog_pool = nullptr;   // device program store
   int pool_cap = 0, pool_used = 0;
@@ -1134,7 +1134,7 @@ static int create_handle(const cfmg_desc* d, cudaStream_t shared, cfmg_handle** 
   const bool mixed = d->precision == CFMG_MIXED;
   const bool vc = d->op == CFMG_VARCOEF;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  size_t total = al(kNormParts * sizeof(double)) + al(S_COUNT * sizeof(double)) + al((size_t)pool_ops * sizeof(Op));
+  size_t total = al(kPartials * sizeof(double)) + al(S_COUNT * sizeof(double)) + al((size_t)pool_ops * sizeof(Op));
   for (const Level& l : h->lv) {
     size_t n = l.len;
     total += 8 * al(n * 8) + al(n);           // x y r b diag idiag widiag Rcoef Pcoef + msk (Pcoef counted below)
@@ -1155,7 +1155,7 @@ static int create_handle(const cfmg_desc* d, cudaStream_t shared, cfmg_handle** 
     p += al(b);
     return q;
   };
-  h->partials = (double*)take(kNormParts * sizeof(double));
+  h->partials = (double*)take(kPartials * sizeof(double));
   h->prog_pool = (Op*)take((size_t)pool_ops * sizeof(Op));
   h->pool_cap = pool_ops;
   h->dscal = (double*)take(S_COUNT * sizeof(double));

@@ -100,6 +100,9 @@ template <class T>
 void launch_norm(const T* x, const uint8_t* msk, size_t n, double* partials, double* out, const double* normb,
                  int norm_kind, cudaStream_t s);
 constexpr int kNormParts = 1024;
+// the handle's partial-sum scratch: two sums per block for the fused
+// residual pass of the mixed loop (k_mixed.cu), one for the norms
+constexpr int kPartials = 2 * kNormParts;
 
 // ---- operator descriptors and the coarse-level program engine (k_coarse.cu)
 // One Op describes one launch-worth of work on one level: its kind, the

@@ -17,7 +17,8 @@
 namespace cfmg {
 
 constexpr int kMxThreads = 256;
-constexpr int kMxParts = 1024;  // blocks of the fused pass (= norm partials)
+constexpr int kMxParts = 1024;  // blocks of the fused pass; two sums each
+static_assert(2 * kMxParts <= kPartials, "the fused pass writes 2*kMxParts partial sums");
 
 // per-block partial sums -> 2 * kMxParts doubles: [sum r^2 | sum r]. With
 // NEUMANN the FP64 r is kept for the mean-removing pass and sum r is

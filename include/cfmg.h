@@ -96,7 +96,7 @@ extern "C" {
 /* options for cfmg_set_option */
 #define CFMG_OPT_ENGINE_CELLS 0 /* FP32 levels of at most this many cells (tx*ty*tz), FP64
                                    levels of at most 1/16 of it, run in the coarse-level
-                                   engine; 0 turns the engine off (default 80000) */
+                                   engine; 0 turns the engine off (default 20000) */
 #define CFMG_OPT_COARSEST_FP64 2 /* mixed form, coarsest-level smoothing in FP64: -1 (default) when the
                                     coarsest level holds at most 1/16 of CFMG_OPT_ENGINE_CELLS cells,
                                     0 never (FP32), 1 always */

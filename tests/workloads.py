@@ -104,3 +104,28 @@ def config4(ninst: int = 2048, seed: int = 3, lo: int = 64, hi: int = 1024, nh: 
         rhs = np.asfortranarray(rng.standard_normal((t, t, 1)))
         out.append((n, nlev, msk, rhs))
     return out
+
+
+def config5(ninst: int = 16, n: int = 2048, seed: int = 4, nh: int = 3):
+    """Adjoint config: ninst 2D cell-centred variable-coefficient problems,
+    div(kappa grad x) = b, kappa = exp(0.5 * gaussian_filter(N(0,1), 16))
+    (normalised to unit standard deviation of the smoothed field), disk
+    mask r = 0.45, b ~ N(0,1) on wet cells with the mean removed, and a
+    target x* ~ N(0,1) (seed 4). Returns (param dict, list of (msk, kappa,
+    b, xstar))."""
+    from scipy.ndimage import gaussian_filter
+
+    rng = np.random.default_rng(seed)
+    t = n + 2 * nh
+    msk = F.get_circular_domain((t, t, 1), nh=nh, radius=0.45)
+    out = []
+    for _ in range(ninst):
+        g = gaussian_filter(rng.standard_normal((t, t)), 16.0, mode="reflect", truncate=4.0)
+        kap = np.asfortranarray(np.exp(0.5 * g / g.std())[:, :, None])
+        b = np.asfortranarray(rng.standard_normal((t, t, 1)))
+        xs = np.asfortranarray(rng.standard_normal((t, t, 1)))
+        out.append((msk, kap, b, xs))
+    nlev = int(np.floor(np.log2(n / 8))) + 1
+    param = dict(nx=n, ny=n, nz=1, nh=nh, case="twod", location="centers", operator="varcoef", cycle="v", npre=2,
+                 npost=2, omega=0.8, ndeepest=20, nlevels=nlev)
+    return param, out
