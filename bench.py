@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--nlevels", type=int, default=0, help="levels (0: the deepest hierarchy that converges, 5)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the single-thread CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="config2", choices=["config2", "config4", "config5"],
+    ap.add_argument("--workload", default="config2", choices=["config2", "config3", "config4", "config5"],
                     help="config4: batched solves of uneven sizes (one engine launch per batch)")
     ap.add_argument("--ninst", type=int, default=2048, help="config4 batch size")
     ap.add_argument("--quick", action="store_true",
@@ -141,10 +141,10 @@ class Clocks:
 
 
 # ------------------------------------------------------------- our arm
-def make_gmg(cfmg, param, vmsk, noise, precision, stream_ptr):
+def make_gmg(cfmg, param, vmsk, noise, precision, stream_ptr, tol=TOL, maxite=MAXITE):
     import workloads as W
 
-    p = cfmg.Param(**param, tol=TOL, maxite=MAXITE, residual_norm="l2", precision=precision, verbose=False)
+    p = cfmg.Param(**param, tol=tol, maxite=maxite, residual_norm="l2", precision=precision, verbose=False)
     mg = cfmg.get_gmg(p)
     mg.set_stream(stream_ptr)
     mg.oper[1].msk = vmsk
@@ -417,6 +417,111 @@ def solve_l2(og):
     return res, nite
 
 
+def run_3d(args, rank, world, local):
+    """Configuration 3: 512 x 512 x 256 cell-centred 7-point masked Poisson
+    (coastline extruded in z, cut by a bottom topography), V-cycle,
+    8 levels, Jacobi 2/2, solved to ||r||/||b|| <= 1e-9 in the mixed form and
+    in the FP64 drop-in (whose pointwise arithmetic is the reference's, bit
+    for bit); the mixed solution's error against the FP64 one is reported."""
+    import numpy as np
+    import torch
+
+    import cfmg
+    import workloads as W
+
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    tol = 1e-9
+    n = args.n if args.n != 4096 else 512
+    param, msk, noise = W.config3(n, n, n // 2, nlevels=args.nlevels or 8)
+    mgm, b = make_gmg(cfmg, param, msk, noise, "mixed", sp, tol=tol, maxite=400)
+    mgd, _ = make_gmg(cfmg, param, msk, noise, "fp64", sp, tol=tol, maxite=400)
+    level_cells = [g.tx * g.ty * g.tz for g in mgm.levels]
+
+    def solve(mg):
+        cfmg.set_to_zero(mg, 1, "x")
+        return cfmg.solve(mg)
+
+    for _ in range(max(args.warmup, 3)):
+        res_m, nit_m = solve(mgm)
+    barrier(world)
+    torch.cuda.synchronize()
+    n0 = launch_count(cfmg, mgm)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            res_m, nit_m = solve(mgm)
+        e1.record(stream)
+        e1.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    ms_mixed = e0.elapsed_time(e1) / args.steps
+    launches = launch_count(cfmg, mgm) - n0
+    x_mixed = mgm.download(1, "x")
+
+    res_d, nit_d = solve(mgd)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    res_d, nit_d = solve(mgd)
+    e1.record(stream)
+    e1.synchronize()
+    ms_fp64 = e0.elapsed_time(e1)
+    x_fp64 = mgd.download(1, "x")
+    wet = mgm.download(1, "msk").astype(bool)
+    err = float(np.linalg.norm((x_mixed - x_fp64)[wet]) / np.linalg.norm(x_fp64[wet]))
+
+    hb = torch.from_numpy(np.ascontiguousarray(b.ravel(order="F"))).pin_memory()
+    hx = torch.empty_like(hb).pin_memory()
+    nbytes = hb.numel() * 8
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        mgm.upload_ptr(1, "b", hb.data_ptr())
+        cfmg.set_to_zero(mgm, 1, "x")
+        cfmg.solve(mgm)
+        mgm.download_ptr(1, "x", hx.data_ptr())
+    e1.record(stream)
+    e1.synchronize()
+    ms_e2e = e0.elapsed_time(e1) / args.steps
+
+    # roofline: one level-1 FP32 7-point Jacobi sweep of the mixed form
+    nl, tl = profile(cfmg, mgm, "sweep", 1, "mixed", lambda: solve(mgm))
+    g1 = mgm.levels[1]
+    sweep_cells = g1.tx * g1.ty * (g1.tz - 2)  # linear range 1+tx*ty : len-tx*ty
+    ms_launch = tl / max(nl, 1)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    bytes_per_launch = 16.0 * sweep_cells
+    achieved = bytes_per_launch / (ms_launch * 1e-3) / 1e9 if ms_launch > 0 else 0.0
+    ms_mixed = max_over_ranks(ms_mixed, world)
+    ms_e2e = max_over_ranks(ms_e2e, world)
+    return {"metric": f"ms/solve to 1e-9 rel residual (mixed FP32-in-FP64), {n}x{n}x{n // 2} cell-centred "
+                      "7-point V-cycle",
+            "value": ms_mixed / world, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-in-f64",
+            "data": "synthetic (seeded coastline x bottom-topography mask, N(0,1) rhs)",
+            "config": {"workload": f"config3: {n}x{n}x{n // 2} cell-centred 3D 7-point masked Poisson, V-cycle, "
+                                   f"{mgm.nlevels} levels, Jacobi 2/2, omega 0.8",
+                       "levels": mgm.nlevels, "fine_cells": level_cells[0], "tol_l2": tol,
+                       "l2_flush": "inputs larger than L2 (level-1 FP64 field = %.0f MB)" % (level_cells[0] * 8 / 1e6),
+                       "parallelism": f"replicas x{world}"},
+            "cycles_mixed": nit_m, "res_mixed": res_m, "cycles_fp64": nit_d, "res_fp64": res_d,
+            "ms_per_solve_fp64": ms_fp64, "mixed_speedup_vs_fp64": ms_fp64 / ms_mixed,
+            "mixed_rel_err_vs_fp64": err,
+            "e2e": {"value": ms_e2e / world, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+                    "d2h_bytes_per_step": nbytes},
+            "gpu_launches": launches,
+            "roofline": {"kernel": "FP32 7-point Jacobi sweep, level 1", "bound": "hbm", "achieved": achieved,
+                         "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                         "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)", "traffic": None,
+                         "launches_timed": nl, "ms_per_launch": ms_launch, "bytes_per_launch": bytes_per_launch},
+            "clocks": clk.summary()}
+
+
 def run_batch(args, rank, world, local):
     """Configuration 4: ninst independent 2D cell-centred 5-point masked
     solves (sizes log-uniform 64^2..1024^2, disk or noise masks) to 1e-10 in
@@ -554,6 +659,8 @@ def main():
     rank, world, local = dist_init()
     if args.impl == "reference":
         out = run_reference(args, rank, world)
+    elif args.workload == "config3":
+        out = run_3d(args, rank, world, local)
     elif args.workload == "config4":
         out = run_batch(args, rank, world, local)
     elif args.workload == "config5":

@@ -82,6 +82,11 @@ __global__ void __launch_bounds__(kTbW * kTbTy, 1) k_smooth_tb(const float* __re
   }
   __syncthreads();
 
+  // Warp-uniform fast path: threadIdx.y is constant across a warp, so a
+  // warp whose rows are all valid for a sweep, in a tile whose loaded
+  // region lies inside U, skips the per-row margin and per-cell U tests.
+  const int ti0 = ui0 + (int)blockIdx.x * CW - H, tj0 = uj0 + (int)blockIdx.y * CH - H;  // tile origin
+  const bool tile_in_u = ti0 >= ui0 && ti0 + kTbW - 1 <= ui1 && tj0 >= uj0 && tj0 + kTbH - 1 <= uj1;
 #pragma unroll 1
   for (int s = 0; s < 2 * NITE; ++s) {
     const float* src = (s & 1) ? Y : X;
@@ -101,20 +106,35 @@ __global__ void __launch_bounds__(kTbW * kTbTy, 1) k_smooth_tb(const float* __re
       w0 = src[r0 * kTbW + li - 1];
       c0 = src[r0 * kTbW + li];
       e0 = src[r0 * kTbW + li + 1];
+      if (tile_in_u && r0 >= m && r0 + kTbRows <= kTbH - m) {
 #pragma unroll
-      for (int r = 0; r < kTbRows; ++r) {
-        const int lj = r0 + r;
-        const int rn = (lj + 1 < kTbH) ? lj + 1 : lj;
-        const float wp = src[rn * kTbW + li - 1];
-        const float cp = src[rn * kTbW + li];
-        const float ep = src[rn * kTbW + li + 1];
-        if (lj >= m && lj < kTbH - m) {
-          dst[lj * kTbW + li] = (inU >> r & 1u)
-                                    ? tb_update<ST>(c0, W[lj * kTbW + li], B[lj * kTbW + li], cff, cp, cm, e0, w0, ep, wp, em, wm)
-                                    : c0;
+        for (int r = 0; r < kTbRows; ++r) {
+          const int lj = r0 + r;
+          const float wp = src[(lj + 1) * kTbW + li - 1];
+          const float cp = src[(lj + 1) * kTbW + li];
+          const float ep = src[(lj + 1) * kTbW + li + 1];
+          dst[lj * kTbW + li] = tb_update<ST>(c0, W[lj * kTbW + li], B[lj * kTbW + li], cff, cp, cm, e0, w0, ep, wp,
+                                              em, wm);
+          wm = w0; cm = c0; em = e0;
+          w0 = wp; c0 = cp; e0 = ep;
         }
-        wm = w0; cm = c0; em = e0;
-        w0 = wp; c0 = cp; e0 = ep;
+      } else {
+#pragma unroll
+        for (int r = 0; r < kTbRows; ++r) {
+          const int lj = r0 + r;
+          const int rn = (lj + 1 < kTbH) ? lj + 1 : lj;
+          const float wp = src[rn * kTbW + li - 1];
+          const float cp = src[rn * kTbW + li];
+          const float ep = src[rn * kTbW + li + 1];
+          if (lj >= m && lj < kTbH - m) {
+            dst[lj * kTbW + li] = (inU >> r & 1u)
+                                      ? tb_update<ST>(c0, W[lj * kTbW + li], B[lj * kTbW + li], cff, cp, cm, e0, w0,
+                                                      ep, wp, em, wm)
+                                      : c0;
+          }
+          wm = w0; cm = c0; em = e0;
+          w0 = wp; c0 = cp; e0 = ep;
+        }
       }
     }
     __syncthreads();

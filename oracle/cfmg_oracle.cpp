@@ -181,7 +181,7 @@ void residual_laplacian3d(orc_gmg* g, int lev) {
   Level& l = g->L(lev);
   const Grid& gr = l.g;
   const size_t n1 = gr.tx, n2 = (size_t)gr.tx * gr.ty;
-  #pragma omp parallel for schedule(static)
+  #pragma omp parallel for collapse(2) schedule(static)
   for (int k = gr.kc0(); k <= gr.kc1(); ++k)
     for (int j = gr.jc0(); j <= gr.jc1(); ++j)
       for (int i = gr.ic0(); i <= gr.ic1(); ++i) {
@@ -220,7 +220,7 @@ void smooth_laplacian9_3d(orc_gmg* g, int lev, int /*nite*/) {
   const Grid& gr = l.g;
   const size_t n1 = gr.tx, n2 = (size_t)gr.tx * gr.ty;
   const double omega = g->p.omega, cff = 1.0 - omega;
-  #pragma omp parallel for schedule(static)
+  #pragma omp parallel for collapse(2) schedule(static)
   for (int k = gr.nh; k <= gr.nz + gr.nh + 1; ++k)
     for (int j = gr.nh; j <= gr.ny + gr.nh + 1; ++j)
       for (int i = gr.nh; i <= gr.nx + gr.nh + 1; ++i) {
@@ -228,7 +228,7 @@ void smooth_laplacian9_3d(orc_gmg* g, int lev, int /*nite*/) {
         l.y[I] = cff * l.x[I] - (omega * l.idiag[I]) *
                                     ((l.b[I] - faces19(l.x, I, n1, n2) / 2) - edges19(l.x, I, n1, n2) / 4);
       }
-  #pragma omp parallel for schedule(static)
+  #pragma omp parallel for collapse(2) schedule(static)
   for (int k = gr.kc0(); k <= gr.kc1(); ++k)
     for (int j = gr.jc0(); j <= gr.jc1(); ++j)
       for (int i = gr.ic0(); i <= gr.ic1(); ++i) {
@@ -243,7 +243,7 @@ void residual_laplacian9_3d(orc_gmg* g, int lev) {
   Level& l = g->L(lev);
   const Grid& gr = l.g;
   const size_t n1 = gr.tx, n2 = (size_t)gr.tx * gr.ty;
-  #pragma omp parallel for schedule(static)
+  #pragma omp parallel for collapse(2) schedule(static)
   for (int k = gr.kc0(); k <= gr.kc1(); ++k)
     for (int j = gr.jc0(); j <= gr.jc1(); ++j)
       for (int i = gr.ic0(); i <= gr.ic1(); ++i) {
@@ -271,14 +271,14 @@ void smooth_laplacian9_2d(orc_gmg* g, int lev, int nite) {
   const size_t n1 = gr.tx;
   const double omega = g->p.omega, cff = 1.0 - omega;
   for (int kt = 0; kt < nite; ++kt) {
-    #pragma omp parallel for schedule(static)
+    #pragma omp parallel for collapse(2) schedule(static)
     for (int k = 1; k <= gr.nz; ++k)
       for (int j = gr.nh; j <= gr.ny + gr.nh + 1; ++j)
         for (int i = gr.nh; i <= gr.nx + gr.nh + 1; ++i) {
           size_t I = gr.at(i, j, k);
           l.y[I] = cff * l.x[I] - (omega * l.idiag[I]) * ((l.b[I] - faces9(l.x, I, n1) / 2) - diags9(l.x, I, n1) / 4);
         }
-    #pragma omp parallel for schedule(static)
+    #pragma omp parallel for collapse(2) schedule(static)
     for (int k = 1; k <= gr.nz; ++k)
       for (int j = gr.jc0(); j <= gr.jc1(); ++j)
         for (int i = gr.ic0(); i <= gr.ic1(); ++i) {
@@ -293,7 +293,7 @@ void residual_laplacian9_2d(orc_gmg* g, int lev) {
   Level& l = g->L(lev);
   const Grid& gr = l.g;
   const size_t n1 = gr.tx;
-  #pragma omp parallel for schedule(static)
+  #pragma omp parallel for collapse(2) schedule(static)
   for (int k = 1; k <= gr.nz; ++k)
     for (int j = gr.jc0(); j <= gr.jc1(); ++j)
       for (int i = gr.ic0(); i <= gr.ic1(); ++i) {
@@ -661,7 +661,7 @@ M default_msk(orc_gmg* g, int lev) {
       for (int j = nh + 2; j <= gr.ny + nh; ++j)
         for (int i = nh + 2; i <= gr.nx + nh; ++i) msk[gr.at(i, j, k)] = 1;
   } else {
-    #pragma omp parallel for schedule(static)
+    #pragma omp parallel for collapse(2) schedule(static)
     for (int k = gr.kc0(); k <= gr.kc1(); ++k)
       for (int j = gr.jc0(); j <= gr.jc1(); ++j)
         for (int i = gr.ic0(); i <= gr.ic1(); ++i) msk[gr.at(i, j, k)] = 1;

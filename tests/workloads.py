@@ -129,3 +129,39 @@ def config5(ninst: int = 16, n: int = 2048, seed: int = 4, nh: int = 3):
     param = dict(nx=n, ny=n, nz=1, nh=nh, case="twod", location="centers", operator="varcoef", cycle="v", npre=2,
                  npost=2, omega=0.8, ndeepest=20, nlevels=nlev)
     return param, out
+
+
+def config3(nx: int = 512, ny: int = 512, nz: int = 256, nh: int = 3, seed: int = 2, land: float = 0.30,
+            nlevels: int = 8, coast_sigma: float = 32.0, depth_sigma: float = 4.0):
+    """3D cell-centred 7-point config: the config-2 coastline recipe at
+    nx x ny (smoothed noise, sigma = 32 cells, 30 % land) extruded in z,
+    cut by a bottom topography: a column (i, j) is wet for k <= depth(i, j),
+    with depth = nz * gaussian_filter(U[0.2, 1], 4 cells). With the
+    coastline smoothed at 4 cells instead (32 scaled by 512/4096), the
+    reference's V-cycle stalls near 0.9 per cycle (CPU oracle, full size):
+    the coverage-thresholded coarse masks cut the narrow channels. Only the largest
+    face-connected wet region is kept: the operator is Neumann, and an
+    isolated pocket would make a mean-free right-hand side inconsistent.
+    RHS N(0,1) on wet cells (the wet mean is removed by ``rhs``). Returns
+    (param dict, level-1 mask, raw RHS noise)."""
+    from scipy.ndimage import gaussian_filter, label
+
+    rng = np.random.default_rng(seed)
+    noise = rng.standard_normal((nx, ny))
+    sm = gaussian_filter(noise, coast_sigma, mode="reflect", truncate=4.0)
+    coast = sm > np.quantile(sm, land)
+    depth = nz * gaussian_filter(rng.uniform(0.2, 1.0, (nx, ny)), depth_sigma, mode="reflect", truncate=4.0)
+    k = np.arange(1, nz + 1)
+    wet = coast[:, :, None] & (k[None, None, :] <= depth[:, :, None])
+    lab, nl = label(wet)
+    if nl > 1:
+        keep = 1 + int(np.argmax(np.bincount(lab.ravel())[1:]))
+        wet = lab == keep
+    del lab
+    tx, ty, tz = nx + 2 * nh, ny + 2 * nh, nz + 2 * nh
+    msk = np.zeros((tx, ty, tz), dtype=np.uint8, order="F")
+    msk[nh:nh + nx, nh:nh + ny, nh:nh + nz] = wet
+    rhs_noise = np.asfortranarray(rng.standard_normal((tx, ty, tz)))
+    param = dict(nx=nx, ny=ny, nz=nz, nh=nh, case="threed", location="centers", operator="laplacian", cycle="v",
+                 nlevels=nlevels, npre=2, npost=2, omega=0.8, ndeepest=20)
+    return param, msk, rhs_noise
