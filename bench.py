@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the single-thread CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="config2", choices=["config2", "config3", "config4", "config5"],
-                    help="config4: batched solves of uneven sizes (one engine launch per batch)")
+                    help="config3: the 3D 7-point case; config4: batched solves of uneven sizes (one graph launch per batch); config5: forward + adjoint solves")
     ap.add_argument("--ninst", type=int, default=2048, help="config4 batch size")
     ap.add_argument("--quick", action="store_true",
                     help="mixed form only: one warm-up and one timed solve (a short run for ncu)")
@@ -525,7 +525,7 @@ def run_3d(args, rank, world, local):
 def run_batch(args, rank, world, local):
     """Configuration 4: ninst independent 2D cell-centred 5-point masked
     solves (sizes log-uniform 64^2..1024^2, disk or noise masks) to 1e-10 in
-    one launch of the batched engine; the schedule is picked by the
+    one graph launch of the batched solver; the schedule is picked by the
     autotuner on a stratified sample. Reports the batch time and the p50/p99
     of the per-instance completion time (device clock)."""
     import numpy as np
@@ -539,8 +539,10 @@ def run_batch(args, rank, world, local):
     torch.cuda.set_device(local)
     probs = W.config4(args.ninst)
     sizes = [q[0] for q in probs]
+    # the slowest noise-coastline instances contract by ~0.8 per V-cycle
+    # (CPU oracle): 1e-10 takes up to ~110 cycles
     base = cfmg.Param(nx=64, ny=64, nz=1, case="twod", location="centers", operator="laplacian", cycle="v",
-                      npre=2, npost=2, omega=0.8, ndeepest=20, tol=TOL, maxite=MAXITE, residual_norm="l2",
+                      npre=2, npost=2, omega=0.8, ndeepest=20, tol=TOL, maxite=200, residual_norm="l2",
                       precision="mixed", verbose=False)
 
     def make(p, idx):
@@ -577,7 +579,7 @@ def run_batch(args, rank, world, local):
     ms = float(np.mean(times))
     td = np.concatenate(dones)
     cells = int(sum((n + 6) ** 2 for n in sizes))
-    return {"metric": f"ms per batch of {len(probs)} masked solves to 1e-10 (mixed, one engine launch)",
+    return {"metric": f"ms per batch of {len(probs)} masked solves to 1e-10 (mixed, one graph launch)",
             "value": ms, "unit": "ms/batch", "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
             "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32-in-f64", "data": "synthetic (seeded sizes, disk/noise masks, N(0,1) rhs)",

@@ -54,6 +54,7 @@ struct cfmg_handle {
   // adjoint scratch (level-1 FP64 arrays, allocated on the first cfmg_adjoint)
   double *adj_x = nullptr, *adj_b = nullptr, *adj_gk = nullptr;
   bool record = false;  // emit() records every Op (whole-solve programs) instead of running it
+  bool record_tb = false;  // while recording: temporally blocked smoothing is recorded as OPK_TB Ops
 };
 
 constexpr int kProgPoolOps = 8192;  // device store of engine programs (~1.9 MB)
@@ -78,6 +79,23 @@ struct cfmg_batch {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [zero_x]
   std::vector<double> hsc;
   std::string err;
+  // lockstep form (closed topology, 5- and 9-point): see k_batch.cu
+  bool lockstep = false;
+  BInst* bi = nullptr;         // per-instance level-1 state (device)
+  long long* l1start = nullptr;  // level-1 chunk prefix sums (device, ninst + 1)
+  long long l1chunks = 0;
+  double* bpart = nullptr;     // 2 partial sums per level-1 chunk
+  int* active = nullptr;       // per instance: still iterating
+  int* nactive = nullptr;      // instances continuing after this iteration
+  Op* sops = nullptr;          // the Ops of all cycle steps (device)
+  long long* scs = nullptr;    // their chunk (or tile) prefix sums (device)
+  struct Step {
+    int tb, stencil, nite;     // tb: OPK_TB Ops of one (stencil, nite)
+    long long op0, cs0;        // offsets into sops / scs
+    int nops;
+    long long nchunks;
+  };
+  std::vector<Step> steps;
 };
 
 
@@ -329,7 +347,7 @@ int sweep(cfmg_handle* h, int lev, int kind, const T* x, T* y, const Box* bx) {
 // topology, 2D 5- and 9-point): the result goes to the partner buffer.
 template <class T>
 bool tb_eligible(const cfmg_handle* h, int lev) {
-  if (sizeof(T) != 4 || !h->tb_on || h->record || xperio(h) || threed(h)) return false;
+  if (sizeof(T) != 4 || !h->tb_on || (h->record && !h->record_tb) || xperio(h) || threed(h)) return false;
   if (h->d.op != CFMG_LAPLACIAN && h->d.op != CFMG_LAPLACIAN9) return false;
   const Level& l = h->lv[lev - 1];
   return !(h->engine_on && (long long)l.len <= engine_limit(h, CFMG_MIXED));
@@ -342,6 +360,20 @@ int smooth_tb(cfmg_handle* h, int lev, int nite) {
   for (int left = nite; left > 0;) {
     const int n = left > 3 ? 3 : left;
     View<float> v = view<float>(l);
+    if (h->record) {  // the batched solver runs this pass (OPK_TB)
+      Op op = mkop(OPK_TB, 1, lev, CFMG_K_SWEEP, l);
+      op.x = v.x; op.y = v.y; op.b = v.b; op.w = v.widiag;
+      op.cff = 1.0 - h->d.omega;
+      op.box = Box{l.nh, l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, 1, l.tz};
+      op.np_i = n;
+      op.np_j = stencil;
+      tb_tiles(n, op.box.i0, op.box.i1, op.box.j0, op.box.j1, &op.kf0, &op.kf1);
+      op.n = (long long)op.kf0 * op.kf1 * l.tz;
+      h->pending.push_back(op);
+      l.xswap ^= 1;
+      left -= n;
+      continue;
+    }
     {
       Launch k(h, CFMG_K_SWEEP, lev, CFMG_MIXED);
       launch_smooth_tb(stencil, n, v.x, v.y, v.b, v.widiag, (float)(1.0 - h->d.omega), l.tx, l.ty, l.tz, l.nh,
@@ -1587,6 +1619,245 @@ int batch_build(cfmg_batch* b) {
   return CFMG_OK;
 }
 
+// ---------------------------------------------------- lockstep batches
+// One FP32 cycle of every instance as a sequence of steps aligned at the
+// coarsest level: depth d is level nlev - d + 1 of an instance, which takes
+// part in a step when nlev >= need.
+enum VOp { V_SMOOTH, V_RESID, V_RESTRICT, V_ZERO, V_PROLONG, V_COARSEST };
+struct VStep {
+  int op, depth, need, arg;
+};
+
+// vcycle! from depth `top` (src/gmg_cycles.jl:67-83); `fblock`: a V-cycle
+// inside the F-cycle, taken only by instances with at least `top` levels
+void vsteps_v(std::vector<VStep>& s, const cfmg_desc& d, int top, bool fblock) {
+  for (int dp = top; dp >= 2; --dp) {
+    const int need = fblock ? top : dp;
+    s.push_back({V_SMOOTH, dp, need, d.npre});
+    s.push_back({V_RESID, dp, need, 0});
+    s.push_back({V_RESTRICT, dp, need, CFMG_R});
+    s.push_back({V_ZERO, dp - 1, need, 0});
+  }
+  s.push_back({V_COARSEST, 1, fblock ? top : 1, d.ndeepest});
+  for (int dp = 2; dp <= top; ++dp) {
+    const int need = fblock ? top : dp;
+    s.push_back({V_PROLONG, dp, need, 0});
+    s.push_back({V_SMOOTH, dp, need, d.npost});
+  }
+}
+
+// fcycle! (src/gmg_cycles.jl:85-100): arg of a restriction at depth dp is
+// resolved per instance (:r on level 1, :b below)
+void vsteps_f(std::vector<VStep>& s, const cfmg_desc& d, int D) {
+  for (int dp = D; dp >= 2; --dp) {
+    s.push_back({V_RESTRICT, dp, dp, -1});
+    s.push_back({V_ZERO, dp - 1, dp, 0});
+  }
+  s.push_back({V_COARSEST, 1, 1, d.ndeepest});
+  for (int e = 2; e <= D; ++e) {
+    s.push_back({V_PROLONG, e, e, 0});
+    vsteps_v(s, d, e, true);
+  }
+}
+
+int record_vstep(cfmg_handle* h, const VStep& v, std::vector<Op>& out) {
+  const int nl = L(h);
+  const int lev = nl - v.depth + 1;
+  h->record = true;
+  h->pending.clear();
+  int rc = CFMG_OK;
+  switch (v.op) {
+    case V_SMOOTH: rc = smooth_t<float>(h, lev, v.arg); break;
+    case V_RESID: rc = residual_t<float>(h, lev); break;
+    case V_RESTRICT: rc = restrict_t<float>(h, lev, v.arg >= 0 ? v.arg : (lev > 1 ? CFMG_B : CFMG_R)); break;
+    case V_ZERO: rc = zero_t<float>(h, lev, CFMG_X); break;
+    case V_PROLONG: rc = prolong_t<float>(h, lev); break;
+    case V_COARSEST: rc = coarsest_t<float>(h, v.arg); break;
+  }
+  h->record = false;
+  out.swap(h->pending);
+  h->pending.clear();
+  return rc;
+}
+
+int lockstep_build(cfmg_batch* b) {
+  const int ninst = (int)b->inst.size();
+  const cfmg_desc& d = b->d;
+  b->nsc = BS_HIST + d.maxite + 2;
+  BCUDA(b, cudaMalloc((void**)&b->sc, sizeof(double) * (size_t)ninst * b->nsc));
+  BCUDA(b, cudaMemsetAsync(b->sc, 0, sizeof(double) * (size_t)ninst * b->nsc, b->stream));
+  int D = 0;
+  for (int i = 0; i < ninst; ++i) {
+    cfmg_handle* h = b->inst[i];
+    int rc = prepare_mixed(h);
+    if (rc != CFMG_OK) return bfail(b, rc, "instance " + std::to_string(i) + ": " + h->err);
+    BCUDA(b, cudaMemcpyAsync(b->sc + (size_t)i * b->nsc + BS_NWET, h->dscal + S_NWET, sizeof(double),
+                             cudaMemcpyDeviceToDevice, b->stream));
+    D = std::max(D, L(h));
+  }
+  // the cycle's steps; an instance whose blocked passes would not leave every
+  // FP32 x in its own buffer after one cycle is recorded without them
+  std::vector<VStep> vs;
+  vs.push_back({V_ZERO, 0, 1, 0});  // level 1 (resolved below): x = 0 before the cycle
+  if (d.cycle == CFMG_CYCLE_F) vsteps_f(vs, d, D);
+  else vsteps_v(vs, d, D, false);
+  std::vector<std::vector<std::vector<Op>>> rec(ninst);  // [inst][step] -> Ops
+  for (int i = 0; i < ninst; ++i) {
+    cfmg_handle* h = b->inst[i];
+    for (int pass = 0; pass < 2; ++pass) {
+      h->record_tb = pass == 0;
+      for (Level& l : h->lv) l.xswap = 0;
+      rec[i].assign(vs.size(), {});
+      for (size_t k = 0; k < vs.size(); ++k) {
+        VStep v = vs[k];
+        if (L(h) < v.need) continue;
+        if (k == 0) v.depth = L(h);
+        if (L(h) == 1 && v.op != V_ZERO && v.op != V_COARSEST) continue;
+        int rc = record_vstep(h, v, rec[i][k]);
+        if (rc != CFMG_OK) return bfail(b, rc, "instance " + std::to_string(i) + ": " + h->err);
+        for (Op& op : rec[i][k]) op.inst = i;
+      }
+      bool home = true;
+      for (const Level& l : h->lv) home = home && l.xswap == 0;
+      if (home) break;
+      if (pass == 1) return bfail(b, CFMG_ERR_UNSUPPORTED, "batched cycle leaves an FP32 field swapped");
+    }
+    h->record_tb = false;
+  }
+  // launches: per step, the k-th Op of every instance; OPK_TB Ops of one
+  // (stencil, pairs) go to the blocked kernel, the rest to the generic one
+  std::vector<Op> all;
+  std::vector<long long> cs;
+  auto add_step = [&](std::vector<Op>& ops, int tb, int stencil, int nite) {
+    if (ops.empty()) return;
+    cfmg_batch::Step st;
+    st.tb = tb; st.stencil = stencil; st.nite = nite;
+    st.op0 = (long long)all.size();
+    st.cs0 = (long long)cs.size();
+    st.nops = (int)ops.size();
+    long long acc = 0;
+    for (const Op& op : ops) {
+      cs.push_back(acc);
+      acc += tb ? op.n : (op.n + kBChunk - 1) / kBChunk;
+    }
+    cs.push_back(acc);
+    st.nchunks = acc;
+    all.insert(all.end(), ops.begin(), ops.end());
+    b->steps.push_back(st);
+  };
+  for (size_t k = 0; k < vs.size(); ++k) {
+    size_t depth = 0;
+    for (int i = 0; i < ninst; ++i) depth = std::max(depth, rec[i][k].size());
+    for (size_t q = 0; q < depth; ++q) {
+      std::vector<Op> gen;
+      std::vector<std::vector<Op>> tbs(8);  // [stencil 9?][pairs]
+      for (int i = 0; i < ninst; ++i) {
+        if (q >= rec[i][k].size()) continue;
+        const Op& op = rec[i][k][q];
+        if (op.kind == OPK_TB) tbs[(op.np_j == 9 ? 4 : 0) + op.np_i].push_back(op);
+        else gen.push_back(op);
+      }
+      for (int t = 0; t < 8; ++t) add_step(tbs[t], 1, t >= 4 ? 9 : 5, t & 3);
+      add_step(gen, 0, 0, 0);
+    }
+  }
+  // level-1 state and chunks
+  std::vector<BInst> hb(ninst);
+  std::vector<long long> l1(ninst + 1, 0);
+  for (int i = 0; i < ninst; ++i) {
+    cfmg_handle* h = b->inst[i];
+    const Level& l = h->lv[0];
+    BInst& B = hb[i];
+    std::memset(&B, 0, sizeof(B));
+    B.x = l.x; B.b = l.b; B.r = l.r; B.d = l.diag; B.m = l.msk;
+    B.b32 = l.b32; B.r32 = l.r32; B.e32 = view<float>(l).x;
+    B.sc = b->sc + (size_t)i * b->nsc;
+    B.g = geom(l);
+    B.box = interior(l);
+    B.kind = h->d.op == CFMG_LAPLACIAN9 ? OPK_RESID9 : OPK_RESID5;
+    if (B.kind == OPK_RESID5) {
+      B.lo = B.g.n1;
+      B.n = B.g.len - 2 * B.g.n1;
+    } else {
+      B.n = box_count(B.box);
+    }
+    B.len = (long long)l.len;
+    B.neumann = !vertices(h);
+    B.norm_kind = h->d.norm_kind;
+    B.maxite = h->d.maxite;
+    B.tol = h->d.tol;
+    l1[i + 1] = l1[i] + (B.len + kBChunk - 1) / kBChunk;
+  }
+  b->l1chunks = l1[ninst];
+  BCUDA(b, cudaMalloc((void**)&b->bi, sizeof(BInst) * ninst));
+  BCUDA(b, cudaMemcpy(b->bi, hb.data(), sizeof(BInst) * ninst, cudaMemcpyHostToDevice));
+  BCUDA(b, cudaMalloc((void**)&b->l1start, sizeof(long long) * (ninst + 1)));
+  BCUDA(b, cudaMemcpy(b->l1start, l1.data(), sizeof(long long) * (ninst + 1), cudaMemcpyHostToDevice));
+  BCUDA(b, cudaMalloc((void**)&b->bpart, sizeof(double) * 2 * (size_t)b->l1chunks));
+  BCUDA(b, cudaMalloc((void**)&b->active, sizeof(int) * ninst));
+  BCUDA(b, cudaMalloc((void**)&b->nactive, sizeof(int)));
+  BCUDA(b, cudaMemset(b->active, 0, sizeof(int) * ninst));
+  BCUDA(b, cudaMemset(b->nactive, 0, sizeof(int)));
+  if (!all.empty()) {
+    BCUDA(b, cudaMalloc((void**)&b->sops, sizeof(Op) * all.size()));
+    BCUDA(b, cudaMemcpy(b->sops, all.data(), sizeof(Op) * all.size(), cudaMemcpyHostToDevice));
+    BCUDA(b, cudaMalloc((void**)&b->scs, sizeof(long long) * cs.size()));
+    BCUDA(b, cudaMemcpy(b->scs, cs.data(), sizeof(long long) * cs.size(), cudaMemcpyHostToDevice));
+  }
+  const int kind = hb[0].kind;
+  const bool neumann = hb[0].neumann;
+  for (int i = 1; i < ninst; ++i)
+    if (hb[i].kind != kind || hb[i].neumann != neumann)
+      return bfail(b, CFMG_ERR_ARG, "batched instances must share the operator and location");
+  // the graph: init, then while (any instance iterates) { iteration }
+  for (int z = 0; z < 2; ++z) {
+    cudaGraph_t g = nullptr;
+    BCUDA(b, cudaGraphCreate(&g, 0));
+    BCUDA(b, cudaStreamBeginCaptureToGraph(b->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    launch_binit(b->bi, ninst, z, b->active, b->nactive, b->stream);
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (e != cudaSuccess) return bfail(b, CFMG_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+    cudaGraphNode_t init = nullptr;
+    size_t nn = 1;
+    BCUDA(b, cudaGraphGetNodes(g, &init, &nn));
+    cudaGraphConditionalHandle hc;
+    BCUDA(b, cudaGraphConditionalHandleCreate(&hc, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = hc;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    BCUDA(b, cudaGraphAddNode(&cnode, g, &init, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    BCUDA(b, cudaStreamBeginCaptureToGraph(b->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    launch_bres(kind, neumann, b->bi, b->l1start, ninst, b->l1chunks, b->active, b->bpart, b->stream);
+    launch_bfinal(b->bi, b->l1start, ninst, b->bpart, b->active, b->nactive, b->stream);
+    if (neumann) launch_brhs(b->bi, b->l1start, ninst, b->l1chunks, b->active, b->stream);
+    for (const cfmg_batch::Step& st : b->steps) {
+      if (st.tb) {
+        if (!launch_btb(st.stencil, st.nite, b->sops + st.op0, b->scs + st.cs0, st.nops, st.nchunks, b->active,
+                        b->stream)) {
+          cudaStreamEndCapture(b->stream, &body);
+          return bfail(b, CFMG_ERR_UNSUPPORTED, "blocked pass shape");
+        }
+      } else {
+        launch_bstage(b->sops + st.op0, b->scs + st.cs0, st.nops, st.nchunks, b->active, b->stream);
+      }
+    }
+    launch_bupdate(b->bi, b->l1start, ninst, b->l1chunks, b->active, b->stream);
+    launch_bcond(hc, b->nactive, b->stream);
+    e = cudaStreamEndCapture(b->stream, &body);
+    if (e != cudaSuccess) return bfail(b, CFMG_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&b->graph[z], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return bfail(b, CFMG_ERR_CUDA, std::string("batch instantiate: ") + cudaGetErrorString(e));
+  }
+  b->hsc.resize((size_t)ninst * b->nsc);
+  b->built = true;
+  return CFMG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1615,9 +1886,10 @@ int cfmg_batch_create(const cfmg_desc* d, int ninst, const int* nx, const int* n
       cfmg_batch_destroy(b);
       return fail(nullptr, rc, "batch instance " + std::to_string(i) + ": " + cfmg_last_error(nullptr));
     }
-    h->tb_on = false;  // instance handles run through the engine only
     b->inst.push_back(h);
   }
+  b->lockstep = fused_ok(b->inst[0]);
+  for (cfmg_handle* h : b->inst) h->tb_on = b->lockstep;  // the engine form runs no blocked passes
   *out = b;
   return CFMG_OK;
 }
@@ -1629,7 +1901,8 @@ int cfmg_batch_destroy(cfmg_batch* b) {
     if (g) cudaGraphExecDestroy(g);
   for (cfmg_handle* h : b->inst) cfmg_destroy(h);
   for (void* p : {(void*)b->progs, (void*)b->ptrs, (void*)b->nops, (void*)b->counter, (void*)b->red, (void*)b->sc,
-                  (void*)b->nwet})
+                  (void*)b->nwet, (void*)b->bi, (void*)b->l1start, (void*)b->bpart, (void*)b->active,
+                  (void*)b->nactive, (void*)b->sops, (void*)b->scs})
     if (p) cudaFree(p);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
@@ -1655,24 +1928,28 @@ int cfmg_batch_solve(cfmg_batch* b, int zero_x, double* res, int* nite, double* 
         g = nullptr;
       }
     for (void** p : {(void**)&b->progs, (void**)&b->ptrs, (void**)&b->nops, (void**)&b->counter, (void**)&b->red,
-                     (void**)&b->sc, (void**)&b->nwet})
+                     (void**)&b->sc, (void**)&b->nwet, (void**)&b->bi, (void**)&b->l1start, (void**)&b->bpart,
+                     (void**)&b->active, (void**)&b->nactive, (void**)&b->sops, (void**)&b->scs})
       if (*p) {
         cudaFree(*p);
         *p = nullptr;
       }
-    TRY(batch_build(b));
+    b->steps.clear();
+    TRY(b->lockstep ? lockstep_build(b) : batch_build(b));
   }
   BCUDA(b, cudaGraphLaunch(b->graph[zero_x ? 1 : 0], b->stream));
   const int ninst = (int)b->inst.size();
   BCUDA(b, cudaMemcpyAsync(b->hsc.data(), b->sc, sizeof(double) * b->hsc.size(), cudaMemcpyDeviceToHost, b->stream));
   BCUDA(b, cudaStreamSynchronize(b->stream));
+  const int kt0 = b->lockstep ? (int)BS_T0 : (int)SS_T0, kt1 = b->lockstep ? (int)BS_T1 : (int)SS_T1;
+  const int kres = b->lockstep ? (int)BS_RES : (int)SS_RES, knite = b->lockstep ? (int)BS_NITE : (int)SS_NITE;
   double t0 = 1e300;
-  for (int i = 0; i < ninst; ++i) t0 = std::min(t0, b->hsc[(size_t)i * b->nsc + SS_T0]);
+  for (int i = 0; i < ninst; ++i) t0 = std::min(t0, b->hsc[(size_t)i * b->nsc + kt0]);
   for (int i = 0; i < ninst; ++i) {
     const double* c = &b->hsc[(size_t)i * b->nsc];
-    if (res) res[i] = c[SS_RES];
-    if (nite) nite[i] = (int)c[SS_NITE];
-    if (t_done_ms) t_done_ms[i] = (c[SS_T1] - t0) * 1e-6;
+    if (res) res[i] = c[kres];
+    if (nite) nite[i] = (int)c[knite];
+    if (t_done_ms) t_done_ms[i] = (c[kt1] - t0) * 1e-6;
   }
   return CFMG_OK;
 }

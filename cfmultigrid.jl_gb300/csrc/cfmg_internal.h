@@ -129,6 +129,10 @@ enum OpKind : int {
   OPK_STAMP,     // sc[s0] = %globaltimer (ns)
   OPK_HIST,      // sc[s0 + sc[s1]] = sc[s2]
   OPK_ZERO_IF,   // y[0..n) = 0 (double) when sc[s0] != 0
+  // batched solver: one temporally blocked FP32 smoothing pass, x -> y over
+  // the update box `box`; np_i = sweep pairs (1..3), np_j = stencil (5 or
+  // 9), kf0 x kf1 tiles per layer, n = tiles in all layers
+  OPK_TB,
 };
 struct Op {
   int kind, prec, lev, cls;  // cls: CFMG_K_* class for accounting
@@ -145,7 +149,8 @@ struct Op {
   double* sc;
   void* y2;
   double tol;
-  int s0, s1, s2, maxite, norm_kind, pad;
+  int s0, s1, s2, maxite, norm_kind;
+  int inst;  // batched solver: the instance the Op belongs to
 };
 // scalar block of a whole-solve program
 enum SolveSlot { SS_NORMB = 0, SS_NR, SS_RES, SS_NITE, SS_NWET, SS_MEAN, SS_SCALE, SS_ISCALE, SS_T0, SS_T1,
@@ -162,6 +167,46 @@ void launch_program(const Op* prog, int nops, double* red, cudaStream_t s);  // 
 // sweeps over the box U in one pass, x -> xo; false if nite is not 1..4
 bool launch_smooth_tb(int stencil, int nite, const float* x, float* xo, const float* b, const float* w, float cff,
                       int tx, int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s);
+
+// ---- batched solver (k_batch.cu): independent 2D instances advance in
+// lockstep, one launch per step of the iteration for all of them. Every
+// launch is a grid-stride loop over the chunks (kBChunk work items) of its
+// Ops; a chunk of an instance that has converged is skipped.
+constexpr int kBChunk = 4096;
+constexpr int kBThreads = 256;
+// per-instance scalar block (double): see k_bfinal for their use
+enum BSlot { BS_NORMB = 0, BS_RES, BS_NITE, BS_NWET, BS_NEXT, BS_CUR, BS_ICUR, BS_MEAN, BS_T0, BS_T1, BS_ZEROX,
+             BS_HIST };
+// level-1 state of one instance for the FP64 steps of its solve loop
+struct BInst {
+  double *x, *b, *r, *d;
+  const uint8_t* m;
+  float *b32, *r32;
+  const float* e32;  // the FP32 correction after the cycle
+  double* sc;        // scalar block (BSlot)
+  Geom g;
+  Box box;
+  long long lo, n;   // the residual's index space: linear lo + t (5-point) or the box (9-point)
+  long long len;
+  int kind, neumann, norm_kind, maxite;
+  double tol;
+};
+// chunks: cstart[i] = first chunk of item i (prefix sums, cstart[nitems] = total)
+void launch_bstage(const Op* ops, const long long* cstart, int nops, long long nchunks, const int* active,
+                   cudaStream_t s);
+void tb_tiles(int nite, int ui0, int ui1, int uj0, int uj1, int* ntx, int* nty);
+bool launch_btb(int stencil, int nite, const Op* ops, const long long* tstart, int nops, long long ntiles,
+                const int* active, cudaStream_t s);
+void launch_binit(const BInst* bi, int ninst, int zero_x, int* active, int* nactive, cudaStream_t s);
+void launch_bres(int kind, bool neumann, const BInst* bi, const long long* cstart, int ninst, long long nchunks,
+                 const int* active, double* partials, cudaStream_t s);
+void launch_bfinal(const BInst* bi, const long long* cstart, int ninst, const double* partials, int* active,
+                   int* nactive, cudaStream_t s);
+void launch_brhs(const BInst* bi, const long long* cstart, int ninst, long long nchunks, const int* active,
+                 cudaStream_t s);
+void launch_bupdate(const BInst* bi, const long long* cstart, int ninst, long long nchunks, const int* active,
+                    cudaStream_t s);
+void launch_bcond(cudaGraphConditionalHandle hc, int* nactive, cudaStream_t s);
 
 // device scalars of a handle (dscal[])
 enum Scal { S_NORM = 0, S_RES = 1, S_NORMB = 2, S_NWET = 3, S_SCALE = 4, S_MEAN = 5, S_TMP0 = 6, S_ISCALE = 7,

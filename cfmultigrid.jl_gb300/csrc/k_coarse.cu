@@ -8,7 +8,7 @@
 // barrier (release/acquire at cluster scope) makes the Op's global-memory
 // writes visible before the next Op reads them. The per-cell arithmetic is
 // the same device code as the standalone kernels, so results are identical.
-#include "ops_dev.cuh"
+#include "exec_dev.cuh"
 
 namespace cfmg {
 
@@ -19,104 +19,6 @@ __device__ __forceinline__ unsigned cluster_rank() {
 }
 __device__ __forceinline__ void cluster_barrier() {
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
-__device__ __forceinline__ void box3(const Box& b, long long t, int& i, int& j, int& k) {
-  const long long ni = b.i1 - b.i0 + 1, nj = b.j1 - b.j0 + 1;
-  i = b.i0 + (int)(t % ni);
-  const long long q = t / ni;
-  j = b.j0 + (int)(q % nj);
-  k = b.k0 + (int)(q / nj);
-}
-
-template <class T>
-__device__ void exec(const Op& op, long long t, long long st) {
-  const T* x = (const T*)op.x;
-  const T* b = (const T*)op.b;
-  const T* w = (const T*)op.w;
-  const T* d = (const T*)op.d;
-  T* y = (T*)op.y;
-  const T cff = (T)op.cff;
-  const long long n1 = op.g.n1, n2 = op.g.n2;
-  int i, j, k;
-  switch (op.kind) {
-    case OPK_SWEEP5:
-      for (; t < op.n; t += st) d_sweep5(x, y, b, w, cff, n1, op.lo + t);
-      break;
-    case OPK_SWEEP7:
-      for (; t < op.n; t += st) d_sweep7(x, y, b, w, cff, n1, n2, op.lo + t);
-      break;
-    case OPK_SWEEPVC:
-      for (; t < op.n; t += st) d_sweepvc(x, y, b, w, (const T*)op.cE, (const T*)op.cN, cff, n1, op.lo + t);
-      break;
-    case OPK_SWEEP9:
-      for (; t < op.n; t += st) {
-        box3(op.box, t, i, j, k);
-        d_sweep9(x, y, b, w, cff, n1, lin(op.g, i, j, k));
-      }
-      break;
-    case OPK_SWEEP19:
-      for (; t < op.n; t += st) {
-        box3(op.box, t, i, j, k);
-        d_sweep19(x, y, b, w, cff, n1, n2, lin(op.g, i, j, k));
-      }
-      break;
-    case OPK_RESID5:
-      for (; t < op.n; t += st) d_resid5(y, x, b, d, op.m, n1, op.lo + t);
-      break;
-    case OPK_RESIDVC:
-      for (; t < op.n; t += st) d_residvc(y, x, b, d, (const T*)op.cE, (const T*)op.cN, op.m, n1, op.lo + t);
-      break;
-    case OPK_RESID7:
-      for (; t < op.n; t += st) {
-        box3(op.box, t, i, j, k);
-        d_resid7(y, x, b, d, op.m, n1, n2, lin(op.g, i, j, k));
-      }
-      break;
-    case OPK_RESID9:
-      for (; t < op.n; t += st) {
-        box3(op.box, t, i, j, k);
-        d_resid9(y, x, b, d, op.m, n1, lin(op.g, i, j, k));
-      }
-      break;
-    case OPK_RESID19:
-      for (; t < op.n; t += st) {
-        box3(op.box, t, i, j, k);
-        d_resid19(y, x, b, d, op.m, n1, n2, lin(op.g, i, j, k));
-      }
-      break;
-#define CFMG_RESTRICT_CASE(K)                                                  \
-  case OPK_RESTRICT0 + K:                                                      \
-    for (; t < op.n; t += st) {                                                \
-      box3(op.box, t, i, j, k);                                                \
-      d_restrict<T, K>(x, y, (const T*)op.coef, op.g, op.gc, i, j, k);         \
-    }                                                                          \
-    break;
-      CFMG_RESTRICT_CASE(0)
-      CFMG_RESTRICT_CASE(1)
-      CFMG_RESTRICT_CASE(2)
-      CFMG_RESTRICT_CASE(3)
-#define CFMG_PROLONG_CASE(K)                                                   \
-  case OPK_PROLONG0 + K:                                                       \
-    for (; t < op.n; t += st) {                                                \
-      const int p = (int)(t % op.np_i);                                        \
-      const long long q = t / op.np_i;                                         \
-      d_prolong<T, K>(y, x, (const T*)op.coef, op.g, op.gc, p, (int)(q % op.np_j), (int)(q / op.np_j), op.kf0); \
-    }                                                                          \
-    break;
-      CFMG_PROLONG_CASE(0)
-      CFMG_PROLONG_CASE(1)
-      CFMG_PROLONG_CASE(2)
-      CFMG_PROLONG_CASE(3)
-    case OPK_FILL:
-      for (; t < op.n; t += st) d_fill_line(y + t * op.g.tx, op.g.tx, op.g.nh);
-      break;
-    case OPK_ZERO:
-      for (; t < op.n; t += st) y[t] = T(0);
-      break;
-    default:
-      break;
-  }
 }
 
 // Block-wide FP64 sum (fixed order: warp shuffles, then warp 0 over the
@@ -249,8 +151,8 @@ __device__ void run_program(const Op* __restrict__ prog, int nops, long long t0,
           for (long long t = t0; t < op.n; t += st) ((double*)op.y)[t] = 0.0;
         break;
       default:
-        if (op.prec == 0) exec<double>(op, t0, st);
-        else exec<float>(op, t0, st);
+        if (op.prec == 0) exec<double>(op, t0, st, op.n);
+        else exec<float>(op, t0, st, op.n);
         break;
     }
     cluster_barrier();

@@ -46,16 +46,16 @@ __device__ __forceinline__ float tb_update(float c, float wv, float bv, float cf
   }
 }
 
-// x: current x, xo: the other buffer (receives the smoothed field).
-// U (1-based, inclusive) is the update box; k-layers in blockIdx.z.
+// One tile: x is the current x, xo the other buffer (receives the
+// smoothed field). U (1-based, inclusive) is the update box; (bx, by) the
+// tile, bz the k-layer. smem holds 4 kTbH x kTbW floats.
 template <int ST, int NITE>
-__global__ void __launch_bounds__(kTbW * kTbTy, 1) k_smooth_tb(const float* __restrict__ x, float* __restrict__ xo,
-                                                               const float* __restrict__ b,
-                                                               const float* __restrict__ w, float cff, int tx,
-                                                               int ty, int ui0, int ui1, int uj0, int uj1) {
+__device__ __forceinline__ void tb_tile(const float* __restrict__ x, float* __restrict__ xo,
+                                        const float* __restrict__ b, const float* __restrict__ w, float cff, int tx,
+                                        int ty, int ui0, int ui1, int uj0, int uj1, int bx, int by, int bz,
+                                        float* smem) {
   constexpr int H = 2 * NITE;
   constexpr int CW = kTbW - 2 * H, CH = kTbH - 2 * H;
-  extern __shared__ float smem[];
   float* X = smem;               // [kTbH][kTbW]
   float* Y = smem + kTbH * kTbW;
   float* B = smem + 2 * kTbH * kTbW;
@@ -63,9 +63,9 @@ __global__ void __launch_bounds__(kTbW * kTbTy, 1) k_smooth_tb(const float* __re
 
   const int li = threadIdx.x;
   const int r0 = threadIdx.y * kTbRows;
-  const int gi = ui0 + (int)blockIdx.x * CW - H + li;  // 1-based global column
-  const int gj0 = uj0 + (int)blockIdx.y * CH - H + r0;  // first global row of this thread
-  const long long plane = (long long)tx * ty * blockIdx.z;
+  const int gi = ui0 + bx * CW - H + li;  // 1-based global column
+  const int gj0 = uj0 + by * CH - H + r0;  // first global row of this thread
+  const long long plane = (long long)tx * ty * bz;
 
   unsigned inU = 0;  // bit r: cell (gi, gj0+r) lies in U
   const bool col_in = gi >= 1 && gi <= tx;
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(kTbW * kTbTy, 1) k_smooth_tb(const float* __re
   // Warp-uniform fast path: threadIdx.y is constant across a warp, so a
   // warp whose rows are all valid for a sweep, in a tile whose loaded
   // region lies inside U, skips the per-row margin and per-cell U tests.
-  const int ti0 = ui0 + (int)blockIdx.x * CW - H, tj0 = uj0 + (int)blockIdx.y * CH - H;  // tile origin
+  const int ti0 = ui0 + bx * CW - H, tj0 = uj0 + by * CH - H;  // tile origin
   const bool tile_in_u = ti0 >= ui0 && ti0 + kTbW - 1 <= ui1 && tj0 >= uj0 && tj0 + kTbH - 1 <= uj1;
 #pragma unroll 1
   for (int s = 0; s < 2 * NITE; ++s) {
@@ -153,6 +153,45 @@ __global__ void __launch_bounds__(kTbW * kTbTy, 1) k_smooth_tb(const float* __re
 }
 
 template <int ST, int NITE>
+__global__ void __launch_bounds__(kTbW * kTbTy, 1) k_smooth_tb(const float* __restrict__ x, float* __restrict__ xo,
+                                                               const float* __restrict__ b,
+                                                               const float* __restrict__ w, float cff, int tx,
+                                                               int ty, int ui0, int ui1, int uj0, int uj1) {
+  extern __shared__ float smem[];
+  tb_tile<ST, NITE>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z,
+                    smem);
+}
+
+// Batched form: a grid-stride loop over the tiles of many OPK_TB Ops
+// (tstart: prefix sums of their tile counts); tiles of converged instances
+// are skipped. The barrier at the end of each tile keeps the next tile's
+// loads behind this tile's last shared-memory reads.
+template <int ST, int NITE>
+__global__ void __launch_bounds__(kTbW * kTbTy, 1) k_btb(const Op* __restrict__ ops,
+                                                         const long long* __restrict__ tstart, int nops,
+                                                         long long ntiles, const int* __restrict__ active) {
+  extern __shared__ float smem[];
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    int lo = 0, hi = nops - 1;  // last op with tstart[op] <= t
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tstart[mid] <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    const Op& op = ops[lo];
+    if (!active[op.inst]) continue;
+    const long long q = t - tstart[lo];
+    const long long per_layer = (long long)op.kf0 * op.kf1;
+    const int bz = (int)(q / per_layer);
+    const int rem = (int)(q - (long long)bz * per_layer);
+    tb_tile<ST, NITE>((const float*)op.x, (float*)op.y, (const float*)op.b, (const float*)op.w, (float)op.cff,
+                      op.g.tx, op.g.ty, op.box.i0, op.box.i1, op.box.j0, op.box.j1, rem % op.kf0, rem / op.kf0, bz,
+                      smem);
+    __syncthreads();
+  }
+}
+
+template <int ST, int NITE>
 static void launch_tb_n(const float* x, float* xo, const float* b, const float* w, float cff, int tx, int ty, int nz,
                         int ui0, int ui1, int uj0, int uj1, cudaStream_t s) {
   constexpr int H = 2 * NITE;
@@ -179,6 +218,45 @@ bool launch_smooth_tb(int stencil, int nite, const float* x, float* xo, const fl
   CFMG_TB(5, 1) CFMG_TB(5, 2) CFMG_TB(5, 3) CFMG_TB(5, 4)
   CFMG_TB(9, 1) CFMG_TB(9, 2) CFMG_TB(9, 3) CFMG_TB(9, 4)
 #undef CFMG_TB
+  return false;
+}
+
+// tile counts of one pass over the box U (the host builds OPK_TB Ops with
+// these: kf0 x kf1 tiles per layer)
+void tb_tiles(int nite, int ui0, int ui1, int uj0, int uj1, int* ntx, int* nty) {
+  const int H = 2 * nite, CW = kTbW - 2 * H, CH = kTbH - 2 * H;
+  *ntx = (ui1 - ui0 + CW) / CW;
+  *nty = (uj1 - uj0 + CH) / CH;
+}
+
+template <int ST, int NITE>
+static void launch_btb_n(const Op* ops, const long long* tstart, int nops, long long ntiles, const int* active,
+                         cudaStream_t s) {
+  const size_t smem = 4 * (size_t)kTbH * kTbW * sizeof(float);
+  static bool attr = false;
+  static int nsm = 0;
+  if (!attr) {
+    cudaFuncSetAttribute(k_btb<ST, NITE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    attr = true;
+  }
+  const long long grid = ntiles < nsm ? ntiles : nsm;  // one resident CTA per SM
+  k_btb<ST, NITE><<<(unsigned)grid, dim3(kTbW, kTbTy, 1), smem, s>>>(ops, tstart, nops, ntiles, active);
+}
+
+bool launch_btb(int stencil, int nite, const Op* ops, const long long* tstart, int nops, long long ntiles,
+                const int* active, cudaStream_t s) {
+  if (ntiles <= 0) return true;
+#define CFMG_BTB(ST, N)                                              \
+  if (stencil == ST && nite == N) {                                  \
+    launch_btb_n<ST, N>(ops, tstart, nops, ntiles, active, s);       \
+    return true;                                                     \
+  }
+  CFMG_BTB(5, 1) CFMG_BTB(5, 2) CFMG_BTB(5, 3)
+  CFMG_BTB(9, 1) CFMG_BTB(9, 2) CFMG_BTB(9, 3)
+#undef CFMG_BTB
   return false;
 }
 

@@ -72,3 +72,36 @@ def dataclasses_replace(p, **kw):
     import dataclasses
 
     return dataclasses.replace(p, **kw)
+
+
+def test_batch_vertex_9point_matches_single_solves():
+    """Vertex-centred 9-point instances (the coastline-style operator of the
+    F-cycle configuration): the batched solve agrees with single solves,
+    and a second batched solve continuing from the converged x stops at
+    once."""
+    sizes = [96, 160, 256, 64, 200]
+    p = _param(location="vertices", operator="laplacian9", cycle="f", npre=3, npost=3, maxite=60)
+    nlev = [int(np.floor(np.log2(n / 8))) + 1 for n in sizes]
+    batch = cfmg.Batch(p, sizes, sizes, nlev)
+    rng = np.random.default_rng(11)
+    probs = []
+    for i, n in enumerate(sizes):
+        t = n + 6
+        cells = F.get_circular_domain((t, t, 1), nh=3, radius=0.45)
+        msk = F.get_mask_at_corners(cells)
+        noise = np.asfortranarray(rng.standard_normal((t, t, 1)))
+        probs.append((msk, noise))
+        _setup(batch.instance(i), msk, noise)
+    res, nite, _ = batch.solve()
+    assert np.all(res <= 1e-10), res
+    for i, n in enumerate(sizes):
+        g = batch.instance(i)
+        s = cfmg.get_gmg(dataclasses_replace(p, nx=n, ny=n, nlevels=nlev[i]))
+        _setup(s, *probs[i])
+        r1, n1 = cfmg.solve(s)
+        assert r1 <= 1e-10 and abs(int(nite[i]) - n1) <= 1, (i, nite[i], n1)
+        w = probs[i][0].astype(bool)
+        a, c = g.data[1].x[w], s.data[1].x[w]
+        assert np.linalg.norm(a - c) <= 1e-6 * np.linalg.norm(c), i
+    res2, nite2, _ = batch.solve(from_zero=False)
+    assert np.all(nite2 == 0) and np.all(res2 <= 1e-10), (nite2, res2)

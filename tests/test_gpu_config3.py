@@ -24,6 +24,9 @@ def _oracle(param, msk, noise):
     og = O.OracleGmg(dict(param, tol=TOL * TOL, maxite=60, verbose=False), setup=False)
     og.field(1, "msk")[...] = msk
     og.setup_operators()
+    for lev in range(1, og.nlevels + 1):  # the setup leaves x = msk; both sides start from 0
+        for f in ("x", "y", "r", "b"):
+            og.field(lev, f)[...] = 0.0
     b = W.rhs(noise, og.field(1, "msk"))
     og.field(1, "b")[...] = b
     return og, b
@@ -40,6 +43,58 @@ def _gpu(param, msk, b, precision):
             cfmg.set_to_zero(mg, lev, f)
     mg.data[1].b = b
     return mg
+
+
+def _pair():
+    param, msk, noise = _problem()
+    og, b = _oracle(param, msk, noise)
+    mg = _gpu(param, msk, b, "fp64")
+    return og, mg
+
+
+def test_config3_setup_bitwise():
+    og, mg = _pair()
+    assert og.nlevels == mg.nlevels
+    for lev in range(1, og.nlevels + 1):
+        for f in ("msk", "diag", "idiag", "Rcoef", "Pcoef"):
+            a, c = og.field(lev, f), mg.download(lev, f)
+            bad = np.argwhere(a != c)
+            assert bad.size == 0, (lev, f, len(bad), bad[:4].tolist(), a[tuple(bad[0])], c[tuple(bad[0])])
+
+
+@pytest.mark.parametrize("engine", ["engine", "standalone"])
+def test_config3_operators_bitwise(engine):
+    og, mg = _pair()
+    mg.set_option("engine_cells", 10**9 if engine == "engine" else 0)
+    rng = np.random.default_rng(3)
+    L = og.nlevels
+    for lev in range(1, L + 1):
+        for f in ("x", "b", "y", "r"):
+            a = np.asfortranarray(rng.standard_normal(og.shape(lev)))
+            og.field(lev, f)[...] = a
+            mg.upload(lev, f, a)
+
+    def check(what):
+        for lev in range(1, L + 1):
+            for f in ("x", "y", "r", "b"):
+                a, c = og.field(lev, f), mg.download(lev, f)
+                bad = np.argwhere(a != c)
+                assert bad.size == 0, (what, lev, f, len(bad), bad[:4].tolist())
+
+    for lev in range(1, L + 1):
+        og.smooth(lev, 2)
+        mg.smoother[lev](mg, lev, 2)
+        check(f"smooth{lev}")
+        og.residual(lev)
+        mg.residual[lev](mg, lev)
+        check(f"residual{lev}")
+    for lev in range(1, L):
+        og.restrict(lev, "r")
+        mg.restriction[lev](mg, lev, "r")
+        check(f"restrict{lev}")
+        og.prolong(lev)
+        mg.prolongation[lev](mg, lev)
+        check(f"prolong{lev}")
 
 
 def test_config3_fp64_matches_oracle():
