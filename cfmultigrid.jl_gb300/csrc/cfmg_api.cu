@@ -82,17 +82,17 @@ struct cfmg_batch {
   // lockstep form (closed topology, 5- and 9-point): see k_batch.cu
   bool lockstep = false;
   BInst* bi = nullptr;         // per-instance level-1 state (device)
-  long long* l1start = nullptr;  // level-1 chunk prefix sums (device, ninst + 1)
+  long long* l1start = nullptr;  // first level-1 chunk of each instance (device, ninst + 1)
+  int4* l1tab = nullptr;       // level-1 chunk table {instance, chunk, instance, 0}
   long long l1chunks = 0;
   double* bpart = nullptr;     // 2 partial sums per level-1 chunk
   int* active = nullptr;       // per instance: still iterating
   int* nactive = nullptr;      // instances continuing after this iteration
   Op* sops = nullptr;          // the Ops of all cycle steps (device)
-  long long* scs = nullptr;    // their chunk (or tile) prefix sums (device)
+  int4* stab = nullptr;        // their chunk (or tile) tables {Op, chunk, instance, 0} (device)
   struct Step {
     int tb, stencil, nite;     // tb: OPK_TB Ops of one (stencil, nite)
-    long long op0, cs0;        // offsets into sops / scs
-    int nops;
+    long long tab0;            // offset into stab
     long long nchunks;
   };
   std::vector<Step> steps;
@@ -357,8 +357,11 @@ int smooth_tb(cfmg_handle* h, int lev, int nite) {
   Level& l = h->lv[lev - 1];
   const int stencil = h->d.op == CFMG_LAPLACIAN9 ? 9 : 5;
   TRY(flush(h));
+  // up to 3 pairs per pass (kTbMaxPairs for a long smoothing such as the
+  // coarsest solve's; the batched solver's blocked kernel takes up to 3)
+  const int per = (nite > 3 && !h->record) ? kTbMaxPairs : 3;
   for (int left = nite; left > 0;) {
-    const int n = left > 3 ? 3 : left;
+    const int n = left > per ? per : left;
     View<float> v = view<float>(l);
     if (h->record) {  // the batched solver runs this pass (OPK_TB)
       Op op = mkop(OPK_TB, 1, lev, CFMG_K_SWEEP, l);
@@ -1727,22 +1730,19 @@ int lockstep_build(cfmg_batch* b) {
   // launches: per step, the k-th Op of every instance; OPK_TB Ops of one
   // (stencil, pairs) go to the blocked kernel, the rest to the generic one
   std::vector<Op> all;
-  std::vector<long long> cs;
+  std::vector<int4> tab;
   auto add_step = [&](std::vector<Op>& ops, int tb, int stencil, int nite) {
     if (ops.empty()) return;
     cfmg_batch::Step st;
     st.tb = tb; st.stencil = stencil; st.nite = nite;
-    st.op0 = (long long)all.size();
-    st.cs0 = (long long)cs.size();
-    st.nops = (int)ops.size();
-    long long acc = 0;
+    st.tab0 = (long long)tab.size();
     for (const Op& op : ops) {
-      cs.push_back(acc);
-      acc += tb ? op.n : (op.n + kBChunk - 1) / kBChunk;
+      const int o = (int)all.size();
+      all.push_back(op);
+      const long long nc = tb ? op.n : (op.n + kBChunk - 1) / kBChunk;
+      for (long long c = 0; c < nc; ++c) tab.push_back(make_int4(o, (int)c, op.inst, 0));
     }
-    cs.push_back(acc);
-    st.nchunks = acc;
-    all.insert(all.end(), ops.begin(), ops.end());
+    st.nchunks = (long long)tab.size() - st.tab0;
     b->steps.push_back(st);
   };
   for (size_t k = 0; k < vs.size(); ++k) {
@@ -1789,6 +1789,11 @@ int lockstep_build(cfmg_batch* b) {
     l1[i + 1] = l1[i] + (B.len + kBChunk - 1) / kBChunk;
   }
   b->l1chunks = l1[ninst];
+  std::vector<int4> l1t((size_t)b->l1chunks);
+  for (int i = 0; i < ninst; ++i)
+    for (long long c = l1[i]; c < l1[i + 1]; ++c) l1t[c] = make_int4(i, (int)(c - l1[i]), i, 0);
+  BCUDA(b, cudaMalloc((void**)&b->l1tab, sizeof(int4) * l1t.size()));
+  BCUDA(b, cudaMemcpy(b->l1tab, l1t.data(), sizeof(int4) * l1t.size(), cudaMemcpyHostToDevice));
   BCUDA(b, cudaMalloc((void**)&b->bi, sizeof(BInst) * ninst));
   BCUDA(b, cudaMemcpy(b->bi, hb.data(), sizeof(BInst) * ninst, cudaMemcpyHostToDevice));
   BCUDA(b, cudaMalloc((void**)&b->l1start, sizeof(long long) * (ninst + 1)));
@@ -1801,8 +1806,8 @@ int lockstep_build(cfmg_batch* b) {
   if (!all.empty()) {
     BCUDA(b, cudaMalloc((void**)&b->sops, sizeof(Op) * all.size()));
     BCUDA(b, cudaMemcpy(b->sops, all.data(), sizeof(Op) * all.size(), cudaMemcpyHostToDevice));
-    BCUDA(b, cudaMalloc((void**)&b->scs, sizeof(long long) * cs.size()));
-    BCUDA(b, cudaMemcpy(b->scs, cs.data(), sizeof(long long) * cs.size(), cudaMemcpyHostToDevice));
+    BCUDA(b, cudaMalloc((void**)&b->stab, sizeof(int4) * tab.size()));
+    BCUDA(b, cudaMemcpy(b->stab, tab.data(), sizeof(int4) * tab.size(), cudaMemcpyHostToDevice));
   }
   const int kind = hb[0].kind;
   const bool neumann = hb[0].neumann;
@@ -1831,21 +1836,20 @@ int lockstep_build(cfmg_batch* b) {
     BCUDA(b, cudaGraphAddNode(&cnode, g, &init, nullptr, 1, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     BCUDA(b, cudaStreamBeginCaptureToGraph(b->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    launch_bres(kind, neumann, b->bi, b->l1start, ninst, b->l1chunks, b->active, b->bpart, b->stream);
+    launch_bres(kind, neumann, b->bi, b->l1tab, b->l1chunks, b->active, b->bpart, b->stream);
     launch_bfinal(b->bi, b->l1start, ninst, b->bpart, b->active, b->nactive, b->stream);
-    if (neumann) launch_brhs(b->bi, b->l1start, ninst, b->l1chunks, b->active, b->stream);
+    if (neumann) launch_brhs(b->bi, b->l1tab, b->l1chunks, b->active, b->stream);
     for (const cfmg_batch::Step& st : b->steps) {
       if (st.tb) {
-        if (!launch_btb(st.stencil, st.nite, b->sops + st.op0, b->scs + st.cs0, st.nops, st.nchunks, b->active,
-                        b->stream)) {
+        if (!launch_btb(st.stencil, st.nite, b->sops, b->stab + st.tab0, st.nchunks, b->active, b->stream)) {
           cudaStreamEndCapture(b->stream, &body);
           return bfail(b, CFMG_ERR_UNSUPPORTED, "blocked pass shape");
         }
       } else {
-        launch_bstage(b->sops + st.op0, b->scs + st.cs0, st.nops, st.nchunks, b->active, b->stream);
+        launch_bstage(b->sops, b->stab + st.tab0, st.nchunks, b->active, b->stream);
       }
     }
-    launch_bupdate(b->bi, b->l1start, ninst, b->l1chunks, b->active, b->stream);
+    launch_bupdate(b->bi, b->l1tab, b->l1chunks, b->active, b->stream);
     launch_bcond(hc, b->nactive, b->stream);
     e = cudaStreamEndCapture(b->stream, &body);
     if (e != cudaSuccess) return bfail(b, CFMG_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
@@ -1901,8 +1905,8 @@ int cfmg_batch_destroy(cfmg_batch* b) {
     if (g) cudaGraphExecDestroy(g);
   for (cfmg_handle* h : b->inst) cfmg_destroy(h);
   for (void* p : {(void*)b->progs, (void*)b->ptrs, (void*)b->nops, (void*)b->counter, (void*)b->red, (void*)b->sc,
-                  (void*)b->nwet, (void*)b->bi, (void*)b->l1start, (void*)b->bpart, (void*)b->active,
-                  (void*)b->nactive, (void*)b->sops, (void*)b->scs})
+                  (void*)b->nwet, (void*)b->bi, (void*)b->l1start, (void*)b->l1tab, (void*)b->bpart,
+                  (void*)b->active, (void*)b->nactive, (void*)b->sops, (void*)b->stab})
     if (p) cudaFree(p);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
@@ -1928,8 +1932,9 @@ int cfmg_batch_solve(cfmg_batch* b, int zero_x, double* res, int* nite, double* 
         g = nullptr;
       }
     for (void** p : {(void**)&b->progs, (void**)&b->ptrs, (void**)&b->nops, (void**)&b->counter, (void**)&b->red,
-                     (void**)&b->sc, (void**)&b->nwet, (void**)&b->bi, (void**)&b->l1start, (void**)&b->bpart,
-                     (void**)&b->active, (void**)&b->nactive, (void**)&b->sops, (void**)&b->scs})
+                     (void**)&b->sc, (void**)&b->nwet, (void**)&b->bi, (void**)&b->l1start, (void**)&b->l1tab,
+                     (void**)&b->bpart, (void**)&b->active, (void**)&b->nactive, (void**)&b->sops,
+                     (void**)&b->stab})
       if (*p) {
         cudaFree(*p);
         *p = nullptr;

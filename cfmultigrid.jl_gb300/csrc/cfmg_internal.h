@@ -164,7 +164,11 @@ void launch_op(const Op& op, cudaStream_t s);                   // one Op as a s
 void launch_program(const Op* prog, int nops, double* red, cudaStream_t s);  // a device-resident program
 
 // temporally blocked FP32 smoother (k_tb.cu): nite pairs of 5- or 9-point
-// sweeps over the box U in one pass, x -> xo; false if nite is not 1..4
+// sweeps over the box U in one pass, x -> xo; false if nite is not
+// 1..kTbMaxPairs. A pass of p pairs recomputes a halo of 2p cells around each
+// 128 x 72 tile: 3 pairs suit large levels, longer passes cut the launches
+// of the many-pair coarsest solves.
+constexpr int kTbMaxPairs = 10;
 bool launch_smooth_tb(int stencil, int nite, const float* x, float* xo, const float* b, const float* w, float cff,
                       int tx, int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s);
 
@@ -172,7 +176,7 @@ bool launch_smooth_tb(int stencil, int nite, const float* x, float* xo, const fl
 // lockstep, one launch per step of the iteration for all of them. Every
 // launch is a grid-stride loop over the chunks (kBChunk work items) of its
 // Ops; a chunk of an instance that has converged is skipped.
-constexpr int kBChunk = 4096;
+constexpr int kBChunk = 1024;
 constexpr int kBThreads = 256;
 // per-instance scalar block (double): see k_bfinal for their use
 enum BSlot { BS_NORMB = 0, BS_RES, BS_NITE, BS_NWET, BS_NEXT, BS_CUR, BS_ICUR, BS_MEAN, BS_T0, BS_T1, BS_ZEROX,
@@ -191,21 +195,19 @@ struct BInst {
   int kind, neumann, norm_kind, maxite;
   double tol;
 };
-// chunks: cstart[i] = first chunk of item i (prefix sums, cstart[nitems] = total)
-void launch_bstage(const Op* ops, const long long* cstart, int nops, long long nchunks, const int* active,
-                   cudaStream_t s);
+// Work tables: one int4 per chunk (or tile) = {Op or instance, chunk of it,
+// instance, 0}; a launch compacts the active entries of each window.
+void launch_bstage(const Op* ops, const int4* tab, long long nchunks, const int* active, cudaStream_t s);
 void tb_tiles(int nite, int ui0, int ui1, int uj0, int uj1, int* ntx, int* nty);
-bool launch_btb(int stencil, int nite, const Op* ops, const long long* tstart, int nops, long long ntiles,
-                const int* active, cudaStream_t s);
+bool launch_btb(int stencil, int nite, const Op* ops, const int4* tab, long long ntiles, const int* active,
+                cudaStream_t s);
 void launch_binit(const BInst* bi, int ninst, int zero_x, int* active, int* nactive, cudaStream_t s);
-void launch_bres(int kind, bool neumann, const BInst* bi, const long long* cstart, int ninst, long long nchunks,
-                 const int* active, double* partials, cudaStream_t s);
+void launch_bres(int kind, bool neumann, const BInst* bi, const int4* tab, long long nchunks, const int* active,
+                 double* partials, cudaStream_t s);
 void launch_bfinal(const BInst* bi, const long long* cstart, int ninst, const double* partials, int* active,
                    int* nactive, cudaStream_t s);
-void launch_brhs(const BInst* bi, const long long* cstart, int ninst, long long nchunks, const int* active,
-                 cudaStream_t s);
-void launch_bupdate(const BInst* bi, const long long* cstart, int ninst, long long nchunks, const int* active,
-                    cudaStream_t s);
+void launch_brhs(const BInst* bi, const int4* tab, long long nchunks, const int* active, cudaStream_t s);
+void launch_bupdate(const BInst* bi, const int4* tab, long long nchunks, const int* active, cudaStream_t s);
 void launch_bcond(cudaGraphConditionalHandle hc, int* nactive, cudaStream_t s);
 
 // device scalars of a handle (dscal[])

@@ -27,15 +27,33 @@ __device__ __forceinline__ unsigned long long gtimer() {
   return t;
 }
 
-// last item i with cstart[i] <= c
-__device__ __forceinline__ int find_item(const long long* __restrict__ cstart, int nitems, long long c) {
-  int lo = 0, hi = nitems - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (cstart[mid] <= c) lo = mid;
-    else hi = mid - 1;
+// Block-wide ordered compaction of a window of `win` (<= blockDim.x) table
+// entries (base .. base+win-1): the entries whose instance is still active,
+// as offsets from base in list[]; returns their count. wsum needs
+// blockDim/32 + 1 ints.
+__device__ __forceinline__ int active_window(const int4* __restrict__ tab, long long base, long long n, int win,
+                                             const int* __restrict__ active, int* list, int* wsum) {
+  const long long c = base + threadIdx.x;
+  bool ok = false;
+  if ((int)threadIdx.x < win && c < n) ok = active[tab[c].z] != 0;
+  const unsigned bal = __ballot_sync(0xffffffffu, ok);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) wsum[wid] = __popc(bal);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int a = 0;
+    for (int w = 0; w < nw; ++w) {
+      const int v = wsum[w];
+      wsum[w] = a;
+      a += v;
+    }
+    wsum[nw] = a;
   }
-  return lo;
+  __syncthreads();
+  if (ok) list[wsum[wid] + __popc(bal & ((1u << lane) - 1u))] = threadIdx.x;
+  const int cnt = wsum[nw];
+  __syncthreads();
+  return cnt;
 }
 
 // fixed-order block sum (kBThreads threads); valid in thread 0
@@ -52,21 +70,31 @@ __device__ __forceinline__ double bsum(double v, double* sh) {
 }
 
 // ------------------------------------------------------------ cycle steps
-// Generic step: the chunks of a list of Ops (any kinds, one per instance
-// or more), each executed with the per-item code of the program engine.
-__global__ void __launch_bounds__(kBThreads, 3) k_bstage(const Op* __restrict__ ops, const long long* __restrict__ cstart,
-                                                      int nops, long long nchunks, const int* __restrict__ active) {
+// Generic step: the active chunks of a list of Ops (tab[c] = {op, chunk of
+// the op, instance}), each executed with the per-item code of the program
+// engine, 4 (FP32) or 2 (FP64) items per thread in flight.
+__global__ void __launch_bounds__(kBThreads, 2) k_bstage(const Op* __restrict__ ops, const int4* __restrict__ tab,
+                                                         long long nchunks, int win, const int* __restrict__ active) {
   __shared__ Op op;
-  for (long long c = blockIdx.x; c < nchunks; c += gridDim.x) {
-    const int o = find_item(cstart, nops, c);
-    if (!active[ops[o].inst]) continue;
-    __syncthreads();  // the previous chunk's readers of op are done
-    if (threadIdx.x < sizeof(Op) / sizeof(int)) ((int*)&op)[threadIdx.x] = ((const int*)&ops[o])[threadIdx.x];
-    __syncthreads();
-    const long long t0 = (c - cstart[o]) * kBChunk;
-    const long long e = t0 + kBChunk < op.n ? t0 + kBChunk : op.n;
-    if (op.prec == 0) exec<double>(op, t0 + threadIdx.x, kBThreads, e);
-    else exec<float>(op, t0 + threadIdx.x, kBThreads, e);
+  __shared__ int list[kBThreads];
+  __shared__ int wsum[kBThreads / 32 + 1];
+  int cur = -1;
+  for (long long base = (long long)blockIdx.x * win; base < nchunks; base += (long long)gridDim.x * win) {
+    const int cnt = active_window(tab, base, nchunks, win, active, list, wsum);
+    for (int q = 0; q < cnt; ++q) {
+      const int4 en = tab[base + list[q]];
+      if (en.x != cur) {
+        __syncthreads();  // the previous Op's readers are done
+        if (threadIdx.x < sizeof(Op) / sizeof(int)) ((int*)&op)[threadIdx.x] = ((const int*)&ops[en.x])[threadIdx.x];
+        __syncthreads();
+        cur = en.x;
+      }
+      const long long t0 = (long long)en.y * kBChunk;
+      const long long e = t0 + kBChunk < op.n ? t0 + kBChunk : op.n;
+      if (op.prec == 0) exec<double, 2>(op, t0 + threadIdx.x, kBThreads, e);
+      else exec<float, 4>(op, t0 + threadIdx.x, kBThreads, e);
+    }
+    __syncthreads();  // list is rewritten by the next window
   }
 }
 static_assert(sizeof(Op) / sizeof(int) <= kBThreads, "one thread per word of an Op");
@@ -104,69 +132,86 @@ __global__ void __launch_bounds__(kBThreads) k_binit(const BInst* __restrict__ b
   }
 }
 
-// Fused FP64 residual over the level-1 chunks of every active instance:
-// r = b - A x per cell (the residual operator's arithmetic), the chunk's
-// sum r^2 and sum r to partials[2c], partials[2c+1], and the scaled FP32
-// right-hand side (vertex-centred) or the FP64 r (cell-centred, for the
-// mean-removing pass).
+// Fused FP64 residual over the active level-1 chunks (tab[c] = {instance,
+// chunk of its level 1, instance}): r = b - A x per cell (the residual
+// operator's arithmetic), the chunk's sum r^2 and sum r to partials[2c],
+// partials[2c+1], and the scaled FP32 right-hand side (vertex-centred) or
+// the FP64 r (cell-centred, for the mean-removing pass).
 template <int KIND, bool NEUMANN>
-__global__ void __launch_bounds__(kBThreads) k_bres(const BInst* __restrict__ bi, const long long* __restrict__ cstart,
-                                                    int ninst, long long nchunks, const int* __restrict__ active,
+__global__ void __launch_bounds__(kBThreads) k_bres(const BInst* __restrict__ bi, const int4* __restrict__ tab,
+                                                    long long nchunks, int win, const int* __restrict__ active,
                                                     double* __restrict__ partials) {
+  constexpr int U = kBChunk / kBThreads;
+  __shared__ int list[kBThreads];
+  __shared__ int wsum[kBThreads / 32 + 1];
   __shared__ double sh2[kBThreads / 32], sh1[kBThreads / 32];
-  for (long long c = blockIdx.x; c < nchunks; c += gridDim.x) {
-    const int i = find_item(cstart, ninst, c);
-    if (!active[i]) continue;
-    const BInst& B = bi[i];
-    const double scale = B.sc[BS_NEXT];
-    const long long t0 = (c - cstart[i]) * kBChunk;
-    const long long e = t0 + kBChunk < B.n ? t0 + kBChunk : B.n;
-    const long long ni = B.box.i1 - B.box.i0 + 1, nj = B.box.j1 - B.box.j0 + 1;
-    double s2 = 0.0, s1 = 0.0, c1 = 0.0;
-    for (long long t = t0 + threadIdx.x; t < e; t += kBThreads) {
-      long long I;
-      if (KIND == OPK_RESID9) {
-        const int ii = B.box.i0 + (int)(t % ni);
-        const long long q = t / ni;
-        I = lin(B.g, ii, B.box.j0 + (int)(q % nj), B.box.k0 + (int)(q / nj));
-      } else {
-        I = B.lo + t;
-      }
-      const double v = (KIND == OPK_RESID9) ? v_resid9(B.x, B.b, B.d, B.m, B.g.n1, I)
-                                            : v_resid5(B.x, B.b, B.d, B.m, B.g.n1, I);
-      s2 = __fma_rn(v, v, s2);
-      if (NEUMANN) {
-        B.r[I] = v;
-        const double tt = __dadd_rn(s1, v);
-        c1 = __dadd_rn(c1, (fabs(s1) >= fabs(v)) ? __dadd_rn(__dsub_rn(s1, tt), v) : __dadd_rn(__dsub_rn(v, tt), s1));
-        s1 = tt;
-      } else {
-        const float f = (float)(v * scale);
-        B.b32[I] = f;
-        B.r32[I] = f;
-      }
-    }
-    s1 = __dadd_rn(s1, c1);
+  for (long long base = (long long)blockIdx.x * win; base < nchunks; base += (long long)gridDim.x * win) {
+    const int cnt = active_window(tab, base, nchunks, win, active, list, wsum);
+    for (int q = 0; q < cnt; ++q) {
+      const long long c = base + list[q];
+      const int4 en = tab[c];
+      const BInst& B = bi[en.x];
+      const double scale = B.sc[BS_NEXT];
+      const long long t0 = (long long)en.y * kBChunk;
+      const long long ni = B.box.i1 - B.box.i0 + 1, nj = B.box.j1 - B.box.j0 + 1;
+      double s2 = 0.0, s1 = 0.0, c1 = 0.0;
+      double v[U];
+      long long I[U];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      s2 = __dadd_rn(s2, __shfl_down_sync(0xffffffffu, s2, o));
-      s1 = __dadd_rn(s1, __shfl_down_sync(0xffffffffu, s1, o));
-    }
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) {
-      sh2[threadIdx.x >> 5] = s2;
-      sh1[threadIdx.x >> 5] = s1;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double a = 0.0, b = 0.0;
-      for (int w = 0; w < kBThreads / 32; ++w) {
-        a = __dadd_rn(a, sh2[w]);
-        b = __dadd_rn(b, sh1[w]);
+      for (int u = 0; u < U; ++u) {
+        const long long t = t0 + threadIdx.x + (long long)u * kBThreads;
+        I[u] = -1;
+        if (t < B.n) {
+          if (KIND == OPK_RESID9) {
+            const int ii = B.box.i0 + (int)(t % ni);
+            const long long qq = t / ni;
+            I[u] = lin(B.g, ii, B.box.j0 + (int)(qq % nj), B.box.k0 + (int)(qq / nj));
+            v[u] = v_resid9(B.x, B.b, B.d, B.m, B.g.n1, I[u]);
+          } else {
+            I[u] = B.lo + t;
+            v[u] = v_resid5(B.x, B.b, B.d, B.m, B.g.n1, I[u]);
+          }
+        }
       }
-      partials[2 * c] = a;
-      partials[2 * c + 1] = b;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (I[u] < 0) continue;
+        s2 = __fma_rn(v[u], v[u], s2);
+        if (NEUMANN) {
+          B.r[I[u]] = v[u];
+          const double tt = __dadd_rn(s1, v[u]);
+          c1 = __dadd_rn(c1, (fabs(s1) >= fabs(v[u])) ? __dadd_rn(__dsub_rn(s1, tt), v[u])
+                                                       : __dadd_rn(__dsub_rn(v[u], tt), s1));
+          s1 = tt;
+        } else {
+          const float f = (float)(v[u] * scale);
+          B.b32[I[u]] = f;
+          B.r32[I[u]] = f;
+        }
+      }
+      s1 = __dadd_rn(s1, c1);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        s2 = __dadd_rn(s2, __shfl_down_sync(0xffffffffu, s2, o));
+        s1 = __dadd_rn(s1, __shfl_down_sync(0xffffffffu, s1, o));
+      }
+      __syncthreads();
+      if ((threadIdx.x & 31) == 0) {
+        sh2[threadIdx.x >> 5] = s2;
+        sh1[threadIdx.x >> 5] = s1;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < kBThreads / 32; ++w) {
+          a = __dadd_rn(a, sh2[w]);
+          b = __dadd_rn(b, sh1[w]);
+        }
+        partials[2 * c] = a;
+        partials[2 * c + 1] = b;
+      }
     }
+    __syncthreads();
   }
 }
 
@@ -227,35 +272,64 @@ __global__ void __launch_bounds__(kBThreads) k_bfinal(const BInst* __restrict__ 
 }
 
 // cell-centred: b32 = r32 = msk ? (r - mean) * CUR : 0 over the whole array
-__global__ void __launch_bounds__(kBThreads) k_brhs(const BInst* __restrict__ bi, const long long* __restrict__ cstart,
-                                                    int ninst, long long nchunks, const int* __restrict__ active) {
-  for (long long c = blockIdx.x; c < nchunks; c += gridDim.x) {
-    const int i = find_item(cstart, ninst, c);
-    if (!active[i]) continue;
-    const BInst& B = bi[i];
-    const double mean = B.sc[BS_MEAN], scale = B.sc[BS_CUR];
-    const long long t0 = (c - cstart[i]) * kBChunk;
-    const long long e = t0 + kBChunk < B.len ? t0 + kBChunk : B.len;
-    for (long long t = t0 + threadIdx.x; t < e; t += kBThreads) {
-      const float f = B.m[t] ? (float)((B.r[t] - mean) * scale) : 0.f;
-      B.b32[t] = f;
-      B.r32[t] = f;
+__global__ void __launch_bounds__(kBThreads) k_brhs(const BInst* __restrict__ bi, const int4* __restrict__ tab,
+                                                    long long nchunks, int win, const int* __restrict__ active) {
+  constexpr int U = kBChunk / kBThreads;
+  __shared__ int list[kBThreads];
+  __shared__ int wsum[kBThreads / 32 + 1];
+  for (long long base = (long long)blockIdx.x * win; base < nchunks; base += (long long)gridDim.x * win) {
+    const int cnt = active_window(tab, base, nchunks, win, active, list, wsum);
+    for (int q = 0; q < cnt; ++q) {
+      const int4 en = tab[base + list[q]];
+      const BInst& B = bi[en.x];
+      const double mean = B.sc[BS_MEAN], scale = B.sc[BS_CUR];
+      const long long t0 = (long long)en.y * kBChunk + threadIdx.x;
+      float f[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const long long t = t0 + (long long)u * kBThreads;
+        f[u] = 0.f;
+        if (t < B.len && B.m[t]) f[u] = (float)((B.r[t] - mean) * scale);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const long long t = t0 + (long long)u * kBThreads;
+        if (t < B.len) {
+          B.b32[t] = f[u];
+          B.r32[t] = f[u];
+        }
+      }
     }
+    __syncthreads();
   }
 }
 
 // x += e32 * ICUR over the whole array
-__global__ void __launch_bounds__(kBThreads) k_bupdate(const BInst* __restrict__ bi,
-                                                       const long long* __restrict__ cstart, int ninst,
-                                                       long long nchunks, const int* __restrict__ active) {
-  for (long long c = blockIdx.x; c < nchunks; c += gridDim.x) {
-    const int i = find_item(cstart, ninst, c);
-    if (!active[i]) continue;
-    const BInst& B = bi[i];
-    const double is = B.sc[BS_ICUR];
-    const long long t0 = (c - cstart[i]) * kBChunk;
-    const long long e = t0 + kBChunk < B.len ? t0 + kBChunk : B.len;
-    for (long long t = t0 + threadIdx.x; t < e; t += kBThreads) B.x[t] = __fma_rn((double)B.e32[t], is, B.x[t]);
+__global__ void __launch_bounds__(kBThreads) k_bupdate(const BInst* __restrict__ bi, const int4* __restrict__ tab,
+                                                       long long nchunks, int win, const int* __restrict__ active) {
+  constexpr int U = kBChunk / kBThreads;
+  __shared__ int list[kBThreads];
+  __shared__ int wsum[kBThreads / 32 + 1];
+  for (long long base = (long long)blockIdx.x * win; base < nchunks; base += (long long)gridDim.x * win) {
+    const int cnt = active_window(tab, base, nchunks, win, active, list, wsum);
+    for (int q = 0; q < cnt; ++q) {
+      const int4 en = tab[base + list[q]];
+      const BInst& B = bi[en.x];
+      const double is = B.sc[BS_ICUR];
+      const long long t0 = (long long)en.y * kBChunk + threadIdx.x;
+      double xn[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const long long t = t0 + (long long)u * kBThreads;
+        if (t < B.len) xn[u] = __fma_rn((double)B.e32[t], is, B.x[t]);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const long long t = t0 + (long long)u * kBThreads;
+        if (t < B.len) B.x[t] = xn[u];
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -268,7 +342,9 @@ __global__ void k_bcond(cudaGraphConditionalHandle hc, int* nactive) {
 
 // ------------------------------------------------------------- launchers
 static int g_nsm = 0;
-static long long grid_for(long long nchunks, int per_sm) {
+// resident blocks (per_sm per SM), each taking windows of `win` entries so
+// that every block has work while entries are few
+static long long grid_for(long long nchunks, int per_sm, int* win) {
   if (!g_nsm) {
     int dev = 0;
     cudaGetDevice(&dev);
@@ -276,28 +352,34 @@ static long long grid_for(long long nchunks, int per_sm) {
     if (g_nsm <= 0) g_nsm = 1;
   }
   const long long g = (long long)g_nsm * per_sm;
-  return nchunks < g ? (nchunks > 0 ? nchunks : 1) : g;
+  long long w = (nchunks + g - 1) / g;
+  w = w < 1 ? 1 : (w > kBThreads ? kBThreads : w);
+  *win = (int)w;
+  const long long windows = (nchunks + w - 1) / w;
+  return windows < g ? (windows > 0 ? windows : 1) : g;
 }
 
-void launch_bstage(const Op* ops, const long long* cstart, int nops, long long nchunks, const int* active,
-                   cudaStream_t s) {
+void launch_bstage(const Op* ops, const int4* tab, long long nchunks, const int* active, cudaStream_t s) {
   if (nchunks <= 0) return;
-  k_bstage<<<(unsigned)grid_for(nchunks, 8), kBThreads, 0, s>>>(ops, cstart, nops, nchunks, active);
+  int win;
+  const unsigned g = (unsigned)grid_for(nchunks, 2, &win);
+  k_bstage<<<g, kBThreads, 0, s>>>(ops, tab, nchunks, win, active);
 }
 
 void launch_binit(const BInst* bi, int ninst, int zero_x, int* active, int* nactive, cudaStream_t s) {
   k_binit<<<ninst, kBThreads, 0, s>>>(bi, zero_x, active, nactive);
 }
 
-void launch_bres(int kind, bool neumann, const BInst* bi, const long long* cstart, int ninst, long long nchunks,
-                 const int* active, double* partials, cudaStream_t s) {
-  const unsigned g = (unsigned)grid_for(nchunks, 8);
+void launch_bres(int kind, bool neumann, const BInst* bi, const int4* tab, long long nchunks, const int* active,
+                 double* partials, cudaStream_t s) {
+  int win;
+  const unsigned g = (unsigned)grid_for(nchunks, 6, &win);
   if (kind == OPK_RESID9) {
-    if (neumann) k_bres<OPK_RESID9, true><<<g, kBThreads, 0, s>>>(bi, cstart, ninst, nchunks, active, partials);
-    else k_bres<OPK_RESID9, false><<<g, kBThreads, 0, s>>>(bi, cstart, ninst, nchunks, active, partials);
+    if (neumann) k_bres<OPK_RESID9, true><<<g, kBThreads, 0, s>>>(bi, tab, nchunks, win, active, partials);
+    else k_bres<OPK_RESID9, false><<<g, kBThreads, 0, s>>>(bi, tab, nchunks, win, active, partials);
   } else {
-    if (neumann) k_bres<OPK_RESID5, true><<<g, kBThreads, 0, s>>>(bi, cstart, ninst, nchunks, active, partials);
-    else k_bres<OPK_RESID5, false><<<g, kBThreads, 0, s>>>(bi, cstart, ninst, nchunks, active, partials);
+    if (neumann) k_bres<OPK_RESID5, true><<<g, kBThreads, 0, s>>>(bi, tab, nchunks, win, active, partials);
+    else k_bres<OPK_RESID5, false><<<g, kBThreads, 0, s>>>(bi, tab, nchunks, win, active, partials);
   }
 }
 
@@ -306,14 +388,16 @@ void launch_bfinal(const BInst* bi, const long long* cstart, int ninst, const do
   k_bfinal<<<ninst, kBThreads, 0, s>>>(bi, cstart, partials, active, nactive);
 }
 
-void launch_brhs(const BInst* bi, const long long* cstart, int ninst, long long nchunks, const int* active,
-                 cudaStream_t s) {
-  k_brhs<<<(unsigned)grid_for(nchunks, 8), kBThreads, 0, s>>>(bi, cstart, ninst, nchunks, active);
+void launch_brhs(const BInst* bi, const int4* tab, long long nchunks, const int* active, cudaStream_t s) {
+  int win;
+  const unsigned g = (unsigned)grid_for(nchunks, 6, &win);
+  k_brhs<<<g, kBThreads, 0, s>>>(bi, tab, nchunks, win, active);
 }
 
-void launch_bupdate(const BInst* bi, const long long* cstart, int ninst, long long nchunks, const int* active,
-                    cudaStream_t s) {
-  k_bupdate<<<(unsigned)grid_for(nchunks, 8), kBThreads, 0, s>>>(bi, cstart, ninst, nchunks, active);
+void launch_bupdate(const BInst* bi, const int4* tab, long long nchunks, const int* active, cudaStream_t s) {
+  int win;
+  const unsigned g = (unsigned)grid_for(nchunks, 6, &win);
+  k_bupdate<<<g, kBThreads, 0, s>>>(bi, tab, nchunks, win, active);
 }
 
 void launch_bcond(cudaGraphConditionalHandle hc, int* nactive, cudaStream_t s) {

@@ -151,8 +151,8 @@ __device__ void run_program(const Op* __restrict__ prog, int nops, long long t0,
           for (long long t = t0; t < op.n; t += st) ((double*)op.y)[t] = 0.0;
         break;
       default:
-        if (op.prec == 0) exec<double>(op, t0, st, op.n);
-        else exec<float>(op, t0, st, op.n);
+        if (op.prec == 0) exec<double, 1>(op, t0, st, op.n);
+        else exec<float, 1>(op, t0, st, op.n);
         break;
     }
     cluster_barrier();

@@ -162,32 +162,53 @@ __global__ void __launch_bounds__(kTbW * kTbTy, 1) k_smooth_tb(const float* __re
                     smem);
 }
 
-// Batched form: a grid-stride loop over the tiles of many OPK_TB Ops
-// (tstart: prefix sums of their tile counts); tiles of converged instances
-// are skipped. The barrier at the end of each tile keeps the next tile's
-// loads behind this tile's last shared-memory reads.
+// Batched form: a grid-stride loop over windows of 1024 entries of a tile
+// table (tab[t] = {OPK_TB Op, tile of the Op, instance}); the tiles of
+// instances that are still active are compacted and run one after the
+// other. The barrier at the end of each tile keeps the next tile's loads
+// behind this tile's last shared-memory reads.
 template <int ST, int NITE>
-__global__ void __launch_bounds__(kTbW * kTbTy, 1) k_btb(const Op* __restrict__ ops,
-                                                         const long long* __restrict__ tstart, int nops,
-                                                         long long ntiles, const int* __restrict__ active) {
+__global__ void __launch_bounds__(kTbW * kTbTy, 1) k_btb(const Op* __restrict__ ops, const int4* __restrict__ tab,
+                                                         long long ntiles, int win, const int* __restrict__ active) {
   extern __shared__ float smem[];
-  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    int lo = 0, hi = nops - 1;  // last op with tstart[op] <= t
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (tstart[mid] <= t) lo = mid;
-      else hi = mid - 1;
-    }
-    const Op& op = ops[lo];
-    if (!active[op.inst]) continue;
-    const long long q = t - tstart[lo];
-    const long long per_layer = (long long)op.kf0 * op.kf1;
-    const int bz = (int)(q / per_layer);
-    const int rem = (int)(q - (long long)bz * per_layer);
-    tb_tile<ST, NITE>((const float*)op.x, (float*)op.y, (const float*)op.b, (const float*)op.w, (float)op.cff,
-                      op.g.tx, op.g.ty, op.box.i0, op.box.i1, op.box.j0, op.box.j1, rem % op.kf0, rem / op.kf0, bz,
-                      smem);
+  __shared__ int list[kTbW * kTbTy];
+  __shared__ int wsum[kTbW * kTbTy / 32 + 1];
+  const int tid = threadIdx.y * kTbW + threadIdx.x;
+  const int nt = kTbW * kTbTy;
+  for (long long base = (long long)blockIdx.x * win; base < ntiles; base += (long long)gridDim.x * win) {
+    // ordered compaction of the window's active tiles
+    const long long c = base + tid;
+    bool ok = false;
+    if (tid < win && c < ntiles) ok = active[tab[c].z] != 0;
+    const unsigned bal = __ballot_sync(0xffffffffu, ok);
+    const int lane = tid & 31, wid = tid >> 5;
+    if (lane == 0) wsum[wid] = __popc(bal);
     __syncthreads();
+    if (tid == 0) {
+      int a = 0;
+      for (int w = 0; w < nt / 32; ++w) {
+        const int v = wsum[w];
+        wsum[w] = a;
+        a += v;
+      }
+      wsum[nt / 32] = a;
+    }
+    __syncthreads();
+    if (ok) list[wsum[wid] + __popc(bal & ((1u << lane) - 1u))] = tid;
+    __syncthreads();
+    const int cnt = wsum[nt / 32];
+    for (int q = 0; q < cnt; ++q) {
+      const int4 en = tab[base + list[q]];
+      const Op& op = ops[en.x];
+      const long long per_layer = (long long)op.kf0 * op.kf1;
+      const int bz = (int)(en.y / per_layer);
+      const int rem = (int)(en.y - (long long)bz * per_layer);
+      tb_tile<ST, NITE>((const float*)op.x, (float*)op.y, (const float*)op.b, (const float*)op.w, (float)op.cff,
+                        op.g.tx, op.g.ty, op.box.i0, op.box.i1, op.box.j0, op.box.j1, rem % op.kf0, rem / op.kf0, bz,
+                        smem);
+      __syncthreads();
+    }
+    __syncthreads();  // list is rewritten by the next window
   }
 }
 
@@ -206,7 +227,7 @@ static void launch_tb_n(const float* x, float* xo, const float* b, const float* 
   k_smooth_tb<ST, NITE><<<grid, dim3(kTbW, kTbTy, 1), smem, s>>>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1);
 }
 
-// nite pairs of sweeps in one pass (nite in 1..4); returns false when the
+// nite pairs of sweeps in one pass (nite in 1..kTbMaxPairs); returns false when the
 // caller must fall back to single sweeps.
 bool launch_smooth_tb(int stencil, int nite, const float* x, float* xo, const float* b, const float* w, float cff,
                       int tx, int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s) {
@@ -215,8 +236,10 @@ bool launch_smooth_tb(int stencil, int nite, const float* x, float* xo, const fl
     launch_tb_n<ST, N>(x, xo, b, w, cff, tx, ty, nz, ui0, ui1, uj0, uj1, s);                 \
     return true;                                                                             \
   }
-  CFMG_TB(5, 1) CFMG_TB(5, 2) CFMG_TB(5, 3) CFMG_TB(5, 4)
-  CFMG_TB(9, 1) CFMG_TB(9, 2) CFMG_TB(9, 3) CFMG_TB(9, 4)
+  CFMG_TB(5, 1) CFMG_TB(5, 2) CFMG_TB(5, 3) CFMG_TB(5, 4) CFMG_TB(5, 5)
+  CFMG_TB(5, 6) CFMG_TB(5, 7) CFMG_TB(5, 8) CFMG_TB(5, 9) CFMG_TB(5, 10)
+  CFMG_TB(9, 1) CFMG_TB(9, 2) CFMG_TB(9, 3) CFMG_TB(9, 4) CFMG_TB(9, 5)
+  CFMG_TB(9, 6) CFMG_TB(9, 7) CFMG_TB(9, 8) CFMG_TB(9, 9) CFMG_TB(9, 10)
 #undef CFMG_TB
   return false;
 }
@@ -230,8 +253,7 @@ void tb_tiles(int nite, int ui0, int ui1, int uj0, int uj1, int* ntx, int* nty) 
 }
 
 template <int ST, int NITE>
-static void launch_btb_n(const Op* ops, const long long* tstart, int nops, long long ntiles, const int* active,
-                         cudaStream_t s) {
+static void launch_btb_n(const Op* ops, const int4* tab, long long ntiles, const int* active, cudaStream_t s) {
   const size_t smem = 4 * (size_t)kTbH * kTbW * sizeof(float);
   static bool attr = false;
   static int nsm = 0;
@@ -242,16 +264,20 @@ static void launch_btb_n(const Op* ops, const long long* tstart, int nops, long 
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     attr = true;
   }
-  const long long grid = ntiles < nsm ? ntiles : nsm;  // one resident CTA per SM
-  k_btb<ST, NITE><<<(unsigned)grid, dim3(kTbW, kTbTy, 1), smem, s>>>(ops, tstart, nops, ntiles, active);
+  // one resident CTA per SM, each taking windows of `win` tiles
+  long long win = (ntiles + nsm - 1) / nsm;
+  if (win > kTbW * kTbTy) win = kTbW * kTbTy;
+  const long long windows = (ntiles + win - 1) / win;
+  const long long grid = windows < nsm ? windows : nsm;
+  k_btb<ST, NITE><<<(unsigned)grid, dim3(kTbW, kTbTy, 1), smem, s>>>(ops, tab, ntiles, (int)win, active);
 }
 
-bool launch_btb(int stencil, int nite, const Op* ops, const long long* tstart, int nops, long long ntiles,
-                const int* active, cudaStream_t s) {
+bool launch_btb(int stencil, int nite, const Op* ops, const int4* tab, long long ntiles, const int* active,
+                cudaStream_t s) {
   if (ntiles <= 0) return true;
 #define CFMG_BTB(ST, N)                                              \
   if (stencil == ST && nite == N) {                                  \
-    launch_btb_n<ST, N>(ops, tstart, nops, ntiles, active, s);       \
+    launch_btb_n<ST, N>(ops, tab, ntiles, active, s);                \
     return true;                                                     \
   }
   CFMG_BTB(5, 1) CFMG_BTB(5, 2) CFMG_BTB(5, 3)

@@ -89,41 +89,65 @@ __device__ __forceinline__ T vc_sum(const T* x, const T* cE, const T* cN, long l
 }
 
 // ---------------------------------------------------------- sweeps at I
+// v_* return the new value at I, d_* store it.
 // sloop2d! (src/laplacian.jl:66-73): y = (1-w)x - (w*idiag)*(b - s4)
 template <class T>
-__device__ __forceinline__ void d_sweep5(const T* x, T* y, const T* b, const T* w, T cff, long long n1, long long I) {
+__device__ __forceinline__ T v_sweep5(const T* x, const T* b, const T* w, T cff, long long n1, long long I) {
   typedef Ar<T> A;
-  y[I] = A::sub(A::mul(cff, x[I]), A::mul(w[I], A::sub(b[I], sum4(x, I, n1))));
+  return A::sub(A::mul(cff, x[I]), A::mul(w[I], A::sub(b[I], sum4(x, I, n1))));
 }
 // sloop3d_v1! (src/laplacian.jl:11-20)
 template <class T>
-__device__ __forceinline__ void d_sweep7(const T* x, T* y, const T* b, const T* w, T cff, long long n1, long long n2,
-                                         long long I) {
+__device__ __forceinline__ T v_sweep7(const T* x, const T* b, const T* w, T cff, long long n1, long long n2,
+                                      long long I) {
   typedef Ar<T> A;
-  y[I] = A::sub(A::mul(cff, x[I]), A::mul(w[I], A::sub(b[I], faces6(x, I, n1, n2))));
+  return A::sub(A::mul(cff, x[I]), A::mul(w[I], A::sub(b[I], faces6(x, I, n1, n2))));
 }
 // in-plane laplacian9 (2D 9-point extension): b - faces/2 - diagonals/4
 template <class T>
-__device__ __forceinline__ void d_sweep9(const T* x, T* y, const T* b, const T* w, T cff, long long n1, long long I) {
+__device__ __forceinline__ T v_sweep9(const T* x, const T* b, const T* w, T cff, long long n1, long long I) {
   typedef Ar<T> A;
   T t = A::fmx(sum4(x, I, n1), T(-0.5), b[I]);
   t = A::fmx(diags4(x, I, n1), T(-0.25), t);
-  y[I] = A::sub(A::mul(cff, x[I]), A::mul(w[I], t));
+  return A::sub(A::mul(cff, x[I]), A::mul(w[I], t));
 }
 // smooth_laplacian9! body (src/laplacian9.jl:14-44)
 template <class T>
-__device__ __forceinline__ void d_sweep19(const T* x, T* y, const T* b, const T* w, T cff, long long n1, long long n2,
-                                          long long I) {
+__device__ __forceinline__ T v_sweep19(const T* x, const T* b, const T* w, T cff, long long n1, long long n2,
+                                       long long I) {
   typedef Ar<T> A;
   T t = A::fmx(faces6(x, I, n1, n2), T(-0.5), b[I]);
   t = A::fmx(edges12(x, I, n1, n2), T(-0.25), t);
-  y[I] = A::sub(A::mul(cff, x[I]), A::mul(w[I], t));
+  return A::sub(A::mul(cff, x[I]), A::mul(w[I], t));
+}
+template <class T>
+__device__ __forceinline__ T v_sweepvc(const T* x, const T* b, const T* w, const T* cE, const T* cN, T cff,
+                                       long long n1, long long I) {
+  typedef Ar<T> A;
+  return A::sub(A::mul(cff, x[I]), A::mul(w[I], A::sub(b[I], vc_sum(x, cE, cN, I, n1))));
+}
+template <class T>
+__device__ __forceinline__ void d_sweep5(const T* x, T* y, const T* b, const T* w, T cff, long long n1, long long I) {
+  y[I] = v_sweep5(x, b, w, cff, n1, I);
+}
+template <class T>
+__device__ __forceinline__ void d_sweep7(const T* x, T* y, const T* b, const T* w, T cff, long long n1, long long n2,
+                                         long long I) {
+  y[I] = v_sweep7(x, b, w, cff, n1, n2, I);
+}
+template <class T>
+__device__ __forceinline__ void d_sweep9(const T* x, T* y, const T* b, const T* w, T cff, long long n1, long long I) {
+  y[I] = v_sweep9(x, b, w, cff, n1, I);
+}
+template <class T>
+__device__ __forceinline__ void d_sweep19(const T* x, T* y, const T* b, const T* w, T cff, long long n1, long long n2,
+                                          long long I) {
+  y[I] = v_sweep19(x, b, w, cff, n1, n2, I);
 }
 template <class T>
 __device__ __forceinline__ void d_sweepvc(const T* x, T* y, const T* b, const T* w, const T* cE, const T* cN, T cff,
                                           long long n1, long long I) {
-  typedef Ar<T> A;
-  y[I] = A::sub(A::mul(cff, x[I]), A::mul(w[I], A::sub(b[I], vc_sum(x, cE, cN, I, n1))));
+  y[I] = v_sweepvc(x, b, w, cE, cN, cff, n1, I);
 }
 
 // ------------------------------------------------------- residuals at I
@@ -180,10 +204,15 @@ __device__ __forceinline__ void d_resid19(T* r, const T* x, const T* b, const T*
   r[I] = v_resid19(x, b, d, m, n1, n2, I);
 }
 template <class T>
+__device__ __forceinline__ T v_residvc(const T* x, const T* b, const T* d, const T* cE, const T* cN, const uint8_t* m,
+                                       long long n1, long long I) {
+  typedef Ar<T> A;
+  return mask_mul(m[I], A::sub(A::add(A::mul(d[I], x[I]), b[I]), vc_sum(x, cE, cN, I, n1)));
+}
+template <class T>
 __device__ __forceinline__ void d_residvc(T* r, const T* x, const T* b, const T* d, const T* cE, const T* cN,
                                           const uint8_t* m, long long n1, long long I) {
-  typedef Ar<T> A;
-  r[I] = mask_mul(m[I], A::sub(A::add(A::mul(d[I], x[I]), b[I]), vc_sum(x, cE, cN, I, n1)));
+  r[I] = v_residvc(x, b, d, cE, cN, m, n1, I);
 }
 
 // ---------------------------------------------------------- restriction
@@ -192,8 +221,8 @@ __device__ __forceinline__ void d_residvc(T* r, const T* x, const T* b, const T*
 // 2 vertices 2D (rvloop2d!, src/RP_on_vertices.jl:96-115), 3 vertices 3D
 // (restriction_vertices!, :1-32).
 template <class T, int KIND>
-__device__ __forceinline__ void d_restrict(const T* x, T* xc, const T* coef, const Geom& gf, const Geom& gc, int ii,
-                                           int jj, int kk) {
+__device__ __forceinline__ T v_restrict(const T* x, const T* coef, const Geom& gf, const Geom& gc, int ii, int jj,
+                                        int kk, long long& C) {
   typedef Ar<T> A;
   const int nh = gc.nh;
   const int i = c2f(ii, nh), j = c2f(jj, nh);
@@ -241,8 +270,15 @@ __device__ __forceinline__ void d_restrict(const T* x, T* xc, const T* coef, con
           }
         }
   }
-  long long C = lin(gc, ii, jj, kk);
-  xc[C] = A::mul(coef[C], s);
+  C = lin(gc, ii, jj, kk);
+  return A::mul(coef[C], s);
+}
+template <class T, int KIND>
+__device__ __forceinline__ void d_restrict(const T* x, T* xc, const T* coef, const Geom& gf, const Geom& gc, int ii,
+                                           int jj, int kk) {
+  long long C;
+  const T v = v_restrict<T, KIND>(x, coef, gf, gc, ii, jj, kk, C);
+  xc[C] = v;
 }
 
 // --------------------------------------------------------- prolongation
