@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--workload", default="config2", choices=["config2", "config3", "config4", "config5"],
                     help="config3: the 3D 7-point case; config4: batched solves of uneven sizes (one graph launch per batch); config5: forward + adjoint solves")
     ap.add_argument("--ninst", type=int, default=2048, help="config4 batch size")
+    ap.add_argument("--no-tune", action="store_true", help="config4: F(2,2) without the autotuner")
     ap.add_argument("--quick", action="store_true",
                     help="mixed form only: one warm-up and one timed solve (a short run for ncu)")
     return ap.parse_args()
@@ -561,7 +562,10 @@ def run_batch(args, rank, world, local):
         return batch
 
     t0 = time.perf_counter()
-    p, report = autotune.tune(base, sizes, make)
+    if args.no_tune:
+        p, report = dataclasses_replace(base, cycle="f"), {"skipped": True}
+    else:
+        p, report = autotune.tune(base, sizes, make)
     t_tune = time.perf_counter() - t0
     t0 = time.perf_counter()
     batch = make(p, list(range(len(probs))))
@@ -648,6 +652,12 @@ def run_adjoint(args, rank, world, local):
                                    f"dL/dkappa", "levels": mg.nlevels},
             "fd_check": {"directions": len(fd_err), "max_rel_err": max(fd_err) if fd_err else None,
                          "bound": 1e-6}}
+
+
+def dataclasses_replace(p, **kw):
+    import dataclasses
+
+    return dataclasses.replace(p, **kw)
 
 
 def dataclasses_asdict(p):

@@ -53,6 +53,11 @@ struct cfmg_handle {
   int coarsest_fp64 = -1;  // mixed form: -1 FP64 when the coarsest level is small, 0 never, 1 always
   // adjoint scratch (level-1 FP64 arrays, allocated on the first cfmg_adjoint)
   double *adj_x = nullptr, *adj_b = nullptr, *adj_gk = nullptr;
+  // integer form of the mixed loop's fused residual (k_mixed.cu): Q*diag of
+  // level 1 as int8 (-128 on dry cells), usable when int_ok
+  int8_t* dq = nullptr;
+  bool int_ok = false;
+  bool int_on = true;
   bool record = false;  // emit() records every Op (whole-solve programs) instead of running it
   bool record_tb = false;  // while recording: temporally blocked smoothing is recorded as OPK_TB Ops
 };
@@ -90,10 +95,12 @@ struct cfmg_batch {
   int* nactive = nullptr;      // instances continuing after this iteration
   Op* sops = nullptr;          // the Ops of all cycle steps (device)
   int4* stab = nullptr;        // their chunk (or tile) tables {Op, chunk, instance, 0} (device)
+  BSmall* ssm = nullptr;       // small-level smoothing descriptors (device)
   struct Step {
-    int tb, stencil, nite;     // tb: OPK_TB Ops of one (stencil, nite)
-    long long tab0;            // offset into stab
-    long long nchunks;
+    int tb, stencil, nite;     // tb: OPK_TB Ops of one (stencil, nite); tb == 2: BSmall blocks
+    long long tab0;            // offset into stab (or ssm)
+    long long nchunks;         // table entries (or BSmall blocks)
+    int smem;                  // BSmall: shared memory bytes
   };
   std::vector<Step> steps;
 };
@@ -514,11 +521,14 @@ template <>
 int coarsest_t<double>(cfmg_handle* h, int nite) {
   return smooth_t<double>(h, L(h), nite);
 }
+bool coarsest_in_fp64(const cfmg_handle* h) {
+  return L(h) > 1 && (h->coarsest_fp64 > 0 ||
+                      (h->coarsest_fp64 < 0 && (long long)h->lv[L(h) - 1].len <= engine_limit(h, CFMG_FP64)));
+}
 template <>
 int coarsest_t<float>(cfmg_handle* h, int nite) {
   if (L(h) == 1) return smooth_t<float>(h, 1, nite);
-  const bool fp64 = h->coarsest_fp64 > 0 ||
-                    (h->coarsest_fp64 < 0 && (long long)h->lv[L(h) - 1].len <= engine_limit(h, CFMG_FP64));
+  const bool fp64 = coarsest_in_fp64(h);
   if (!fp64) return smooth_t<float>(h, L(h), nite);
   const int lev = L(h);
   const Level& c = h->lv[lev - 1];
@@ -710,6 +720,31 @@ int setup_operators_body(cfmg_handle* h) {
 }
 
 // FP32 copies of the operator coefficients for the mixed-precision cycles.
+bool fused_ok(const cfmg_handle* h);
+int resid_kind(const cfmg_handle* h) {
+  if (h->d.op == CFMG_LAPLACIAN9) return threed(h) ? OPK_RESID19 : OPK_RESID9;
+  return threed(h) ? OPK_RESID7 : OPK_RESID5;
+}
+
+// Level-1 Q*diag for the integer form of the fused residual; int_ok when
+// every wet cell's value is an integer in 0..127 and the mask is 0/1.
+int prepare_int(cfmg_handle* h) {
+  h->int_ok = false;
+  const int kind = resid_kind(h);
+  if (!fused_ok(h) || kind == OPK_RESID19) return CFMG_OK;
+  const Level& l1 = h->lv[0];
+  if (!h->dq) CUDA_OK(h, cudaMalloc((void**)&h->dq, l1.len));
+  int* ok = (int*)h->partials;  // scratch
+  const int one = 1;
+  CUDA_OK(h, cudaMemcpyAsync(ok, &one, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  launch_make_dq(l1.diag, l1.msk, kind == OPK_RESID9 ? 4.0 : 1.0, h->dq, (long long)l1.len, ok, h->stream);
+  int hok = 0;
+  CUDA_OK(h, cudaMemcpyAsync(&hok, ok, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_OK(h, cudaStreamSynchronize(h->stream));
+  h->int_ok = hok != 0;
+  return CFMG_OK;
+}
+
 int prepare_mixed(cfmg_handle* h) {
   if (!h->mixed_dirty) return CFMG_OK;
   for (Level& l : h->lv) {
@@ -730,6 +765,7 @@ int prepare_mixed(cfmg_handle* h) {
                              h->stream));
   CUDA_OK(h, cudaMemsetAsync(l1.y, 0, l1.len * sizeof(double), h->stream));
   LAUNCH_OK(h);
+  TRY(prepare_int(h));
   h->mixed_dirty = false;
   return CFMG_OK;
 }
@@ -860,6 +896,7 @@ int remove_wet_mean(cfmg_handle* h, double* x) {
 // norm (and wet sum) and the scaled FP32 right-hand side of the next
 // correction; a Neumann operator adds a mean-removing pass.
 bool fused_ok(const cfmg_handle* h) { return !xperio(h) && h->d.op != CFMG_VARCOEF; }
+bool int_path(const cfmg_handle* h) { return h->int_on && h->int_ok && fused_ok(h); }
 
 int fused_residual(cfmg_handle* h) {
   TRY(flush(h));
@@ -876,6 +913,22 @@ int fused_residual(cfmg_handle* h) {
     n = g.len - 2 * g.n1;
   } else {
     n = box_count(bx);
+  }
+  if (int_path(h)) {
+    {
+      // the F-cycle restricts level 1's r first: it must hold the right-hand side too
+      Launch k(h, CFMG_K_RESIDUAL, 1, CFMG_FP64, 2);
+      launch_resid_int(kind, l1.x, l1.b, h->dq, g, bx, lo, n, h->dscal, l1.b32,
+                       h->d.cycle == CFMG_CYCLE_F ? l1.r32 : nullptr, neumann, h->partials, h->stream);
+      launch_fused_final(h->partials, h->dscal, h->dscal + S_NORMB, neumann ? h->dscal + S_NWET : nullptr,
+                         h->d.norm_kind, h->stream);
+    }
+    if (neumann) {
+      Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED);
+      launch_rhs32_shift(l1.msk, h->dscal + S_MEAN2, l1.b32, l1.r32, (long long)l1.len, h->stream);
+    }
+    LAUNCH_OK(h);
+    return CFMG_OK;
   }
   {
     Launch k(h, CFMG_K_RESIDUAL, 1, CFMG_FP64, 2);
@@ -908,7 +961,8 @@ int mixed_iteration(cfmg_handle* h, int kind) {
     TRY(cycle_t<float>(h, kind));
     {
       Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED);
-      launch_update_scaled(l1.x, view<float>(l1).x, h->dscal + S_ICUR, (long long)l1.len, h->stream);
+      if (int_path(h)) launch_update_scaled_max(l1.x, view<float>(l1).x, h->dscal, (long long)l1.len, h->stream);
+      else launch_update_scaled(l1.x, view<float>(l1).x, h->dscal + S_ICUR, (long long)l1.len, h->stream);
     }
     LAUNCH_OK(h);
     return fused_residual(h);
@@ -1241,6 +1295,7 @@ int cfmg_destroy(cfmg_handle* h) {
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   for (double* p : {h->adj_x, h->adj_b, h->adj_gk})
     if (p) cudaFree(p);
+  if (h->dq) cudaFree(h->dq);
   if (h->arena) cudaFree(h->arena);
   if (h->hscal) cudaFreeHost(h->hscal);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -1468,6 +1523,11 @@ int cfmg_solve(cfmg_handle* h, double* res_out, int* nite_out, double* history) 
   LAUNCH_OK(h);
   if (prec == CFMG_MIXED && fused_ok(h)) {
     init_scale<<<1, 1, 0, h->stream>>>(h->dscal);  // the first right-hand side is scaled from |b|
+    if (int_path(h)) {  // fixed-point range of the first pass: max |x|, max |b|
+      CUDA_OK(h, cudaMemsetAsync(h->dscal + S_MAXX, 0, 2 * sizeof(double), h->stream));
+      launch_maxabs2(l1.x, l1.b, (long long)l1.len, h->dscal, h->stream);
+      h->launches += 1;
+    }
     TRY(fused_residual(h));
   } else {
     TRY(normresidual_dev(h, d.norm_kind));
@@ -1663,6 +1723,35 @@ void vsteps_f(std::vector<VStep>& s, const cfmg_desc& d, int D) {
   }
 }
 
+// A smoothing (or the coarsest solve) of a level small enough for one
+// block's shared memory, 2D 5- or 9-point: one BSmall block instead of a
+// launch per sweep. Same sweeps, ranges and arithmetic as smooth_t.
+bool small_smooth(cfmg_handle* h, const VStep& v, BSmall& out) {
+  if (v.op != V_SMOOTH && v.op != V_COARSEST) return false;
+  if (threed(h) || (h->d.op != CFMG_LAPLACIAN && h->d.op != CFMG_LAPLACIAN9)) return false;
+  const int lev = L(h) - v.depth + 1;
+  const Level& l = h->lv[lev - 1];
+  const bool fp64 = v.op == V_COARSEST && coarsest_in_fp64(h);
+  if (4 * (long long)l.len * (fp64 ? 8 : 4) > kBSmallBytes) return false;
+  if (!fp64 && tb_eligible<float>(h, lev)) return false;
+  if (l.xswap) return false;  // the FP32 x must be in x32
+  std::memset(&out, 0, sizeof(out));
+  out.prec = fp64 ? 0 : 1;
+  out.stencil = h->d.op == CFMG_LAPLACIAN9 ? 9 : 5;
+  out.npairs = v.arg;
+  out.g = geom(l);
+  out.ext = Box{l.nh, l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, 1, l.nz};
+  out.in = interior(l);
+  out.lo = out.g.n1;
+  out.n = out.g.len - 2 * out.g.n1;
+  out.b32 = l.b32;
+  out.x32 = l.x32;
+  out.w = fp64 ? (const void*)l.widiag : (const void*)l.widiag32;
+  out.y = fp64 ? (const void*)l.y : (const void*)l.y32;
+  out.cff = 1.0 - h->d.omega;
+  return true;
+}
+
 int record_vstep(cfmg_handle* h, const VStep& v, std::vector<Op>& out) {
   const int nl = L(h);
   const int lev = nl - v.depth + 1;
@@ -1705,17 +1794,26 @@ int lockstep_build(cfmg_batch* b) {
   if (d.cycle == CFMG_CYCLE_F) vsteps_f(vs, d, D);
   else vsteps_v(vs, d, D, false);
   std::vector<std::vector<std::vector<Op>>> rec(ninst);  // [inst][step] -> Ops
+  std::vector<std::vector<BSmall>> smalls(vs.size());     // [step] -> small-level smoothing blocks
   for (int i = 0; i < ninst; ++i) {
     cfmg_handle* h = b->inst[i];
     for (int pass = 0; pass < 2; ++pass) {
       h->record_tb = pass == 0;
       for (Level& l : h->lv) l.xswap = 0;
       rec[i].assign(vs.size(), {});
+      for (auto& sm : smalls)
+        sm.erase(std::remove_if(sm.begin(), sm.end(), [&](const BSmall& q) { return q.inst == i; }), sm.end());
       for (size_t k = 0; k < vs.size(); ++k) {
         VStep v = vs[k];
         if (L(h) < v.need) continue;
         if (k == 0) v.depth = L(h);
         if (L(h) == 1 && v.op != V_ZERO && v.op != V_COARSEST) continue;
+        BSmall sm;
+        if (L(h) > 1 && small_smooth(h, v, sm)) {
+          sm.inst = i;
+          smalls[k].push_back(sm);
+          continue;
+        }
         int rc = record_vstep(h, v, rec[i][k]);
         if (rc != CFMG_OK) return bfail(b, rc, "instance " + std::to_string(i) + ": " + h->err);
         for (Op& op : rec[i][k]) op.inst = i;
@@ -1734,7 +1832,7 @@ int lockstep_build(cfmg_batch* b) {
   auto add_step = [&](std::vector<Op>& ops, int tb, int stencil, int nite) {
     if (ops.empty()) return;
     cfmg_batch::Step st;
-    st.tb = tb; st.stencil = stencil; st.nite = nite;
+    st.tb = tb; st.stencil = stencil; st.nite = nite; st.smem = 0;
     st.tab0 = (long long)tab.size();
     for (const Op& op : ops) {
       const int o = (int)all.size();
@@ -1745,7 +1843,18 @@ int lockstep_build(cfmg_batch* b) {
     st.nchunks = (long long)tab.size() - st.tab0;
     b->steps.push_back(st);
   };
+  std::vector<BSmall> all_small;
   for (size_t k = 0; k < vs.size(); ++k) {
+    if (!smalls[k].empty()) {  // independent of the other instances' Ops of this step
+      cfmg_batch::Step st;
+      st.tb = 2; st.stencil = 0; st.nite = 0;
+      st.tab0 = (long long)all_small.size();
+      st.nchunks = (long long)smalls[k].size();
+      st.smem = 0;
+      for (const BSmall& q : smalls[k]) st.smem = std::max(st.smem, (int)(4 * q.g.len * (q.prec == 0 ? 8 : 4)));
+      all_small.insert(all_small.end(), smalls[k].begin(), smalls[k].end());
+      b->steps.push_back(st);
+    }
     size_t depth = 0;
     for (int i = 0; i < ninst; ++i) depth = std::max(depth, rec[i][k].size());
     for (size_t q = 0; q < depth; ++q) {
@@ -1803,6 +1912,10 @@ int lockstep_build(cfmg_batch* b) {
   BCUDA(b, cudaMalloc((void**)&b->nactive, sizeof(int)));
   BCUDA(b, cudaMemset(b->active, 0, sizeof(int) * ninst));
   BCUDA(b, cudaMemset(b->nactive, 0, sizeof(int)));
+  if (!all_small.empty()) {
+    BCUDA(b, cudaMalloc((void**)&b->ssm, sizeof(BSmall) * all_small.size()));
+    BCUDA(b, cudaMemcpy(b->ssm, all_small.data(), sizeof(BSmall) * all_small.size(), cudaMemcpyHostToDevice));
+  }
   if (!all.empty()) {
     BCUDA(b, cudaMalloc((void**)&b->sops, sizeof(Op) * all.size()));
     BCUDA(b, cudaMemcpy(b->sops, all.data(), sizeof(Op) * all.size(), cudaMemcpyHostToDevice));
@@ -1840,7 +1953,9 @@ int lockstep_build(cfmg_batch* b) {
     launch_bfinal(b->bi, b->l1start, ninst, b->bpart, b->active, b->nactive, b->stream);
     if (neumann) launch_brhs(b->bi, b->l1tab, b->l1chunks, b->active, b->stream);
     for (const cfmg_batch::Step& st : b->steps) {
-      if (st.tb) {
+      if (st.tb == 2) {
+        launch_bsmall(b->ssm + st.tab0, (int)st.nchunks, st.smem, b->active, b->stream);
+      } else if (st.tb) {
         if (!launch_btb(st.stencil, st.nite, b->sops, b->stab + st.tab0, st.nchunks, b->active, b->stream)) {
           cudaStreamEndCapture(b->stream, &body);
           return bfail(b, CFMG_ERR_UNSUPPORTED, "blocked pass shape");
@@ -1906,7 +2021,7 @@ int cfmg_batch_destroy(cfmg_batch* b) {
   for (cfmg_handle* h : b->inst) cfmg_destroy(h);
   for (void* p : {(void*)b->progs, (void*)b->ptrs, (void*)b->nops, (void*)b->counter, (void*)b->red, (void*)b->sc,
                   (void*)b->nwet, (void*)b->bi, (void*)b->l1start, (void*)b->l1tab, (void*)b->bpart,
-                  (void*)b->active, (void*)b->nactive, (void*)b->sops, (void*)b->stab})
+                  (void*)b->active, (void*)b->nactive, (void*)b->sops, (void*)b->stab, (void*)b->ssm})
     if (p) cudaFree(p);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
@@ -1934,7 +2049,7 @@ int cfmg_batch_solve(cfmg_batch* b, int zero_x, double* res, int* nite, double* 
     for (void** p : {(void**)&b->progs, (void**)&b->ptrs, (void**)&b->nops, (void**)&b->counter, (void**)&b->red,
                      (void**)&b->sc, (void**)&b->nwet, (void**)&b->bi, (void**)&b->l1start, (void**)&b->l1tab,
                      (void**)&b->bpart, (void**)&b->active, (void**)&b->nactive, (void**)&b->sops,
-                     (void**)&b->stab})
+                     (void**)&b->stab, (void**)&b->ssm})
       if (*p) {
         cudaFree(*p);
         *p = nullptr;
@@ -1976,6 +2091,11 @@ int cfmg_set_option(cfmg_handle* h, int option, long long value) {
   }
   if (option == CFMG_OPT_TEMPORAL_BLOCKING) {
     h->tb_on = value != 0;
+    drop_graphs(h);
+    return CFMG_OK;
+  }
+  if (option == CFMG_OPT_INT_RESIDUAL) {
+    h->int_on = value != 0;
     drop_graphs(h);
     return CFMG_OK;
   }

@@ -195,6 +195,25 @@ struct BInst {
   int kind, neumann, norm_kind, maxite;
   double tol;
 };
+// Smoothing of a small level (the coarsest solve, or a coarse level's
+// pre/post smoothing) of one instance by one block in shared memory: x, b,
+// omega*idiag and y are staged, the npairs pairs of sweeps run with the
+// operator's own ranges and per-cell arithmetic (prec 0: FP64, the FP32
+// x and b converted as the coarsest solve does), and x goes back to x32.
+struct BSmall {
+  int inst, prec, stencil, npairs;  // stencil 5: linear range lo..lo+n; 9: ext then interior box
+  Geom g;
+  Box ext, in;
+  long long lo, n;
+  const float* b32;
+  float* x32;
+  const void* w;  // omega*idiag, FP64 or FP32 as prec
+  const void* y;  // the level's partner buffer (cells outside the sweep ranges are read, never written)
+  double cff;
+};
+constexpr int kBSmallBytes = 96 * 1024;  // shared memory of one block: 4 arrays
+void launch_bsmall(const BSmall* s, int n, int smem, const int* active, cudaStream_t st);
+
 // Work tables: one int4 per chunk (or tile) = {Op or instance, chunk of it,
 // instance, 0}; a launch compacts the active entries of each window.
 void launch_bstage(const Op* ops, const int4* tab, long long nchunks, const int* active, cudaStream_t s);
@@ -212,7 +231,7 @@ void launch_bcond(cudaGraphConditionalHandle hc, int* nactive, cudaStream_t s);
 
 // device scalars of a handle (dscal[])
 enum Scal { S_NORM = 0, S_RES = 1, S_NORMB = 2, S_NWET = 3, S_SCALE = 4, S_MEAN = 5, S_TMP0 = 6, S_ISCALE = 7,
-            S_NEXT = 8, S_CUR = 9, S_ICUR = 10, S_MEAN2 = 11, S_COUNT = 16 };
+            S_NEXT = 8, S_CUR = 9, S_ICUR = 10, S_MEAN2 = 11, S_MAXX = 12, S_MAXB = 13, S_COUNT = 16 };
 
 // fused FP64 steps of the mixed loop (k_mixed.cu)
 void launch_resid_fused(int kind, double* r, const double* x, const double* b, const double* d, const uint8_t* m,
@@ -223,6 +242,15 @@ void launch_fused_final(const double* partials, double* ds, const double* normb,
 void launch_rhs32_mean(const double* r, const uint8_t* m, const double* mean_scale, float* b32, float* r32,
                        long long n, cudaStream_t s);
 void launch_update_scaled(double* x, const float* e, const double* iscale, long long n, cudaStream_t s);
+// integer form of the fused pass (kinds 5-, 7- and 9-point)
+void launch_resid_int(int kind, const double* x, const double* b, const int8_t* dq, const Geom& g, const Box& bx,
+                      long long lo, long long n, const double* ds, float* b32, float* r32, bool neumann,
+                      double* partials, cudaStream_t s);
+void launch_rhs32_shift(const uint8_t* m, const double* mean_scale, float* b32, float* r32, long long n,
+                        cudaStream_t s);
+void launch_make_dq(const double* diag, const uint8_t* m, double Q, int8_t* dq, long long n, int* ok, cudaStream_t s);
+void launch_maxabs2(const double* x, const double* b, long long n, double* ds, cudaStream_t s);
+void launch_update_scaled_max(double* x, const float* e, double* ds, long long n, cudaStream_t s);
 
 // message returned by cfmg_last_error(NULL) (cfmg_api.cu)
 void set_global_error(const std::string& msg);

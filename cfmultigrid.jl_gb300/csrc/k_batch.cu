@@ -333,6 +333,57 @@ __global__ void __launch_bounds__(kBThreads) k_bupdate(const BInst* __restrict__
   }
 }
 
+template <class T>
+__device__ void bsmall_run(const BSmall& s, T* X, T* Y, T* B, T* W) {
+  const long long len = s.g.len;
+  for (long long t = threadIdx.x; t < len; t += blockDim.x) {
+    X[t] = (T)s.x32[t];
+    B[t] = (T)s.b32[t];
+    W[t] = ((const T*)s.w)[t];
+    Y[t] = ((const T*)s.y)[t];
+  }
+  __syncthreads();
+  const T cff = (T)s.cff;
+  const long long n1 = s.g.n1;
+  for (int p = 0; p < s.npairs; ++p) {
+    if (s.stencil == 5) {
+      for (long long t = threadIdx.x; t < s.n; t += blockDim.x) Y[s.lo + t] = v_sweep5(X, B, W, cff, n1, s.lo + t);
+      __syncthreads();
+      for (long long t = threadIdx.x; t < s.n; t += blockDim.x) X[s.lo + t] = v_sweep5(Y, B, W, cff, n1, s.lo + t);
+      __syncthreads();
+    } else {
+      int i, j, k;
+      const long long ne = (long long)(s.ext.i1 - s.ext.i0 + 1) * (s.ext.j1 - s.ext.j0 + 1) * (s.ext.k1 - s.ext.k0 + 1);
+      for (long long t = threadIdx.x; t < ne; t += blockDim.x) {
+        box3(s.ext, t, i, j, k);
+        const long long I = lin(s.g, i, j, k);
+        Y[I] = v_sweep9(X, B, W, cff, n1, I);
+      }
+      __syncthreads();
+      const long long ni = (long long)(s.in.i1 - s.in.i0 + 1) * (s.in.j1 - s.in.j0 + 1) * (s.in.k1 - s.in.k0 + 1);
+      for (long long t = threadIdx.x; t < ni; t += blockDim.x) {
+        box3(s.in, t, i, j, k);
+        const long long I = lin(s.g, i, j, k);
+        X[I] = v_sweep9(Y, B, W, cff, n1, I);
+      }
+      __syncthreads();
+    }
+  }
+  for (long long t = threadIdx.x; t < len; t += blockDim.x) s.x32[t] = (float)X[t];
+}
+
+__global__ void __launch_bounds__(kBThreads) k_bsmall(const BSmall* __restrict__ sm, const int* __restrict__ active) {
+  extern __shared__ double dsm[];
+  const BSmall& s = sm[blockIdx.x];
+  if (!active[s.inst]) return;
+  const long long len = s.g.len;
+  if (s.prec == 0) bsmall_run<double>(s, dsm, dsm + len, dsm + 2 * len, dsm + 3 * len);
+  else {
+    float* f = (float*)dsm;
+    bsmall_run<float>(s, f, f + len, f + 2 * len, f + 3 * len);
+  }
+}
+
 // the `while` condition: another iteration while any instance continues
 __global__ void k_bcond(cudaGraphConditionalHandle hc, int* nactive) {
   const int n = *nactive;
@@ -398,6 +449,16 @@ void launch_bupdate(const BInst* bi, const int4* tab, long long nchunks, const i
   int win;
   const unsigned g = (unsigned)grid_for(nchunks, 6, &win);
   k_bupdate<<<g, kBThreads, 0, s>>>(bi, tab, nchunks, win, active);
+}
+
+void launch_bsmall(const BSmall* sm, int n, int smem, const int* active, cudaStream_t st) {
+  if (n <= 0) return;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_bsmall, cudaFuncAttributeMaxDynamicSharedMemorySize, kBSmallBytes);
+    attr = true;
+  }
+  k_bsmall<<<n, kBThreads, smem, st>>>(sm, active);
 }
 
 void launch_bcond(cudaGraphConditionalHandle hc, int* nactive, cudaStream_t s) {

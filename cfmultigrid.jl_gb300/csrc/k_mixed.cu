@@ -123,6 +123,7 @@ __global__ void __launch_bounds__(kMxParts) k_fused_final(const double* __restri
     int e = 0;
     if (rms > 0 && isfinite(rms)) frexp(rms, &e);
     ds[S_NEXT] = ldexp(1.0, -e);
+    ds[S_MAXX] = 0.0;  // the next update collects max |x| afresh
   }
 }
 
@@ -143,6 +144,232 @@ __global__ void k_update_scaled(double* __restrict__ x, const float* __restrict_
                                 long long n) {
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I < n) x[I] = __fma_rn((double)e[I], is[0], x[I]);
+}
+
+// ----------------------------------------------------------------------
+// Integer form of the fused pass. The FP64 pipe of a GB300 runs at 1/64 of
+// the FP32 rate, and the FP64 stencil arithmetic above keeps it busy
+// (about 13 FP64 operations a cell). Here x and b are read as FP64 but
+// converted with integer operations to 64-bit fixed point, v * 2^k rounded
+// to an integer, with k = 58 - E for max(|x|, |b|) < 2^E (S_MAXX, S_MAXB).
+// The residual Q*r = Q*(diag*x + b) - (stencil sum), with Q = 4 for the
+// 9-point weights 1/2 and 1/4 and Q = 1 otherwise, is then an exact
+// integer (|Q r| 2^k < 2^63), so it carries no rounding at all: its error
+// is that of representing x on the 2^-k grid, below 2^-58 max|x| per cell
+// (FP64 arithmetic on the same x rounds at 2^-53 |x| per operation). The
+// FP64 pipe is left with two conversions and one FMA a cell: sum r^2 in
+// FP64 and the FP32 right-hand side. The cell-centred sum r is kept exact
+// in 128-bit integers per thread.
+//
+// dq[I] = Q*diag[I] (an integer in 0..127) on wet cells, -128 on dry ones.
+
+// round(v * 2^k) for |v| 2^k < 2^59; zero and subnormal v give 0
+__device__ __forceinline__ long long to_fix(double v, int k) {
+  const long long u = __double_as_longlong(v);
+  const int ex = (int)(((unsigned long long)u >> 52) & 0x7ffULL);
+  const long long m = (u & 0x000FFFFFFFFFFFFFLL) | 0x0010000000000000LL;
+  const int sh = ex - 1075 + k;  // v = m 2^(ex-1075)
+  long long r;
+  if (sh >= 0) {
+    r = m << sh;
+  } else {
+    const int s = -sh;  // round half up on the magnitude
+    r = s <= 64 ? ((m >> (s - 1)) + 1) >> 1 : 0;
+  }
+  r = ex ? r : 0;
+  return u < 0 ? -r : r;
+}
+
+__device__ __forceinline__ int fix_exponent(const double* ds) {
+  const double mx = fmax(ds[S_MAXX], ds[S_MAXB]);
+  int e = 0;
+  if (mx > 0 && isfinite(mx)) frexp(mx, &e);  // mx < 2^e
+  return 58 - e;
+}
+
+template <int KIND>
+__device__ __forceinline__ long long fix_resid(const double* __restrict__ x, const double* __restrict__ b, int dq,
+                                               int k, long long n1, long long n2, long long I) {
+  if (dq < 0) return 0;
+  const long long X = to_fix(x[I], k), B = to_fix(b[I], k);
+  if (KIND == OPK_RESID9) {
+    const long long F = to_fix(x[I - 1], k) + to_fix(x[I + 1], k) + to_fix(x[I - n1], k) + to_fix(x[I + n1], k);
+    const long long D = to_fix(x[I - 1 - n1], k) + to_fix(x[I + 1 - n1], k) + to_fix(x[I - 1 + n1], k) +
+                        to_fix(x[I + 1 + n1], k);
+    return (long long)dq * X + 4 * B - 2 * F - D;
+  } else if (KIND == OPK_RESID7) {
+    const long long F = to_fix(x[I - 1], k) + to_fix(x[I + 1], k) + to_fix(x[I - n1], k) + to_fix(x[I + n1], k) +
+                        to_fix(x[I - n2], k) + to_fix(x[I + n2], k);
+    return (long long)dq * X + B - F;
+  } else {
+    const long long F = to_fix(x[I - 1], k) + to_fix(x[I + 1], k) + to_fix(x[I - n1], k) + to_fix(x[I + n1], k);
+    return (long long)dq * X + B - F;
+  }
+}
+
+// per-block partial sums: partials[blk] = sum r^2, partials[kMxParts + blk]
+// = sum r. NEUMANN: b32 = (float)(r * scale) here, the mean comes off in a
+// second pass (which also writes r32); else b32 and, when r32 != nullptr,
+// r32 get the right-hand side.
+template <int KIND, bool NEUMANN>
+__global__ void __launch_bounds__(kMxThreads) k_resid_int(const double* __restrict__ x, const double* __restrict__ b,
+                                                          const int8_t* __restrict__ dq, Geom g, Box bx, long long lo,
+                                                          long long n, const double* __restrict__ ds,
+                                                          float* __restrict__ b32, float* __restrict__ r32,
+                                                          double* __restrict__ partials) {
+  constexpr int q = (KIND == OPK_RESID9) ? 2 : 0;  // Q = 2^q
+  const int k = fix_exponent(ds);
+  const float fm = (float)ldexp(ds[S_NEXT], -(k + q));  // power of two: R -> r * scale
+  double s2 = 0.0;
+  __int128 s1 = 0;
+  const long long ni = bx.i1 - bx.i0 + 1, nj = bx.j1 - bx.j0 + 1;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    long long I;
+    if (KIND == OPK_RESID5) {
+      I = lo + t;
+    } else {
+      const int i = bx.i0 + (int)(t % ni);
+      const long long qq = t / ni;
+      I = lin(g, i, bx.j0 + (int)(qq % nj), bx.k0 + (int)(qq / nj));
+    }
+    const long long R = fix_resid<KIND>(x, b, dq[I], k, g.n1, g.n2, I);
+    const double rd = __ll2double_rn(R);
+    s2 = __fma_rn(rd, rd, s2);
+    const float f = __ll2float_rn(R) * fm;
+    b32[I] = f;
+    if (NEUMANN) s1 += (__int128)R;
+    else if (r32) r32[I] = f;
+  }
+  // per-thread exact sum r -> double (hi 2^64 + lo)
+  const double s1d = NEUMANN ? __dadd_rn(__dmul_rn((double)(long long)(s1 >> 64), 18446744073709551616.0),
+                                         (double)(unsigned long long)s1)
+                             : 0.0;
+  __shared__ double sh2[kMxThreads / 32], sh1[kMxThreads / 32];
+  double a2 = s2, a1 = s1d;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a2 += __shfl_down_sync(0xffffffffu, a2, o);
+    a1 += __shfl_down_sync(0xffffffffu, a1, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sh2[threadIdx.x >> 5] = a2;
+    sh1[threadIdx.x >> 5] = a1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double u = 0.0, v = 0.0;
+    for (int w = 0; w < kMxThreads / 32; ++w) {
+      u += sh2[w];
+      v += sh1[w];
+    }
+    partials[blockIdx.x] = ldexp(u, -2 * (k + q));
+    partials[kMxParts + blockIdx.x] = ldexp(v, -(k + q));
+  }
+}
+
+// cell-centred second pass: b32 = r32 = msk ? b32 - mean * scale : 0 with
+// ms[0] = S_MEAN2 and ms[1] = S_CUR
+__global__ void k_rhs32_shift(const uint8_t* __restrict__ m, const double* __restrict__ ms, float* __restrict__ b32,
+                              float* __restrict__ r32, long long n) {
+  long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= n) return;
+  const float sh = (float)(ms[0] * ms[S_CUR - S_MEAN2]);
+  const float f = m[I] ? __fsub_rn(b32[I], sh) : 0.f;
+  b32[I] = f;
+  r32[I] = f;
+}
+
+// dq from diag and msk; *ok is cleared when a wet cell's Q*diag is not an
+// integer in 0..127 or a mask value is not 0/1
+__global__ void k_make_dq(const double* __restrict__ diag, const uint8_t* __restrict__ m, double Q, int8_t* dq,
+                          long long n, int* ok) {
+  long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= n) return;
+  int8_t v = -128;
+  if (m[I] == 1) {
+    const double qd = diag[I] * Q;
+    if (qd >= 0.0 && qd <= 127.0 && qd == floor(qd)) v = (int8_t)qd;
+    else atomicAnd(ok, 0);
+  } else if (m[I] != 0) {
+    atomicAnd(ok, 0);
+  }
+  dq[I] = v;
+}
+
+// max |x| and max |b| (as the bit patterns of non-negative doubles, which
+// order like the values) into ds[S_MAXX], ds[S_MAXB]; both start at 0
+__global__ void k_maxabs2(const double* __restrict__ x, const double* __restrict__ b, long long n, double* ds) {
+  unsigned long long mx = 0, mb = 0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long ux = (unsigned long long)__double_as_longlong(x[t]) & 0x7FFFFFFFFFFFFFFFULL;
+    const unsigned long long ub = (unsigned long long)__double_as_longlong(b[t]) & 0x7FFFFFFFFFFFFFFFULL;
+    mx = ux > mx ? ux : mx;
+    mb = ub > mb ? ub : mb;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long ox = __shfl_down_sync(0xffffffffu, mx, o), ob = __shfl_down_sync(0xffffffffu, mb, o);
+    mx = ox > mx ? ox : mx;
+    mb = ob > mb ? ob : mb;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax((unsigned long long*)(ds + S_MAXX), mx);
+    atomicMax((unsigned long long*)(ds + S_MAXB), mb);
+  }
+}
+
+// x += e * iscale, with max |x| of the result into ds[S_MAXX] (reset by the
+// fused pass's final reduction)
+__global__ void k_update_scaled_max(double* __restrict__ x, const float* __restrict__ e, const double* __restrict__ ds,
+                                    long long n, double* dsw) {
+  long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long mx = 0;
+  if (I < n) {
+    const double v = __fma_rn((double)e[I], ds[S_ICUR], x[I]);
+    x[I] = v;
+    mx = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFULL;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long ox = __shfl_down_sync(0xffffffffu, mx, o);
+    mx = ox > mx ? ox : mx;
+  }
+  if ((threadIdx.x & 31) == 0 && mx) atomicMax((unsigned long long*)(dsw + S_MAXX), mx);
+}
+
+void launch_resid_int(int kind, const double* x, const double* b, const int8_t* dq, const Geom& g, const Box& bx,
+                      long long lo, long long n, const double* ds, float* b32, float* r32, bool neumann,
+                      double* partials, cudaStream_t s) {
+#define CFMG_INT(K)                                                                                        \
+  if (kind == K) {                                                                                         \
+    if (neumann)                                                                                           \
+      k_resid_int<K, true><<<kMxParts, kMxThreads, 0, s>>>(x, b, dq, g, bx, lo, n, ds, b32, r32, partials); \
+    else                                                                                                   \
+      k_resid_int<K, false><<<kMxParts, kMxThreads, 0, s>>>(x, b, dq, g, bx, lo, n, ds, b32, r32, partials); \
+    return;                                                                                                \
+  }
+  CFMG_INT(OPK_RESID5)
+  CFMG_INT(OPK_RESID9)
+  CFMG_INT(OPK_RESID7)
+#undef CFMG_INT
+}
+
+void launch_rhs32_shift(const uint8_t* m, const double* mean_scale, float* b32, float* r32, long long n,
+                        cudaStream_t s) {
+  k_rhs32_shift<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(m, mean_scale, b32, r32, n);
+}
+
+void launch_make_dq(const double* diag, const uint8_t* m, double Q, int8_t* dq, long long n, int* ok,
+                    cudaStream_t s) {
+  k_make_dq<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(diag, m, Q, dq, n, ok);
+}
+
+void launch_maxabs2(const double* x, const double* b, long long n, double* ds, cudaStream_t s) {
+  k_maxabs2<<<1024, 256, 0, s>>>(x, b, n, ds);
+}
+
+void launch_update_scaled_max(double* x, const float* e, double* ds, long long n, cudaStream_t s) {
+  k_update_scaled_max<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, e, ds, n, ds);
 }
 
 void launch_resid_fused(int kind, double* r, const double* x, const double* b, const double* d, const uint8_t* m,

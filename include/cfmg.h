@@ -102,6 +102,9 @@ extern "C" {
                                     0 never (FP32), 1 always */
 #define CFMG_OPT_TEMPORAL_BLOCKING 1 /* 1 (default): FP32 smoothing of fine 2D levels runs all
                                         sweeps of a call in one shared-memory pass; 0: one kernel per sweep */
+#define CFMG_OPT_INT_RESIDUAL 3 /* mixed form, closed topology, 5-, 7- and 2D 9-point operators: 1
+                                   (default) computes the level-1 residual exactly in 64-bit fixed point
+                                   on the integer pipes; 0 in FP64 arithmetic */
 
 typedef struct cfmg_desc {
   int kase;     /* CFMG_TWOD / CFMG_THREED            (Param.case) */

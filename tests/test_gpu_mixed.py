@@ -125,3 +125,35 @@ def test_temporal_blocking_is_bit_identical(name):
         out.append((hist, mg.data[1].x))
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("name", ["config1_256_centers_v", "config2_512_vertices_lap9_f", "3d_48_centers_v"])
+def test_integer_residual_matches_fp64_residual(name):
+    """The fixed-point level-1 residual (default) against the FP64-arithmetic
+    one: same iteration count, residual histories to 1e-6, same solution."""
+    base, mkind = CASES[name]
+    out = {}
+    for on in (1, 0):
+        mg = cfmg.get_gmg(cfmg.Param(**base, tol=1e-10, maxite=40, residual_norm="l2", precision="mixed",
+                                     verbose=False))
+        custom = _mask(base, mg.shape(1), mkind)
+        if custom is not None:
+            mg.oper[1].msk = custom
+            cfmg.setup_operators(mg)
+            for lev in range(1, mg.nlevels + 1):
+                for f in ("x", "y", "r", "b"):
+                    cfmg.set_to_zero(mg, lev, f)
+        msk = mg.download(1, "msk")
+        b = np.asfortranarray(np.random.default_rng(9).standard_normal(mg.shape(1))) * msk
+        F.subtract_mean(b, msk.astype(np.float64))
+        mg.data[1].b = b
+        mg.set_option("int_residual", on)
+        res, n, hist = cfmg.solve(mg, history=True)
+        out[on] = (res, n, hist, mg.data[1].x, msk.astype(bool))
+    (r1, n1, h1, x1, w), (r0, n0, h0, x0, _) = out[1], out[0]
+    assert r1 <= 1e-10 and r0 <= 1e-10 and n1 == n0, (r1, r0, n1, n0)
+    np.testing.assert_allclose(h1, h0, rtol=1e-6)
+    singular = base.get("location", "centers") == "centers"
+    a = _wet_mean_removed(x1, w) if singular else x1 * w
+    c = _wet_mean_removed(x0, w) if singular else x0 * w
+    assert np.linalg.norm(a - c) <= 1e-8 * np.linalg.norm(c)
