@@ -52,6 +52,8 @@ def parse():
                     help="config3: the 3D 7-point case; config4: batched solves of uneven sizes (one graph launch per batch); config5: forward + adjoint solves")
     ap.add_argument("--ninst", type=int, default=2048, help="config4 batch size")
     ap.add_argument("--no-tune", action="store_true", help="config4: F(2,2) without the autotuner")
+    ap.add_argument("--host-loop", action="store_true",
+                    help="config4: the host repeats the batched iteration (a launch list for ncu)")
     ap.add_argument("--quick", action="store_true",
                     help="mixed form only: one warm-up and one timed solve (a short run for ncu)")
     return ap.parse_args()
@@ -569,6 +571,8 @@ def run_batch(args, rank, world, local):
     t_tune = time.perf_counter() - t0
     t0 = time.perf_counter()
     batch = make(p, list(range(len(probs))))
+    if args.host_loop:
+        batch.set_option("host_loop", 1)
     t_setup = time.perf_counter() - t0
     for _ in range(max(args.warmup, 3)):
         batch.solve()

@@ -449,6 +449,11 @@ class Batch:
                                              t.ctypes.data_as(ctypes.c_void_p)))
         return res, nite, t
 
+    def set_option(self, name: str, value: int) -> None:
+        """Batch options: "host_loop" (1: the host repeats the lockstep
+        iteration instead of the graph's while node; for profilers)."""
+        self._check(self._L.cfmg_batch_set_option(self._b, _lib.BATCH_OPTIONS[name], int(value)))
+
     def close(self):
         b = getattr(self, "_b", None)
         if b is not None and b.value:

@@ -34,9 +34,10 @@ EXPORTS = (
     "cfmg_prolong", "cfmg_zero", "cfmg_fill", "cfmg_norm", "cfmg_normresidual", "cfmg_cycle", "cfmg_solve",
     "cfmg_launch_count", "cfmg_profile", "cfmg_profile_read", "cfmg_set_option", "cfmg_norm_noalloc",
     "cfmg_adjoint", "cfmg_batch_create", "cfmg_batch_destroy", "cfmg_batch_instance", "cfmg_batch_solve",
-    "cfmg_batch_last_error",
+    "cfmg_batch_last_error", "cfmg_batch_set_option",
 )
 OPTIONS = {"engine_cells": 0, "temporal_blocking": 1, "coarsest_fp64": 2, "int_residual": 3}
+BATCH_OPTIONS = {"host_loop": 0}
 KERNEL_CLASSES = {"sweep": 0, "residual": 1, "restrict": 2, "prolong": 3, "norm": 4, "fill": 5, "convert": 6,
                   "engine": 7}
 
@@ -102,6 +103,7 @@ def load() -> ctypes.CDLL:
         "cfmg_batch_destroy": [vp],
         "cfmg_batch_instance": [vp, i, ctypes.POINTER(vp)],
         "cfmg_batch_solve": [vp, i, vp, vp, vp],
+        "cfmg_batch_set_option": [vp, i, ctypes.c_longlong],
     }
     for name, args in sig.items():
         f = getattr(L, name)

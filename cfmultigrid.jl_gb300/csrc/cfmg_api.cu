@@ -96,6 +96,9 @@ struct cfmg_batch {
   Op* sops = nullptr;          // the Ops of all cycle steps (device)
   int4* stab = nullptr;        // their chunk (or tile) tables {Op, chunk, instance, 0} (device)
   BSmall* ssm = nullptr;       // small-level smoothing descriptors (device)
+  bool host_loop = false;      // CFMG_BOPT_HOST_LOOP
+  int kind = 0;
+  bool neumann = false;
   struct Step {
     int tb, stencil, nite;     // tb: OPK_TB Ops of one (stencil, nite); tb == 2: BSmall blocks
     long long tab0;            // offset into stab (or ssm)
@@ -1772,6 +1775,26 @@ int record_vstep(cfmg_handle* h, const VStep& v, std::vector<Op>& out) {
   return rc;
 }
 
+// One lockstep iteration of every active instance (see k_batch.cu).
+int lockstep_body(cfmg_batch* b) {
+  const int ninst = (int)b->inst.size();
+  launch_bres(b->kind, b->neumann, b->bi, b->l1tab, b->l1chunks, b->active, b->bpart, b->stream);
+  launch_bfinal(b->bi, b->l1start, ninst, b->bpart, b->active, b->nactive, b->stream);
+  if (b->neumann) launch_brhs(b->bi, b->l1tab, b->l1chunks, b->active, b->stream);
+  for (const cfmg_batch::Step& st : b->steps) {
+    if (st.tb == 2) {
+      launch_bsmall(b->ssm + st.tab0, (int)st.nchunks, st.smem, b->active, b->stream);
+    } else if (st.tb) {
+      if (!launch_btb(st.stencil, st.nite, b->sops, b->stab + st.tab0, st.nchunks, b->active, b->stream))
+        return bfail(b, CFMG_ERR_UNSUPPORTED, "blocked pass shape");
+    } else {
+      launch_bstage(b->sops, b->stab + st.tab0, st.nchunks, b->active, b->stream);
+    }
+  }
+  launch_bupdate(b->bi, b->l1tab, b->l1chunks, b->active, b->stream);
+  return CFMG_OK;
+}
+
 int lockstep_build(cfmg_batch* b) {
   const int ninst = (int)b->inst.size();
   const cfmg_desc& d = b->d;
@@ -1922,10 +1945,10 @@ int lockstep_build(cfmg_batch* b) {
     BCUDA(b, cudaMalloc((void**)&b->stab, sizeof(int4) * tab.size()));
     BCUDA(b, cudaMemcpy(b->stab, tab.data(), sizeof(int4) * tab.size(), cudaMemcpyHostToDevice));
   }
-  const int kind = hb[0].kind;
-  const bool neumann = hb[0].neumann;
+  b->kind = hb[0].kind;
+  b->neumann = hb[0].neumann != 0;
   for (int i = 1; i < ninst; ++i)
-    if (hb[i].kind != kind || hb[i].neumann != neumann)
+    if (hb[i].kind != b->kind || (hb[i].neumann != 0) != b->neumann)
       return bfail(b, CFMG_ERR_ARG, "batched instances must share the operator and location");
   // the graph: init, then while (any instance iterates) { iteration }
   for (int z = 0; z < 2; ++z) {
@@ -1949,22 +1972,12 @@ int lockstep_build(cfmg_batch* b) {
     BCUDA(b, cudaGraphAddNode(&cnode, g, &init, nullptr, 1, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     BCUDA(b, cudaStreamBeginCaptureToGraph(b->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    launch_bres(kind, neumann, b->bi, b->l1tab, b->l1chunks, b->active, b->bpart, b->stream);
-    launch_bfinal(b->bi, b->l1start, ninst, b->bpart, b->active, b->nactive, b->stream);
-    if (neumann) launch_brhs(b->bi, b->l1tab, b->l1chunks, b->active, b->stream);
-    for (const cfmg_batch::Step& st : b->steps) {
-      if (st.tb == 2) {
-        launch_bsmall(b->ssm + st.tab0, (int)st.nchunks, st.smem, b->active, b->stream);
-      } else if (st.tb) {
-        if (!launch_btb(st.stencil, st.nite, b->sops, b->stab + st.tab0, st.nchunks, b->active, b->stream)) {
-          cudaStreamEndCapture(b->stream, &body);
-          return bfail(b, CFMG_ERR_UNSUPPORTED, "blocked pass shape");
-        }
-      } else {
-        launch_bstage(b->sops, b->stab + st.tab0, st.nchunks, b->active, b->stream);
-      }
+    const int rb = lockstep_body(b);
+    if (rb != CFMG_OK) {
+      cudaStreamEndCapture(b->stream, &body);
+      cudaGraphDestroy(g);
+      return rb;
     }
-    launch_bupdate(b->bi, b->l1tab, b->l1chunks, b->active, b->stream);
     launch_bcond(hc, b->nactive, b->stream);
     e = cudaStreamEndCapture(b->stream, &body);
     if (e != cudaSuccess) return bfail(b, CFMG_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
@@ -2036,6 +2049,15 @@ int cfmg_batch_instance(cfmg_batch* b, int i, cfmg_handle** h) {
 
 const char* cfmg_batch_last_error(const cfmg_batch* b) { return b ? b->err.c_str() : ""; }
 
+int cfmg_batch_set_option(cfmg_batch* b, int option, long long value) {
+  if (!b) return CFMG_ERR_ARG;
+  if (option == CFMG_BOPT_HOST_LOOP) {
+    b->host_loop = value != 0;
+    return CFMG_OK;
+  }
+  return bfail(b, CFMG_ERR_ARG, "unknown batch option");
+}
+
 int cfmg_batch_solve(cfmg_batch* b, int zero_x, double* res, int* nite, double* t_done_ms) {
   if (!b) return CFMG_ERR_ARG;
   for (cfmg_handle* h : b->inst)
@@ -2057,8 +2079,20 @@ int cfmg_batch_solve(cfmg_batch* b, int zero_x, double* res, int* nite, double* 
     b->steps.clear();
     TRY(b->lockstep ? lockstep_build(b) : batch_build(b));
   }
-  BCUDA(b, cudaGraphLaunch(b->graph[zero_x ? 1 : 0], b->stream));
   const int ninst = (int)b->inst.size();
+  if (b->lockstep && b->host_loop) {
+    launch_binit(b->bi, ninst, zero_x ? 1 : 0, b->active, b->nactive, b->stream);
+    for (;;) {
+      TRY(lockstep_body(b));
+      int na = 0;
+      BCUDA(b, cudaMemcpyAsync(&na, b->nactive, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+      BCUDA(b, cudaMemsetAsync(b->nactive, 0, sizeof(int), b->stream));
+      BCUDA(b, cudaStreamSynchronize(b->stream));
+      if (na == 0) break;
+    }
+  } else {
+    BCUDA(b, cudaGraphLaunch(b->graph[zero_x ? 1 : 0], b->stream));
+  }
   BCUDA(b, cudaMemcpyAsync(b->hsc.data(), b->sc, sizeof(double) * b->hsc.size(), cudaMemcpyDeviceToHost, b->stream));
   BCUDA(b, cudaStreamSynchronize(b->stream));
   const int kt0 = b->lockstep ? (int)BS_T0 : (int)SS_T0, kt1 = b->lockstep ? (int)BS_T1 : (int)SS_T1;

@@ -200,12 +200,19 @@ CFMG_API int cfmg_adjoint(cfmg_handle* h, const double* g, double* grad_b, doubl
  * handle (cfmg_batch_instance): upload its mask, run cfmg_setup_operators,
  * upload b, and read x back through the usual entry points.
  * cfmg_batch_solve runs every instance's whole mixed-precision solve in one
- * launch of the batched engine (a graph of one kernel), from x = 0 when
- * zero_x is non-zero and else from each instance's current x (as solve!
- * does); clusters take the
- * instances largest first from a device queue, and each instance stops at
- * its own tolerance. res, nite and t_done_ms (time from the batch start to
- * that instance's convergence) receive ninst entries each; any may be NULL. */
+ * graph launch, from x = 0 when zero_x is non-zero and else from each
+ * instance's current x (as solve! does). For the 5- and 9-point operators
+ * the instances advance in lockstep: each kernel of an iteration covers all
+ * instances that have not yet converged, and a graph `while` node repeats
+ * the iteration until none is left (the variable-coefficient operator runs
+ * each instance's whole solve as a program of the cluster engine instead).
+ * Each instance stops at its own tolerance. res, nite and t_done_ms (time
+ * from the batch start to that instance's convergence) receive ninst
+ * entries each; any may be NULL.
+ * cfmg_batch_set_option(b, CFMG_BOPT_HOST_LOOP, 1): the host repeats the
+ * lockstep iteration instead of the `while` node (the same kernels; for
+ * profilers that do not descend into conditional graph nodes). */
+#define CFMG_BOPT_HOST_LOOP 0
 typedef struct cfmg_batch cfmg_batch;
 CFMG_API int cfmg_batch_create(const cfmg_desc* d, int ninst, const int* nx, const int* ny, const int* nlevels,
                                cfmg_batch** out);
@@ -213,6 +220,7 @@ CFMG_API int cfmg_batch_destroy(cfmg_batch* b);
 CFMG_API int cfmg_batch_instance(cfmg_batch* b, int i, cfmg_handle** h);
 CFMG_API int cfmg_batch_solve(cfmg_batch* b, int zero_x, double* res, int* nite, double* t_done_ms);
 CFMG_API const char* cfmg_batch_last_error(const cfmg_batch* b);
+CFMG_API int cfmg_batch_set_option(cfmg_batch* b, int option, long long value);
 
 /* Instrumentation (no counterpart in the reference, which has none).
  * cfmg_launch_count: kernels this handle has launched so far; a replay of a
