@@ -50,6 +50,7 @@ struct cfmg_handle {
   int pool_cap = 0, pool_used = 0;
   std::unordered_map<std::string, int> prog_cache;
   bool tb_on = true;  // temporally blocked FP32 smoothing on fine levels
+  int tb_version = 3;  // 3: packed FP32x2 passes, 1: scalar passes
   int coarsest_fp64 = -1;  // mixed form: -1 FP64 when the coarsest level is small, 0 never, 1 always
   // adjoint scratch (level-1 FP64 arrays, allocated on the first cfmg_adjoint)
   double *adj_x = nullptr, *adj_b = nullptr, *adj_gk = nullptr;
@@ -389,7 +390,8 @@ int smooth_tb(cfmg_handle* h, int lev, int nite) {
     }
     {
       Launch k(h, CFMG_K_SWEEP, lev, CFMG_MIXED);
-      launch_smooth_tb(stencil, n, v.x, v.y, v.b, v.widiag, (float)(1.0 - h->d.omega), l.tx, l.ty, l.tz, l.nh,
+      launch_smooth_tb(h->tb_version, stencil, n, v.x, v.y, v.b, v.widiag, (float)(1.0 - h->d.omega), l.tx, l.ty,
+                       l.tz, l.nh,
                        l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, h->stream);
     }
     l.xswap ^= 1;
@@ -921,8 +923,11 @@ int fused_residual(cfmg_handle* h) {
     {
       // the F-cycle restricts level 1's r first: it must hold the right-hand side too
       Launch k(h, CFMG_K_RESIDUAL, 1, CFMG_FP64, 2);
-      launch_resid_int(kind, l1.x, l1.b, h->dq, g, bx, lo, n, h->dscal, l1.b32,
-                       h->d.cycle == CFMG_CYCLE_F ? l1.r32 : nullptr, neumann, h->partials, h->stream);
+      float* r32 = h->d.cycle == CFMG_CYCLE_F ? l1.r32 : nullptr;
+      if (!launch_resid_int2d(kind, l1.x, l1.b, h->dq, g, bx, h->dscal, l1.b32, r32, neumann, h->partials,
+                              h->stream))
+        launch_resid_int(kind, l1.x, l1.b, h->dq, g, bx, lo, n, h->dscal, l1.b32, r32, neumann, h->partials,
+                         h->stream);
       launch_fused_final(h->partials, h->dscal, h->dscal + S_NORMB, neumann ? h->dscal + S_NWET : nullptr,
                          h->d.norm_kind, h->stream);
     }
@@ -2124,7 +2129,9 @@ int cfmg_set_option(cfmg_handle* h, int option, long long value) {
     return CFMG_OK;
   }
   if (option == CFMG_OPT_TEMPORAL_BLOCKING) {
+    if (value < 0 || value > 3 || value == 2) return fail(h, CFMG_ERR_ARG, "temporal_blocking must be 0, 1 or 3");
     h->tb_on = value != 0;
+    if (value) h->tb_version = (int)value;
     drop_graphs(h);
     return CFMG_OK;
   }

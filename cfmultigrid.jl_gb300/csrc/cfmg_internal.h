@@ -169,8 +169,9 @@ void launch_program(const Op* prog, int nops, double* red, cudaStream_t s);  // 
 // 128 x 72 tile: 3 pairs suit large levels, longer passes cut the launches
 // of the many-pair coarsest solves.
 constexpr int kTbMaxPairs = 10;
-bool launch_smooth_tb(int stencil, int nite, const float* x, float* xo, const float* b, const float* w, float cff,
-                      int tx, int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s);
+// version 3: two columns per thread in packed FP32x2 arithmetic; 1: one column per thread
+bool launch_smooth_tb(int version, int stencil, int nite, const float* x, float* xo, const float* b, const float* w,
+                      float cff, int tx, int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s);
 
 // ---- batched solver (k_batch.cu): independent 2D instances advance in
 // lockstep, one launch per step of the iteration for all of them. Every
@@ -246,6 +247,9 @@ void launch_update_scaled(double* x, const float* e, const double* iscale, long 
 void launch_resid_int(int kind, const double* x, const double* b, const int8_t* dq, const Geom& g, const Box& bx,
                       long long lo, long long n, const double* ds, float* b32, float* r32, bool neumann,
                       double* partials, cudaStream_t s);
+// 2D single-layer form (each x converted once); false: use launch_resid_int
+bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t* dq, const Geom& g, const Box& bx,
+                        const double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s);
 void launch_rhs32_shift(const uint8_t* m, const double* mean_scale, float* b32, float* r32, long long n,
                         cudaStream_t s);
 void launch_make_dq(const double* diag, const uint8_t* m, double Q, int8_t* dq, long long n, int* ok, cudaStream_t s);

@@ -267,6 +267,154 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int(const double* __restri
   }
 }
 
+// 2D levels (one layer): the same residual with every x converted once.
+// A warp owns a strip of 32 consecutive linear indices of a row and walks
+// down RH rows, keeping the converted rows j-1, j, j+1 in registers; the
+// west and east neighbours come from the adjacent lanes (lane 0 and lane
+// 31 convert the one value beyond the strip, x[I-1] and x[I+32], which is
+// also what the linear 5-point range needs at the ends of a row). The
+// residual norm is summed from the FP32 right-hand-side values f = r*scale
+// (exact squares via FMA, double-float accumulation per thread, FP64
+// across threads), so the FP64 pipe does one conversion a cell.
+constexpr int kIntRows = 32;  // rows per warp task
+
+struct StripSpace {
+  long long len;   // array length
+  long long row0;  // linear index of column 0 of the first row
+  int c0, ncols;   // columns of the index space: c0 .. c0+ncols-1 (0-based linear offsets in a row)
+  int nrows;       // rows of the index space
+  int nstrips;     // ceil(ncols / 32)
+  long long n1;
+};
+
+template <int KIND, bool NEUMANN>
+__global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __restrict__ x, const double* __restrict__ b,
+                                                            const int8_t* __restrict__ dq, StripSpace sp,
+                                                            const double* __restrict__ ds, float* __restrict__ b32,
+                                                            float* __restrict__ r32, double* __restrict__ partials) {
+  constexpr int q = (KIND == OPK_RESID9) ? 2 : 0;  // Q = 2^q
+  const int k = fix_exponent(ds);
+  const double scale = ds[S_NEXT];
+  const float fm = (float)ldexp(scale, -(k + q));  // power of two: R -> r * scale
+  const int lane = threadIdx.x & 31;
+  const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const int nchunks = (sp.nrows + kIntRows - 1) / kIntRows;
+  const long long ntasks = (long long)sp.nstrips * nchunks;
+  float hi = 0.f, lo = 0.f;  // double-float sum of f^2
+  __int128 s1 = 0;
+  for (long long task = warp0; task < ntasks; task += nwarps) {
+    const int strip = (int)(task % sp.nstrips);
+    const int chunk = (int)(task / sp.nstrips);
+    const int c = sp.c0 + strip * 32 + lane;  // this lane's column
+    const bool col_ok = c < sp.c0 + sp.ncols;
+    const int ra = chunk * kIntRows, rb = min(ra + kIntRows, sp.nrows);
+    // rows ra-1 and ra
+    long long I = sp.row0 + (long long)ra * sp.n1 + c;
+    // loads are clamped to the array: lanes past the index space and the
+    // rows above the first / below the last output row may reach past its
+    // ends, where the values are never used
+    auto at = [&](long long J) { return x[J < 0 ? 0 : (J >= sp.len ? sp.len - 1 : J)]; };
+    auto load_row = [&](long long Ir, long long& W, long long& C, long long& E) {
+      C = to_fix(at(Ir), k);
+      const long long xe = (lane == 0) ? to_fix(at(Ir - 1), k) : ((lane == 31) ? to_fix(at(Ir + 1), k) : 0);
+      W = __shfl_up_sync(0xffffffffu, C, 1);
+      E = __shfl_down_sync(0xffffffffu, C, 1);
+      if (lane == 0) W = xe;
+      if (lane == 31) E = xe;
+    };
+    long long Wm, Cm, Em, W0, C0, E0, Wp, Cp, Ep;
+    load_row(I - sp.n1, Wm, Cm, Em);
+    load_row(I, W0, C0, E0);
+    for (int r = ra; r < rb; ++r, I += sp.n1) {
+      load_row(I + sp.n1, Wp, Cp, Ep);
+      if (col_ok) {
+        const int d = dq[I];
+        long long R = 0;
+        if (d >= 0) {
+          const long long B = to_fix(b[I], k);
+          if (KIND == OPK_RESID9)
+            R = (long long)d * C0 + 4 * B - 2 * (((W0 + E0) + Cm) + Cp) - (((Wm + Em) + Wp) + Ep);
+          else
+            R = (long long)d * C0 + B - (((W0 + E0) + Cm) + Cp);
+        }
+        const float f = __ll2float_rn(R) * fm;
+        b32[I] = f;
+        if (NEUMANN) s1 += (__int128)R;
+        else if (r32) r32[I] = f;
+        const float p = f * f, e = __fmaf_rn(f, f, -p);  // p + e = f^2 exactly
+        const float sn = hi + p, bp = sn - hi;
+        lo += ((hi - (sn - bp)) + (p - bp)) + e;
+        hi = sn;
+      }
+      Wm = W0; Cm = C0; Em = E0;
+      W0 = Wp; C0 = Cp; E0 = Ep;
+    }
+  }
+  // sum f^2 -> sum r^2 = sum f^2 / scale^2 (exact power of two)
+  const double s2d = ((double)hi + (double)lo) / (scale * scale);
+  const double s1d = NEUMANN ? ldexp(__dadd_rn(__dmul_rn((double)(long long)(s1 >> 64), 18446744073709551616.0),
+                                               (double)(unsigned long long)s1),
+                                     -(k + q))
+                             : 0.0;
+  __shared__ double sh2[kMxThreads / 32], sh1[kMxThreads / 32];
+  double a2 = s2d, a1 = s1d;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a2 += __shfl_down_sync(0xffffffffu, a2, o);
+    a1 += __shfl_down_sync(0xffffffffu, a1, o);
+  }
+  if (lane == 0) {
+    sh2[threadIdx.x >> 5] = a2;
+    sh1[threadIdx.x >> 5] = a1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double u = 0.0, v = 0.0;
+    for (int w = 0; w < kMxThreads / 32; ++w) {
+      u += sh2[w];
+      v += sh1[w];
+    }
+    partials[blockIdx.x] = u;
+    partials[kMxParts + blockIdx.x] = v;
+  }
+}
+
+bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t* dq, const Geom& g, const Box& bx,
+                        const double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s) {
+  if (g.tz != 1) return false;
+  StripSpace sp;
+  sp.n1 = g.n1;
+  sp.len = g.len;
+  if (kind == OPK_RESID5) {  // linear range 1+n1 .. len-n1: rows 2..ty-1, every column
+    sp.row0 = g.n1;
+    sp.c0 = 0;
+    sp.ncols = g.tx;
+    sp.nrows = g.ty - 2;
+  } else if (kind == OPK_RESID9) {  // interior box of the single layer
+    sp.row0 = (long long)(bx.j0 - 1) * g.n1;
+    sp.c0 = bx.i0 - 1;
+    sp.ncols = bx.i1 - bx.i0 + 1;
+    sp.nrows = bx.j1 - bx.j0 + 1;
+  } else {
+    return false;
+  }
+  if (sp.nrows <= 0 || sp.ncols <= 0) return false;
+  sp.nstrips = (sp.ncols + 31) / 32;
+#define CFMG_INT2(K)                                                                                        \
+  if (kind == K) {                                                                                          \
+    if (neumann)                                                                                            \
+      k_resid_int2d<K, true><<<kMxParts, kMxThreads, 0, s>>>(x, b, dq, sp, ds, b32, r32, partials);          \
+    else                                                                                                    \
+      k_resid_int2d<K, false><<<kMxParts, kMxThreads, 0, s>>>(x, b, dq, sp, ds, b32, r32, partials);         \
+    return true;                                                                                            \
+  }
+  CFMG_INT2(OPK_RESID5)
+  CFMG_INT2(OPK_RESID9)
+#undef CFMG_INT2
+  return false;
+}
+
 // cell-centred second pass: b32 = r32 = msk ? b32 - mean * scale : 0 with
 // ms[0] = S_MEAN2 and ms[1] = S_CUR
 __global__ void k_rhs32_shift(const uint8_t* __restrict__ m, const double* __restrict__ ms, float* __restrict__ b32,
@@ -319,22 +467,31 @@ __global__ void k_maxabs2(const double* __restrict__ x, const double* __restrict
 }
 
 // x += e * iscale, with max |x| of the result into ds[S_MAXX] (reset by the
-// fused pass's final reduction)
-__global__ void k_update_scaled_max(double* __restrict__ x, const float* __restrict__ e, const double* __restrict__ ds,
-                                    long long n, double* dsw) {
-  long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+// fused pass's final reduction): a fixed grid of kMxParts blocks, one
+// atomic per block
+__global__ void __launch_bounds__(kMxThreads) k_update_scaled_max(double* __restrict__ x, const float* __restrict__ e,
+                                                                  const double* __restrict__ ds, long long n,
+                                                                  double* dsw) {
+  const double is = ds[S_ICUR];
   unsigned long long mx = 0;
-  if (I < n) {
-    const double v = __fma_rn((double)e[I], ds[S_ICUR], x[I]);
+  for (long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x; I < n; I += (long long)gridDim.x * blockDim.x) {
+    const double v = __fma_rn((double)e[I], is, x[I]);
     x[I] = v;
-    mx = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFULL;
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFULL;
+    mx = u > mx ? u : mx;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long ox = __shfl_down_sync(0xffffffffu, mx, o);
     mx = ox > mx ? ox : mx;
   }
-  if ((threadIdx.x & 31) == 0 && mx) atomicMax((unsigned long long*)(dsw + S_MAXX), mx);
+  __shared__ unsigned long long sh[kMxThreads / 32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < kMxThreads / 32; ++w) mx = sh[w] > mx ? sh[w] : mx;
+    if (mx) atomicMax((unsigned long long*)(dsw + S_MAXX), mx);
+  }
 }
 
 void launch_resid_int(int kind, const double* x, const double* b, const int8_t* dq, const Geom& g, const Box& bx,
@@ -369,7 +526,7 @@ void launch_maxabs2(const double* x, const double* b, long long n, double* ds, c
 }
 
 void launch_update_scaled_max(double* x, const float* e, double* ds, long long n, cudaStream_t s) {
-  k_update_scaled_max<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, e, ds, n, ds);
+  k_update_scaled_max<<<kMxParts, kMxThreads, 0, s>>>(x, e, ds, n, ds);
 }
 
 void launch_resid_fused(int kind, double* r, const double* x, const double* b, const double* d, const uint8_t* m,

@@ -152,6 +152,133 @@ __device__ __forceinline__ void tb_tile(const float* __restrict__ x, float* __re
   }
 }
 
+// ---------------------------------------------------------------------
+// Packed form: the same passes with two columns per thread and the FP32x2
+// instructions of sm_100+ (__fadd2_rn / __fmul2_rn / __ffma2_rn round each
+// lane exactly as the scalar _rn operations do, so the result is the same
+// bit for bit). A 128 x 64 tile lives in shared memory as two planes per
+// row, even columns then odd columns, so that every shared load of a warp
+// reads 32 consecutive words. b and -omega*idiag of the thread's own 4 x 2
+// cells stay in registers. Every sweep computes the whole tile (cells near
+// the tile edge read clamped neighbours and hold values that no later sweep
+// of the valid region reads); cells outside U keep their value.
+constexpr int kT3W = 128, kT3H = 64;  // tile
+constexpr int kT3Tx = 64, kT3Ty = 16, kT3Rows = 4;
+constexpr int kT3Half = kT3W / 2;
+
+template <int ST, int NITE>
+__device__ __forceinline__ void tb3_tile(const float* __restrict__ x, float* __restrict__ xo,
+                                         const float* __restrict__ b, const float* __restrict__ w, float cff, int tx,
+                                         int ty, int ui0, int ui1, int uj0, int uj1, int bx, int by, int bz,
+                                         float* smem) {
+  constexpr int H = 2 * NITE;
+  constexpr int CW = kT3W - 2 * H, CH = kT3H - 2 * H;
+  float* P0 = smem;              // [kT3H][even | odd]
+  float* P1 = smem + kT3H * kT3W;
+  const int lx = threadIdx.x;
+  const int r0 = threadIdx.y * kT3Rows;
+  const int gi0 = ui0 + bx * CW - H + 2 * lx;  // 1-based global column of the even cell
+  const int gj0 = uj0 + by * CH - H + r0;
+  const long long plane = (long long)tx * ty * bz;
+  float2 B[kT3Rows], NW[kT3Rows];
+  unsigned inU = 0;  // bit 2r + e
+#pragma unroll
+  for (int r = 0; r < kT3Rows; ++r) {
+    const int gj = gj0 + r;
+    float v[2], bb[2], ww[2];
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int gi = gi0 + e;
+      const bool in = gi >= 1 && gi <= tx && gj >= 1 && gj <= ty;
+      const long long I = plane + (long long)(gi - 1) + (long long)tx * (gj - 1);
+      v[e] = in ? x[I] : 0.f;
+      bb[e] = in ? b[I] : 0.f;
+      ww[e] = in ? w[I] : 0.f;
+      if (gi >= ui0 && gi <= ui1 && gj >= uj0 && gj <= uj1) inU |= 1u << (2 * r + e);
+    }
+    P0[(r0 + r) * kT3W + lx] = v[0];
+    P0[(r0 + r) * kT3W + kT3Half + lx] = v[1];
+    B[r] = make_float2(bb[0], bb[1]);
+    NW[r] = make_float2(-ww[0], -ww[1]);
+  }
+  __syncthreads();
+  const int ti0 = ui0 + bx * CW - H, tj0 = uj0 + by * CH - H;  // tile origin
+  const bool tile_in_u = ti0 >= ui0 && ti0 + kT3W - 1 <= ui1 && tj0 >= uj0 && tj0 + kT3H - 1 <= uj1;
+  const float2 cff2 = make_float2(cff, cff);
+  const int lw = lx > 0 ? lx - 1 : 0, le = lx < kT3Half - 1 ? lx + 1 : kT3Half - 1;
+#pragma unroll 1
+  for (int s = 0; s < 2 * NITE; ++s) {
+    const float* src = (s & 1) ? P1 : P0;
+    float* dst = (s & 1) ? P0 : P1;
+    // (west, even, odd, east) of a row; rows outside the tile are clamped
+    auto ld = [&](int rr, float& wv, float& av, float& bv, float& ev) {
+      rr = rr < 0 ? 0 : (rr >= kT3H ? kT3H - 1 : rr);
+      const float* row = src + rr * kT3W;
+      av = row[lx];
+      bv = row[kT3Half + lx];
+      wv = row[kT3Half + lw];
+      ev = row[le];
+    };
+    float wm, am, bm, em, w0, a0, b0, e0;
+    ld(r0 - 1, wm, am, bm, em);
+    ld(r0, w0, a0, b0, e0);
+#pragma unroll
+    for (int r = 0; r < kT3Rows; ++r) {
+      float wp, ap, bp, ep;
+      ld(r0 + r + 1, wp, ap, bp, ep);
+      // faces ((W + E) + S) + N, S = row j-1
+      float2 f = __fadd2_rn(make_float2(w0, a0), make_float2(b0, e0));
+      f = __fadd2_rn(f, make_float2(am, bm));
+      f = __fadd2_rn(f, make_float2(ap, bp));
+      float2 t;
+      if (ST == 5) {
+        t = __fadd2_rn(B[r], make_float2(-f.x, -f.y));  // b - s4
+      } else {
+        // diagonals in the order (i-1,j-1), (i+1,j-1), (i-1,j+1), (i+1,j+1)
+        float2 d = __fadd2_rn(make_float2(wm, am), make_float2(bm, em));
+        d = __fadd2_rn(d, make_float2(wp, ap));
+        d = __fadd2_rn(d, make_float2(bp, ep));
+        t = __ffma2_rn(f, make_float2(-0.5f, -0.5f), B[r]);
+        t = __ffma2_rn(d, make_float2(-0.25f, -0.25f), t);
+      }
+      float2 o = __fadd2_rn(__fmul2_rn(cff2, make_float2(a0, b0)), __fmul2_rn(NW[r], t));
+      if (!tile_in_u) {
+        if (!(inU >> (2 * r) & 1u)) o.x = a0;
+        if (!(inU >> (2 * r + 1) & 1u)) o.y = b0;
+      }
+      dst[(r0 + r) * kT3W + lx] = o.x;
+      dst[(r0 + r) * kT3W + kT3Half + lx] = o.y;
+      wm = w0; am = a0; bm = b0; em = e0;
+      w0 = wp; a0 = ap; b0 = bp; e0 = ep;
+    }
+    __syncthreads();
+  }
+  // 2*NITE sweeps: the result is in P0; write the core cells of U
+#pragma unroll
+  for (int r = 0; r < kT3Rows; ++r) {
+    const int lj = r0 + r;
+    if (lj < H || lj >= kT3H - H) continue;
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int lc = 2 * lx + e;
+      if (lc >= H && lc < kT3W - H && (inU >> (2 * r + e) & 1u)) {
+        const long long I = plane + (long long)(gi0 + e - 1) + (long long)tx * (gj0 + r - 1);
+        xo[I] = P0[lj * kT3W + e * kT3Half + lx];
+      }
+    }
+  }
+}
+
+template <int ST, int NITE>
+__global__ void __launch_bounds__(kT3Tx * kT3Ty, 1) k_smooth_tb3(const float* __restrict__ x, float* __restrict__ xo,
+                                                                 const float* __restrict__ b,
+                                                                 const float* __restrict__ w, float cff, int tx,
+                                                                 int ty, int ui0, int ui1, int uj0, int uj1) {
+  extern __shared__ float smem[];
+  tb3_tile<ST, NITE>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1, (int)blockIdx.x, (int)blockIdx.y,
+                     (int)blockIdx.z, smem);
+}
+
 template <int ST, int NITE>
 __global__ void __launch_bounds__(kTbW * kTbTy, 1) k_smooth_tb(const float* __restrict__ x, float* __restrict__ xo,
                                                                const float* __restrict__ b,
@@ -213,8 +340,27 @@ __global__ void __launch_bounds__(kTbW * kTbTy, 1) k_btb(const Op* __restrict__ 
 }
 
 template <int ST, int NITE>
-static void launch_tb_n(const float* x, float* xo, const float* b, const float* w, float cff, int tx, int ty, int nz,
-                        int ui0, int ui1, int uj0, int uj1, cudaStream_t s) {
+static void launch_tb3_n(const float* x, float* xo, const float* b, const float* w, float cff, int tx, int ty,
+                         int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s) {
+  constexpr int H = 2 * NITE;
+  constexpr int CW = kT3W - 2 * H, CH = kT3H - 2 * H;
+  const size_t smem = 2 * (size_t)kT3H * kT3W * sizeof(float);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_smooth_tb3<ST, NITE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  dim3 grid((unsigned)((ui1 - ui0 + CW) / CW), (unsigned)((uj1 - uj0 + CH) / CH), (unsigned)nz);
+  k_smooth_tb3<ST, NITE><<<grid, dim3(kT3Tx, kT3Ty, 1), smem, s>>>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1);
+}
+
+template <int ST, int NITE>
+static void launch_tb_n(int version, const float* x, float* xo, const float* b, const float* w, float cff, int tx,
+                        int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s) {
+  if (version == 3) {
+    launch_tb3_n<ST, NITE>(x, xo, b, w, cff, tx, ty, nz, ui0, ui1, uj0, uj1, s);
+    return;
+  }
   constexpr int H = 2 * NITE;
   constexpr int CW = kTbW - 2 * H, CH = kTbH - 2 * H;
   const size_t smem = 4 * (size_t)kTbH * kTbW * sizeof(float);
@@ -229,11 +375,11 @@ static void launch_tb_n(const float* x, float* xo, const float* b, const float* 
 
 // nite pairs of sweeps in one pass (nite in 1..kTbMaxPairs); returns false when the
 // caller must fall back to single sweeps.
-bool launch_smooth_tb(int stencil, int nite, const float* x, float* xo, const float* b, const float* w, float cff,
-                      int tx, int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s) {
+bool launch_smooth_tb(int version, int stencil, int nite, const float* x, float* xo, const float* b, const float* w,
+                      float cff, int tx, int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s) {
 #define CFMG_TB(ST, N)                                                                       \
   if (stencil == ST && nite == N) {                                                          \
-    launch_tb_n<ST, N>(x, xo, b, w, cff, tx, ty, nz, ui0, ui1, uj0, uj1, s);                 \
+    launch_tb_n<ST, N>(version, x, xo, b, w, cff, tx, ty, nz, ui0, ui1, uj0, uj1, s);        \
     return true;                                                                             \
   }
   CFMG_TB(5, 1) CFMG_TB(5, 2) CFMG_TB(5, 3) CFMG_TB(5, 4) CFMG_TB(5, 5)
