@@ -237,8 +237,11 @@ class Gmg:
         self._check(self._L.cfmg_synchronize(self._h))
 
     def set_option(self, name: str, value: int) -> None:
-        """Tuning knobs (``engine_cells``: levels of at most this many cells
-        run in the coarse-level program engine; 0 turns it off)."""
+        """Tuning knobs: ``engine_cells`` (levels of at most this many cells
+        run in the coarse-level program engine; 0 turns it off),
+        ``temporal_blocking`` (3 packed passes, 1 scalar passes, 0 off),
+        ``coarsest_fp64`` (-1 auto, 0, 1), ``int_residual`` (1 fixed-point
+        level-1 residual of the mixed loop, 0 FP64 arithmetic)."""
         self._check(self._L.cfmg_set_option(self._h, _lib.OPTIONS[name], int(value)))
 
     def set_stream(self, stream_ptr: Optional[int]):

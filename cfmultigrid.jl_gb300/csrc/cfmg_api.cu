@@ -98,6 +98,10 @@ struct cfmg_batch {
   int4* stab = nullptr;        // their chunk (or tile) tables {Op, chunk, instance, 0} (device)
   BSmall* ssm = nullptr;       // small-level smoothing descriptors (device)
   bool host_loop = false;      // CFMG_BOPT_HOST_LOOP
+  bool int_all = false;        // every instance has the integer residual form
+  int4* ttab = nullptr;        // its warp tasks {instance, strip, row chunk, 0}
+  long long* tstart = nullptr; // first task of each instance (ninst + 1)
+  long long ntasks = 0;
   int kind = 0;
   bool neumann = false;
   struct Step {
@@ -1783,9 +1787,15 @@ int record_vstep(cfmg_handle* h, const VStep& v, std::vector<Op>& out) {
 // One lockstep iteration of every active instance (see k_batch.cu).
 int lockstep_body(cfmg_batch* b) {
   const int ninst = (int)b->inst.size();
-  launch_bres(b->kind, b->neumann, b->bi, b->l1tab, b->l1chunks, b->active, b->bpart, b->stream);
-  launch_bfinal(b->bi, b->l1start, ninst, b->bpart, b->active, b->nactive, b->stream);
-  if (b->neumann) launch_brhs(b->bi, b->l1tab, b->l1chunks, b->active, b->stream);
+  if (b->int_all) {
+    launch_bres_int(b->kind, b->neumann, b->bi, b->ttab, b->ntasks, b->active, b->bpart, b->stream);
+    launch_bfinal(b->bi, b->tstart, ninst, b->bpart, b->active, b->nactive, b->stream);
+    if (b->neumann) launch_brhs_shift(b->bi, b->l1tab, b->l1chunks, b->active, b->stream);
+  } else {
+    launch_bres(b->kind, b->neumann, b->bi, b->l1tab, b->l1chunks, b->active, b->bpart, b->stream);
+    launch_bfinal(b->bi, b->l1start, ninst, b->bpart, b->active, b->nactive, b->stream);
+    if (b->neumann) launch_brhs(b->bi, b->l1tab, b->l1chunks, b->active, b->stream);
+  }
   for (const cfmg_batch::Step& st : b->steps) {
     if (st.tb == 2) {
       launch_bsmall(b->ssm + st.tab0, (int)st.nchunks, st.smem, b->active, b->stream);
@@ -1919,6 +1929,19 @@ int lockstep_build(cfmg_batch* b) {
       B.n = box_count(B.box);
     }
     B.len = (long long)l.len;
+    B.dq = h->dq;
+    if (B.kind == OPK_RESID5) {  // linear range: rows 2..ty-1, every column
+      B.row0 = B.g.n1;
+      B.c0 = 0;
+      B.ncols = l.tx;
+      B.nrows = l.ty - 2;
+    } else {
+      B.row0 = (long long)(B.box.j0 - 1) * B.g.n1;
+      B.c0 = B.box.i0 - 1;
+      B.ncols = B.box.i1 - B.box.i0 + 1;
+      B.nrows = B.box.j1 - B.box.j0 + 1;
+    }
+    B.nstrips = (B.ncols + 31) / 32;
     B.neumann = !vertices(h);
     B.norm_kind = h->d.norm_kind;
     B.maxite = h->d.maxite;
@@ -1926,6 +1949,28 @@ int lockstep_build(cfmg_batch* b) {
     l1[i + 1] = l1[i] + (B.len + kBChunk - 1) / kBChunk;
   }
   b->l1chunks = l1[ninst];
+  // integer residual tasks (single-layer levels whose instances all have it)
+  b->int_all = true;
+  for (int i = 0; i < ninst; ++i) {
+    const cfmg_handle* h = b->inst[i];
+    b->int_all = b->int_all && int_path(h) && h->lv[0].tz == 1 && hb[i].nrows > 0 && hb[i].ncols > 0;
+  }
+  std::vector<int4> tt;
+  std::vector<long long> ts(ninst + 1, 0);
+  if (b->int_all) {
+    for (int i = 0; i < ninst; ++i) {
+      ts[i] = (long long)tt.size();
+      const int nch = (hb[i].nrows + kBIntRows - 1) / kBIntRows;
+      for (int ch = 0; ch < nch; ++ch)
+        for (int st = 0; st < hb[i].nstrips; ++st) tt.push_back(make_int4(i, st, ch, 0));
+    }
+    ts[ninst] = (long long)tt.size();
+    b->ntasks = ts[ninst];
+    BCUDA(b, cudaMalloc((void**)&b->ttab, sizeof(int4) * tt.size()));
+    BCUDA(b, cudaMemcpy(b->ttab, tt.data(), sizeof(int4) * tt.size(), cudaMemcpyHostToDevice));
+    BCUDA(b, cudaMalloc((void**)&b->tstart, sizeof(long long) * ts.size()));
+    BCUDA(b, cudaMemcpy(b->tstart, ts.data(), sizeof(long long) * ts.size(), cudaMemcpyHostToDevice));
+  }
   std::vector<int4> l1t((size_t)b->l1chunks);
   for (int i = 0; i < ninst; ++i)
     for (long long c = l1[i]; c < l1[i + 1]; ++c) l1t[c] = make_int4(i, (int)(c - l1[i]), i, 0);
@@ -1935,7 +1980,7 @@ int lockstep_build(cfmg_batch* b) {
   BCUDA(b, cudaMemcpy(b->bi, hb.data(), sizeof(BInst) * ninst, cudaMemcpyHostToDevice));
   BCUDA(b, cudaMalloc((void**)&b->l1start, sizeof(long long) * (ninst + 1)));
   BCUDA(b, cudaMemcpy(b->l1start, l1.data(), sizeof(long long) * (ninst + 1), cudaMemcpyHostToDevice));
-  BCUDA(b, cudaMalloc((void**)&b->bpart, sizeof(double) * 2 * (size_t)b->l1chunks));
+  BCUDA(b, cudaMalloc((void**)&b->bpart, sizeof(double) * 2 * (size_t)std::max(b->l1chunks, b->ntasks)));
   BCUDA(b, cudaMalloc((void**)&b->active, sizeof(int) * ninst));
   BCUDA(b, cudaMalloc((void**)&b->nactive, sizeof(int)));
   BCUDA(b, cudaMemset(b->active, 0, sizeof(int) * ninst));
@@ -2039,7 +2084,8 @@ int cfmg_batch_destroy(cfmg_batch* b) {
   for (cfmg_handle* h : b->inst) cfmg_destroy(h);
   for (void* p : {(void*)b->progs, (void*)b->ptrs, (void*)b->nops, (void*)b->counter, (void*)b->red, (void*)b->sc,
                   (void*)b->nwet, (void*)b->bi, (void*)b->l1start, (void*)b->l1tab, (void*)b->bpart,
-                  (void*)b->active, (void*)b->nactive, (void*)b->sops, (void*)b->stab, (void*)b->ssm})
+                  (void*)b->active, (void*)b->nactive, (void*)b->sops, (void*)b->stab, (void*)b->ssm,
+                  (void*)b->ttab, (void*)b->tstart})
     if (p) cudaFree(p);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
@@ -2076,7 +2122,7 @@ int cfmg_batch_solve(cfmg_batch* b, int zero_x, double* res, int* nite, double* 
     for (void** p : {(void**)&b->progs, (void**)&b->ptrs, (void**)&b->nops, (void**)&b->counter, (void**)&b->red,
                      (void**)&b->sc, (void**)&b->nwet, (void**)&b->bi, (void**)&b->l1start, (void**)&b->l1tab,
                      (void**)&b->bpart, (void**)&b->active, (void**)&b->nactive, (void**)&b->sops,
-                     (void**)&b->stab, (void**)&b->ssm})
+                     (void**)&b->stab, (void**)&b->ssm, (void**)&b->ttab, (void**)&b->tstart})
       if (*p) {
         cudaFree(*p);
         *p = nullptr;

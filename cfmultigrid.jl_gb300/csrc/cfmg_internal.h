@@ -181,7 +181,7 @@ constexpr int kBChunk = 1024;
 constexpr int kBThreads = 256;
 // per-instance scalar block (double): see k_bfinal for their use
 enum BSlot { BS_NORMB = 0, BS_RES, BS_NITE, BS_NWET, BS_NEXT, BS_CUR, BS_ICUR, BS_MEAN, BS_T0, BS_T1, BS_ZEROX,
-             BS_HIST };
+             BS_MAXX, BS_MAXB, BS_HIST };
 // level-1 state of one instance for the FP64 steps of its solve loop
 struct BInst {
   double *x, *b, *r, *d;
@@ -195,6 +195,11 @@ struct BInst {
   long long len;
   int kind, neumann, norm_kind, maxite;
   double tol;
+  // integer form of the residual (when every instance has it): Q*diag, and
+  // the index space as row strips (see k_resid_int2d)
+  const int8_t* dq;
+  long long row0;
+  int c0, ncols, nrows, nstrips;
 };
 // Smoothing of a small level (the coarsest solve, or a coarse level's
 // pre/post smoothing) of one instance by one block in shared memory: x, b,
@@ -226,6 +231,11 @@ void launch_bres(int kind, bool neumann, const BInst* bi, const int4* tab, long 
                  double* partials, cudaStream_t s);
 void launch_bfinal(const BInst* bi, const long long* cstart, int ninst, const double* partials, int* active,
                    int* nactive, cudaStream_t s);
+// integer residual: warp tasks {instance, strip, row chunk, 0}, partials 2 per task
+constexpr int kBIntRows = 32;
+void launch_bres_int(int kind, bool neumann, const BInst* bi, const int4* ttab, long long ntasks, const int* active,
+                     double* partials, cudaStream_t s);
+void launch_brhs_shift(const BInst* bi, const int4* tab, long long nchunks, const int* active, cudaStream_t s);
 void launch_brhs(const BInst* bi, const int4* tab, long long nchunks, const int* active, cudaStream_t s);
 void launch_bupdate(const BInst* bi, const int4* tab, long long nchunks, const int* active, cudaStream_t s);
 void launch_bcond(cudaGraphConditionalHandle hc, int* nactive, cudaStream_t s);

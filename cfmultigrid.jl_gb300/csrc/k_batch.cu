@@ -17,6 +17,8 @@
 // Arithmetic per cell is the single-instance code (ops_dev.cuh); the
 // reductions use a fixed chunk-to-thread assignment and fixed-order block
 // sums, so a batch's results do not depend on the launch shape.
+#include <algorithm>
+
 #include "exec_dev.cuh"
 
 namespace cfmg {
@@ -69,6 +71,19 @@ __device__ __forceinline__ double bsum(double v, double* sh) {
   return t;
 }
 
+// block maximum (kBThreads threads); valid in thread 0
+__device__ __forceinline__ double bmax(double v, double* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kBThreads / 32; ++w) t = fmax(t, sh[w]);
+  return t;
+}
+
 // ------------------------------------------------------------ cycle steps
 // Generic step: the active chunks of a list of Ops (tab[c] = {op, chunk of
 // the op, instance}), each executed with the per-item code of the program
@@ -109,15 +124,21 @@ __global__ void __launch_bounds__(kBThreads) k_binit(const BInst* __restrict__ b
   const BInst& B = bi[blockIdx.x];
   double* sc = B.sc;
   const bool zx = zero_x != 0;
-  double v = 0.0;
+  double v = 0.0, mx = 0.0, mb = 0.0;
   for (long long t = threadIdx.x; t < B.len; t += kBThreads) {
     if (zx) B.x[t] = 0.0;
     const uint8_t mm = B.m[t];
     const double bb = B.b[t];
     if (mm) v = (mm == 1) ? __fma_rn(bb, bb, v) : __dadd_rn(v, __dmul_rn((double)mm, __dmul_rn(bb, bb)));
+    mx = fmax(mx, fabs(B.x[t]));
+    mb = fmax(mb, fabs(bb));
   }
   double tot = bsum(v, sh);
+  __syncthreads();
+  const double tmx = bmax(mx, sh), tmb = bmax(mb, sh);
   if (threadIdx.x == 0) {
+    sc[BS_MAXX] = tmx;
+    sc[BS_MAXB] = tmb;
     if (B.norm_kind == CFMG_NORM_REF_SQUARED && tot == 0.0) tot = 1.0;
     sc[BS_NORMB] = tot;
     sc[BS_NITE] = 0.0;
@@ -215,6 +236,124 @@ __global__ void __launch_bounds__(kBThreads) k_bres(const BInst* __restrict__ bi
   }
 }
 
+// Integer form of the fused residual (see k_resid_int2d in k_mixed.cu):
+// one warp per task {instance, strip of 32 columns, chunk of kBIntRows
+// rows}; the fixed-point exponent is the instance's own (BS_MAXX from its
+// last update, BS_MAXB from the start of the solve). partials[2 task] =
+// sum r^2 (from the FP32 right-hand-side values), partials[2 task + 1] =
+// sum r (exact per task).
+template <int KIND, bool NEUMANN>
+__global__ void __launch_bounds__(kBThreads) k_bres_int(const BInst* __restrict__ bi, const int4* __restrict__ ttab,
+                                                        long long ntasks, const int* __restrict__ active,
+                                                        double* __restrict__ partials) {
+  constexpr int q = (KIND == OPK_RESID9) ? 2 : 0;
+  const int lane = threadIdx.x & 31;
+  const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long task = warp0; task < ntasks; task += nwarps) {
+    const int4 en = ttab[task];
+    if (!active[en.x]) continue;
+    const BInst& B = bi[en.x];
+    const double mx = fmax(B.sc[BS_MAXX], B.sc[BS_MAXB]);
+    int ex = 0;
+    if (mx > 0 && isfinite(mx)) frexp(mx, &ex);
+    const int k = 58 - ex;
+    const double scale = B.sc[BS_NEXT];
+    const float fm = (float)ldexp(scale, -(k + q));
+    const long long n1 = B.g.n1, len = B.len;
+    const double* __restrict__ x = B.x;
+    const int c = B.c0 + en.y * 32 + lane;
+    const bool col_ok = c < B.c0 + B.ncols;
+    const int ra = en.z * kBIntRows, rb = min(ra + kBIntRows, B.nrows);
+    auto at = [&](long long J) { return x[J < 0 ? 0 : (J >= len ? len - 1 : J)]; };
+    auto load_row = [&](long long Ir, long long& W, long long& C, long long& E) {
+      C = to_fix(at(Ir), k);
+      const long long xe = (lane == 0) ? to_fix(at(Ir - 1), k) : ((lane == 31) ? to_fix(at(Ir + 1), k) : 0);
+      W = __shfl_up_sync(0xffffffffu, C, 1);
+      E = __shfl_down_sync(0xffffffffu, C, 1);
+      if (lane == 0) W = xe;
+      if (lane == 31) E = xe;
+    };
+    long long I = B.row0 + (long long)ra * n1 + c;
+    long long Wm, Cm, Em, W0, C0, E0, Wp, Cp, Ep;
+    load_row(I - n1, Wm, Cm, Em);
+    load_row(I, W0, C0, E0);
+    float hi = 0.f, lo = 0.f;
+    __int128 s1 = 0;
+    for (int r = ra; r < rb; ++r, I += n1) {
+      load_row(I + n1, Wp, Cp, Ep);
+      if (col_ok) {
+        const int d = B.dq[I];
+        long long R = 0;
+        if (d >= 0) {
+          const long long Bf = to_fix(B.b[I], k);
+          if (KIND == OPK_RESID9)
+            R = (long long)d * C0 + 4 * Bf - 2 * (((W0 + E0) + Cm) + Cp) - (((Wm + Em) + Wp) + Ep);
+          else
+            R = (long long)d * C0 + Bf - (((W0 + E0) + Cm) + Cp);
+        }
+        const float f = __ll2float_rn(R) * fm;
+        B.b32[I] = f;
+        if (NEUMANN) s1 += (__int128)R;
+        else B.r32[I] = f;
+        const float p = f * f, e = __fmaf_rn(f, f, -p);
+        const float sn = hi + p, bp = sn - hi;
+        lo += ((hi - (sn - bp)) + (p - bp)) + e;
+        hi = sn;
+      }
+      Wm = W0; Cm = C0; Em = E0;
+      W0 = Wp; C0 = Cp; E0 = Ep;
+    }
+    double a2 = ((double)hi + (double)lo) / (scale * scale);
+    double a1 = NEUMANN ? ldexp(__dadd_rn(__dmul_rn((double)(long long)(s1 >> 64), 18446744073709551616.0),
+                                          (double)(unsigned long long)s1),
+                                -(k + q))
+                        : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a2 = __dadd_rn(a2, __shfl_down_sync(0xffffffffu, a2, o));
+      a1 = __dadd_rn(a1, __shfl_down_sync(0xffffffffu, a1, o));
+    }
+    if (lane == 0) {
+      partials[2 * task] = a2;
+      partials[2 * task + 1] = a1;
+    }
+  }
+}
+
+// cell-centred, integer form: b32 = r32 = msk ? b32 - mean * CUR : 0
+__global__ void __launch_bounds__(kBThreads) k_brhs_shift(const BInst* __restrict__ bi, const int4* __restrict__ tab,
+                                                          long long nchunks, int win, const int* __restrict__ active) {
+  constexpr int U = kBChunk / kBThreads;
+  __shared__ int list[kBThreads];
+  __shared__ int wsum[kBThreads / 32 + 1];
+  for (long long base = (long long)blockIdx.x * win; base < nchunks; base += (long long)gridDim.x * win) {
+    const int cnt = active_window(tab, base, nchunks, win, active, list, wsum);
+    for (int q = 0; q < cnt; ++q) {
+      const int4 en = tab[base + list[q]];
+      const BInst& B = bi[en.x];
+      const float sh = (float)(B.sc[BS_MEAN] * B.sc[BS_CUR]);
+      const long long t0 = (long long)en.y * kBChunk + threadIdx.x;
+      float f[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const long long t = t0 + (long long)u * kBThreads;
+        f[u] = 0.f;
+        if (t < B.len && B.m[t]) f[u] = __fsub_rn(B.b32[t], sh);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const long long t = t0 + (long long)u * kBThreads;
+        if (t < B.len) {
+          B.b32[t] = f[u];
+          B.r32[t] = f[u];
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // One block per active instance: its chunks' partial sums in a fixed
 // order, then the loop's bookkeeping.
 //   res = sum/normb (reference rule, sum 0 -> 1) or sqrt(sum/normb) (L2);
@@ -261,6 +400,7 @@ __global__ void __launch_bounds__(kBThreads) k_bfinal(const BInst* __restrict__ 
     int e = 0;
     if (rms > 0 && isfinite(rms)) frexp(rms, &e);
     sc[BS_NEXT] = ldexp(1.0, -e);
+    sc[BS_MAXX] = 0.0;  // the next update collects max |x| afresh
     if (res > B.tol && nite < B.maxite) {
       sc[BS_NITE] = (double)(nite + 1);
       atomicAdd(nactive, 1);
@@ -323,11 +463,23 @@ __global__ void __launch_bounds__(kBThreads) k_bupdate(const BInst* __restrict__
         const long long t = t0 + (long long)u * kBThreads;
         if (t < B.len) xn[u] = __fma_rn((double)B.e32[t], is, B.x[t]);
       }
+      unsigned long long mx = 0;
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const long long t = t0 + (long long)u * kBThreads;
-        if (t < B.len) B.x[t] = xn[u];
+        if (t < B.len) {
+          B.x[t] = xn[u];
+          const unsigned long long ub = (unsigned long long)__double_as_longlong(xn[u]) & 0x7FFFFFFFFFFFFFFFULL;
+          mx = ub > mx ? ub : mx;
+        }
       }
+      // max |x| of the chunk into the instance's BS_MAXX (one atomic per warp)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long ox = __shfl_down_sync(0xffffffffu, mx, o);
+        mx = ox > mx ? ox : mx;
+      }
+      if ((threadIdx.x & 31) == 0 && mx) atomicMax((unsigned long long*)(B.sc + BS_MAXX), mx);
     }
     __syncthreads();
   }
@@ -449,6 +601,27 @@ void launch_bupdate(const BInst* bi, const int4* tab, long long nchunks, const i
   int win;
   const unsigned g = (unsigned)grid_for(nchunks, 6, &win);
   k_bupdate<<<g, kBThreads, 0, s>>>(bi, tab, nchunks, win, active);
+}
+
+void launch_bres_int(int kind, bool neumann, const BInst* bi, const int4* ttab, long long ntasks, const int* active,
+                     double* partials, cudaStream_t s) {
+  int win;
+  grid_for(1, 1, &win);  // device SM count
+  const long long want = (ntasks + kBThreads / 32 - 1) / (kBThreads / 32);  // one warp per task
+  const unsigned grid = (unsigned)std::max(1LL, std::min(want, (long long)g_nsm * 8));
+  if (kind == OPK_RESID9) {
+    if (neumann) k_bres_int<OPK_RESID9, true><<<grid, kBThreads, 0, s>>>(bi, ttab, ntasks, active, partials);
+    else k_bres_int<OPK_RESID9, false><<<grid, kBThreads, 0, s>>>(bi, ttab, ntasks, active, partials);
+  } else {
+    if (neumann) k_bres_int<OPK_RESID5, true><<<grid, kBThreads, 0, s>>>(bi, ttab, ntasks, active, partials);
+    else k_bres_int<OPK_RESID5, false><<<grid, kBThreads, 0, s>>>(bi, ttab, ntasks, active, partials);
+  }
+}
+
+void launch_brhs_shift(const BInst* bi, const int4* tab, long long nchunks, const int* active, cudaStream_t s) {
+  int win;
+  const unsigned g = (unsigned)grid_for(nchunks, 6, &win);
+  k_brhs_shift<<<g, kBThreads, 0, s>>>(bi, tab, nchunks, win, active);
 }
 
 void launch_bsmall(const BSmall* sm, int n, int smem, const int* active, cudaStream_t st) {

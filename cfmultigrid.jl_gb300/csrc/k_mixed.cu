@@ -163,23 +163,6 @@ __global__ void k_update_scaled(double* __restrict__ x, const float* __restrict_
 //
 // dq[I] = Q*diag[I] (an integer in 0..127) on wet cells, -128 on dry ones.
 
-// round(v * 2^k) for |v| 2^k < 2^59; zero and subnormal v give 0
-__device__ __forceinline__ long long to_fix(double v, int k) {
-  const long long u = __double_as_longlong(v);
-  const int ex = (int)(((unsigned long long)u >> 52) & 0x7ffULL);
-  const long long m = (u & 0x000FFFFFFFFFFFFFLL) | 0x0010000000000000LL;
-  const int sh = ex - 1075 + k;  // v = m 2^(ex-1075)
-  long long r;
-  if (sh >= 0) {
-    r = m << sh;
-  } else {
-    const int s = -sh;  // round half up on the magnitude
-    r = s <= 64 ? ((m >> (s - 1)) + 1) >> 1 : 0;
-  }
-  r = ex ? r : 0;
-  return u < 0 ? -r : r;
-}
-
 __device__ __forceinline__ int fix_exponent(const double* ds) {
   const double mx = fmax(ds[S_MAXX], ds[S_MAXB]);
   int e = 0;

@@ -154,14 +154,43 @@ __device__ __forceinline__ void tb_tile(const float* __restrict__ x, float* __re
 
 // ---------------------------------------------------------------------
 // Packed form: the same passes with two columns per thread and the FP32x2
-// instructions of sm_100+ (__fadd2_rn / __fmul2_rn / __ffma2_rn round each
-// lane exactly as the scalar _rn operations do, so the result is the same
-// bit for bit). A 128 x 64 tile lives in shared memory as two planes per
+// instructions of sm_100+ (add/mul/fma.rn.f32x2 round each lane exactly as
+// the scalar _rn operations do, so the result is the same bit for bit). A 128 x 64 tile lives in shared memory as two planes per
 // row, even columns then odd columns, so that every shared load of a warp
 // reads 32 consecutive words. b and -omega*idiag of the thread's own 4 x 2
 // cells stay in registers. Every sweep computes the whole tile (cells near
 // the tile edge read clamped neighbours and hold values that no later sweep
 // of the valid region reads); cells outside U keep their value.
+// Packed operations with an explicit rounding modifier. A packed product
+// feeding a packed sum is still contracted into one FMA by ptxas, so the
+// one place where a product is summed (cff*c - w*t) adds in scalar.
+union F2U {
+  float2 f;
+  unsigned long long u;
+};
+__device__ __forceinline__ float2 p_add(float2 a, float2 b) {
+  F2U x, y, r;
+  x.f = a;
+  y.f = b;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.u) : "l"(x.u), "l"(y.u));
+  return r.f;
+}
+__device__ __forceinline__ float2 p_mul(float2 a, float2 b) {
+  F2U x, y, r;
+  x.f = a;
+  y.f = b;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.u) : "l"(x.u), "l"(y.u));
+  return r.f;
+}
+__device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) {
+  F2U x, y, z, r;
+  x.f = a;
+  y.f = b;
+  z.f = c;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.u) : "l"(x.u), "l"(y.u), "l"(z.u));
+  return r.f;
+}
+
 constexpr int kT3W = 128, kT3H = 64;  // tile
 constexpr int kT3Tx = 64, kT3Ty = 16, kT3Rows = 4;
 constexpr int kT3Half = kT3W / 2;
@@ -227,21 +256,25 @@ __device__ __forceinline__ void tb3_tile(const float* __restrict__ x, float* __r
       float wp, ap, bp, ep;
       ld(r0 + r + 1, wp, ap, bp, ep);
       // faces ((W + E) + S) + N, S = row j-1
-      float2 f = __fadd2_rn(make_float2(w0, a0), make_float2(b0, e0));
-      f = __fadd2_rn(f, make_float2(am, bm));
-      f = __fadd2_rn(f, make_float2(ap, bp));
+      float2 f = p_add(make_float2(w0, a0), make_float2(b0, e0));
+      f = p_add(f, make_float2(am, bm));
+      f = p_add(f, make_float2(ap, bp));
       float2 t;
       if (ST == 5) {
-        t = __fadd2_rn(B[r], make_float2(-f.x, -f.y));  // b - s4
+        t = p_add(B[r], make_float2(-f.x, -f.y));  // b - s4
       } else {
         // diagonals in the order (i-1,j-1), (i+1,j-1), (i-1,j+1), (i+1,j+1)
-        float2 d = __fadd2_rn(make_float2(wm, am), make_float2(bm, em));
-        d = __fadd2_rn(d, make_float2(wp, ap));
-        d = __fadd2_rn(d, make_float2(bp, ep));
-        t = __ffma2_rn(f, make_float2(-0.5f, -0.5f), B[r]);
-        t = __ffma2_rn(d, make_float2(-0.25f, -0.25f), t);
+        float2 d = p_add(make_float2(wm, am), make_float2(bm, em));
+        d = p_add(d, make_float2(wp, ap));
+        d = p_add(d, make_float2(bp, ep));
+        t = p_fma(f, make_float2(-0.5f, -0.5f), B[r]);
+        t = p_fma(d, make_float2(-0.25f, -0.25f), t);
       }
-      float2 o = __fadd2_rn(__fmul2_rn(cff2, make_float2(a0, b0)), __fmul2_rn(NW[r], t));
+      // cff*c - w*t: the two products packed, their sum in scalar adds
+      // (ptxas fuses a packed mul and a packed add into one FMA even with
+      // an explicit rounding modifier; a GPU probe showed 1-4 ulp changes)
+      const float2 m1 = p_mul(cff2, make_float2(a0, b0)), m2 = p_mul(NW[r], t);
+      float2 o = make_float2(__fadd_rn(m1.x, m2.x), __fadd_rn(m1.y, m2.y));
       if (!tile_in_u) {
         if (!(inU >> (2 * r) & 1u)) o.x = a0;
         if (!(inU >> (2 * r + 1) & 1u)) o.y = b0;

@@ -364,6 +364,25 @@ __device__ __forceinline__ void d_prolong(T* xf, const T* x, const T* coef, cons
   }
 }
 
+// ------------------------------------------------------- fixed point
+// Integer form of the mixed loop's level-1 residual (k_mixed.cu, k_batch.cu).
+// round(v * 2^k) for |v| 2^k < 2^59; zero and subnormal v give 0
+__device__ __forceinline__ long long to_fix(double v, int k) {
+  const long long u = __double_as_longlong(v);
+  const int ex = (int)(((unsigned long long)u >> 52) & 0x7ffULL);
+  const long long m = (u & 0x000FFFFFFFFFFFFFLL) | 0x0010000000000000LL;
+  const int sh = ex - 1075 + k;  // v = m 2^(ex-1075)
+  long long r;
+  if (sh >= 0) {
+    r = m << sh;
+  } else {
+    const int s = -sh;  // round half up on the magnitude
+    r = s <= 64 ? ((m >> (s - 1)) + 1) >> 1 : 0;
+  }
+  r = ex ? r : 0;
+  return u < 0 ? -r : r;
+}
+
 // ------------------------------------------------------------------ halo
 // fill! for :xperio (src/halo.jl:6-9) on one (j,k) line. Each statement's
 // right-hand columns are read before any is written, as Julia's sliced

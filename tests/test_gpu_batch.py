@@ -35,13 +35,17 @@ def _setup(g, msk, noise):
     return m
 
 
+@pytest.mark.parametrize("int_res", [1, 0])
 @pytest.mark.parametrize("cycle", ["v", "f"])
-def test_batch_matches_single_solves(cycle):
+def test_batch_matches_single_solves(cycle, int_res):
+    """int_res: the level-1 residual in 64-bit fixed point (1) or FP64
+    arithmetic (0), in the batch and in the single solves alike."""
     probs = W.config4(ninst=10, seed=3, lo=64, hi=288)
     p = _param(cycle=cycle, maxite=100)
     batch = cfmg.Batch(p, [q[0] for q in probs], [q[0] for q in probs], [q[1] for q in probs])
     masks = []
     for i, (n, nlev, msk, noise) in enumerate(probs):
+        batch.instance(i).set_option("int_residual", int_res)
         masks.append(_setup(batch.instance(i), msk, noise))
     res, nite, t = batch.solve()
     assert np.all(t > 0)
@@ -54,6 +58,7 @@ def test_batch_matches_single_solves(cycle):
         assert abs(true - res[i]) <= 1e-6 * res[i], (i, true, res[i])
         # single-handle mixed solve of the same problem: same outcome
         s = cfmg.get_gmg(dataclasses_replace(p, nx=n, ny=n, nlevels=nlev))
+        s.set_option("int_residual", int_res)
         _setup(s, msk, noise)
         r1, n1 = cfmg.solve(s)
         assert (res[i] <= 1e-10) == (r1 <= 1e-10), (i, res[i], r1)
