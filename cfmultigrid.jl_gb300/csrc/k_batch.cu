@@ -292,13 +292,15 @@ __global__ void __launch_bounds__(kBThreads) k_bres_int(const BInst* __restrict_
           else
             R = (long long)d * C0 + Bf - (((W0 + E0) + Cm) + Cp);
         }
-        const float f = __ll2float_rn(R) * fm;
+        const float f = __fmul_rn(__ll2float_rn(R), fm);
         B.b32[I] = f;
         if (NEUMANN) s1 += (__int128)R;
         else B.r32[I] = f;
-        const float p = f * f, e = __fmaf_rn(f, f, -p);
-        const float sn = hi + p, bp = sn - hi;
-        lo += ((hi - (sn - bp)) + (p - bp)) + e;
+        // p + e = f^2 exactly; (hi, lo) += p + e by TwoSum (explicit _rn
+        // operations: a contracted hi + f*f would break the error terms)
+        const float p = __fmul_rn(f, f), e = __fmaf_rn(f, f, -p);
+        const float sn = __fadd_rn(hi, p), bp = __fsub_rn(sn, hi);
+        lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(__fsub_rn(hi, __fsub_rn(sn, bp)), __fsub_rn(p, bp)), e));
         hi = sn;
       }
       Wm = W0; Cm = C0; Em = E0;

@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int(const double* __restri
     const long long R = fix_resid<KIND>(x, b, dq[I], k, g.n1, g.n2, I);
     const double rd = __ll2double_rn(R);
     s2 = __fma_rn(rd, rd, s2);
-    const float f = __ll2float_rn(R) * fm;
+    const float f = __fmul_rn(__ll2float_rn(R), fm);
     b32[I] = f;
     if (NEUMANN) s1 += (__int128)R;
     else if (r32) r32[I] = f;
@@ -321,13 +321,15 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __rest
           else
             R = (long long)d * C0 + B - (((W0 + E0) + Cm) + Cp);
         }
-        const float f = __ll2float_rn(R) * fm;
+        const float f = __fmul_rn(__ll2float_rn(R), fm);
         b32[I] = f;
         if (NEUMANN) s1 += (__int128)R;
         else if (r32) r32[I] = f;
-        const float p = f * f, e = __fmaf_rn(f, f, -p);  // p + e = f^2 exactly
-        const float sn = hi + p, bp = sn - hi;
-        lo += ((hi - (sn - bp)) + (p - bp)) + e;
+        // p + e = f^2 exactly; (hi, lo) += p + e by TwoSum (explicit _rn
+        // operations: a contracted hi + f*f would break the error terms)
+        const float p = __fmul_rn(f, f), e = __fmaf_rn(f, f, -p);
+        const float sn = __fadd_rn(hi, p), bp = __fsub_rn(sn, hi);
+        lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(__fsub_rn(hi, __fsub_rn(sn, bp)), __fsub_rn(p, bp)), e));
         hi = sn;
       }
       Wm = W0; Cm = C0; Em = E0;
