@@ -52,10 +52,13 @@ def test_batch_matches_single_solves(cycle, int_res):
     for i, (n, nlev, msk, noise) in enumerate(probs):
         g = batch.instance(i)
         x = g.data[1].x
-        # the reported residual is the true FP64 one of the batched solution
+        # the reported residual is the batched solution's own: recomputed in
+        # FP64 arithmetic it agrees to the rounding noise of that arithmetic
+        # near 1e-10 (|A||x| 2^-53 per cell against r; the fixed-point form
+        # is exact for x on its 2^-k grid), 1e-4 relative here
         nb = cfmg.norm(g, 1, "b")
         true = cfmg.normresidual(g, nb) ** 0.5
-        assert abs(true - res[i]) <= 1e-6 * res[i], (i, true, res[i])
+        assert abs(true - res[i]) <= (1e-4 if int_res else 1e-6) * res[i], (i, true, res[i])
         # single-handle mixed solve of the same problem: same outcome
         s = cfmg.get_gmg(dataclasses_replace(p, nx=n, ny=n, nlevels=nlev))
         s.set_option("int_residual", int_res)
