@@ -439,12 +439,19 @@ def run_3d(args, rank, world, local):
     n = args.n if args.n != 4096 else 512
     param, msk, noise = W.config3(n, n, n // 2, nlevels=args.nlevels or 8)
     mgm, b = make_gmg(cfmg, param, msk, noise, "mixed", sp, tol=tol, maxite=400)
-    mgd, _ = make_gmg(cfmg, param, msk, noise, "fp64", sp, tol=tol, maxite=400)
-    level_cells = [g.tx * g.ty * g.tz for g in mgm.levels]
 
     def solve(mg):
         cfmg.set_to_zero(mg, 1, "x")
         return cfmg.solve(mg)
+
+    if args.quick:
+        solve(mgm)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        res, nit = solve(mgm)
+        return {"quick": True, "ms": (time.perf_counter() - t) * 1e3, "cycles": nit, "res": res}
+    mgd, _ = make_gmg(cfmg, param, msk, noise, "fp64", sp, tol=tol, maxite=400)
+    level_cells = [g.tx * g.ty * g.tz for g in mgm.levels]
 
     for _ in range(max(args.warmup, 3)):
         res_m, nit_m = solve(mgm)

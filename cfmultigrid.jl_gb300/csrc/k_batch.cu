@@ -266,9 +266,13 @@ __global__ void __launch_bounds__(kBThreads) k_bres_int(const BInst* __restrict_
     const bool col_ok = c < B.c0 + B.ncols;
     const int ra = en.z * kBIntRows, rb = min(ra + kBIntRows, B.nrows);
     auto at = [&](long long J) { return x[J < 0 ? 0 : (J >= len ? len - 1 : J)]; };
-    auto load_row = [&](long long Ir, long long& W, long long& C, long long& E) {
-      C = to_fix(at(Ir), k);
-      const long long xe = (lane == 0) ? to_fix(at(Ir - 1), k) : ((lane == 31) ? to_fix(at(Ir + 1), k) : 0);
+    auto raw = [&](long long Ir, double& xc, double& xe) {
+      xc = at(Ir);
+      xe = at(lane == 0 ? Ir - 1 : (lane == 31 ? Ir + 1 : Ir));
+    };
+    auto conv_row = [&](double xc, double xev, long long& W, long long& C, long long& E) {
+      C = to_fix(xc, k);
+      const long long xe = to_fix(xev, k);
       W = __shfl_up_sync(0xffffffffu, C, 1);
       E = __shfl_down_sync(0xffffffffu, C, 1);
       if (lane == 0) W = xe;
@@ -276,17 +280,30 @@ __global__ void __launch_bounds__(kBThreads) k_bres_int(const BInst* __restrict_
     };
     long long I = B.row0 + (long long)ra * n1 + c;
     long long Wm, Cm, Em, W0, C0, E0, Wp, Cp, Ep;
-    load_row(I - n1, Wm, Cm, Em);
-    load_row(I, W0, C0, E0);
+    double rc, re;
+    raw(I - n1, rc, re);
+    conv_row(rc, re, Wm, Cm, Em);
+    raw(I, rc, re);
+    conv_row(rc, re, W0, C0, E0);
+    double nc, ne;  // one row of look-ahead (see k_resid_int2d)
+    raw(I + n1, nc, ne);
+    double nb = col_ok ? B.b[I] : 0.0;
+    int nd = col_ok ? B.dq[I] : -1;
     float hi = 0.f, lo = 0.f;
     __int128 s1 = 0;
     for (int r = ra; r < rb; ++r, I += n1) {
-      load_row(I + n1, Wp, Cp, Ep);
+      conv_row(nc, ne, Wp, Cp, Ep);
+      const double cb = nb;
+      const int d = nd;
+      if (r + 1 < rb) {
+        raw(I + 2 * n1, nc, ne);
+        nb = col_ok ? B.b[I + n1] : 0.0;
+        nd = col_ok ? B.dq[I + n1] : -1;
+      }
       if (col_ok) {
-        const int d = B.dq[I];
         long long R = 0;
         if (d >= 0) {
-          const long long Bf = to_fix(B.b[I], k);
+          const long long Bf = to_fix(cb, k);
           if (KIND == OPK_RESID9)
             R = (long long)d * C0 + 4 * Bf - 2 * (((W0 + E0) + Cm) + Cp) - (((Wm + Em) + Wp) + Ep);
           else

@@ -298,24 +298,45 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __rest
     // rows above the first / below the last output row may reach past its
     // ends, where the values are never used
     auto at = [&](long long J) { return x[J < 0 ? 0 : (J >= sp.len ? sp.len - 1 : J)]; };
-    auto load_row = [&](long long Ir, long long& W, long long& C, long long& E) {
-      C = to_fix(at(Ir), k);
-      const long long xe = (lane == 0) ? to_fix(at(Ir - 1), k) : ((lane == 31) ? to_fix(at(Ir + 1), k) : 0);
+    // raw loads of a row: x at this lane, and the one value beyond the strip
+    // for lanes 0 / 31 (others load their own x again)
+    auto raw = [&](long long Ir, double& xc, double& xe) {
+      xc = at(Ir);
+      xe = at(lane == 0 ? Ir - 1 : (lane == 31 ? Ir + 1 : Ir));
+    };
+    auto conv_row = [&](double xc, double xev, long long& W, long long& C, long long& E) {
+      C = to_fix(xc, k);
+      const long long xe = to_fix(xev, k);
       W = __shfl_up_sync(0xffffffffu, C, 1);
       E = __shfl_down_sync(0xffffffffu, C, 1);
       if (lane == 0) W = xe;
       if (lane == 31) E = xe;
     };
     long long Wm, Cm, Em, W0, C0, E0, Wp, Cp, Ep;
-    load_row(I - sp.n1, Wm, Cm, Em);
-    load_row(I, W0, C0, E0);
+    double rc, re;
+    raw(I - sp.n1, rc, re);
+    conv_row(rc, re, Wm, Cm, Em);
+    raw(I, rc, re);
+    conv_row(rc, re, W0, C0, E0);
+    // one row of look-ahead: the raw x of row r+1 and b, dq of row r are in
+    // flight while row r-1 is computed
+    double nc, ne;
+    raw(I + sp.n1, nc, ne);
+    double nb = col_ok ? b[I] : 0.0;
+    int nd = col_ok ? dq[I] : -1;
     for (int r = ra; r < rb; ++r, I += sp.n1) {
-      load_row(I + sp.n1, Wp, Cp, Ep);
+      conv_row(nc, ne, Wp, Cp, Ep);
+      const double cb = nb;
+      const int d = nd;
+      if (r + 1 < rb) {
+        raw(I + 2 * sp.n1, nc, ne);
+        nb = col_ok ? b[I + sp.n1] : 0.0;
+        nd = col_ok ? dq[I + sp.n1] : -1;
+      }
       if (col_ok) {
-        const int d = dq[I];
         long long R = 0;
         if (d >= 0) {
-          const long long B = to_fix(b[I], k);
+          const long long B = to_fix(cb, k);
           if (KIND == OPK_RESID9)
             R = (long long)d * C0 + 4 * B - 2 * (((W0 + E0) + Cm) + Cp) - (((Wm + Em) + Wp) + Ep);
           else
@@ -459,11 +480,23 @@ __global__ void __launch_bounds__(kMxThreads) k_update_scaled_max(double* __rest
                                                                   double* dsw) {
   const double is = ds[S_ICUR];
   unsigned long long mx = 0;
-  for (long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x; I < n; I += (long long)gridDim.x * blockDim.x) {
-    const double v = __fma_rn((double)e[I], is, x[I]);
-    x[I] = v;
-    const unsigned long long u = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFULL;
-    mx = u > mx ? u : mx;
+  const long long st = (long long)gridDim.x * blockDim.x;
+  for (long long I0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; I0 < n; I0 += 4 * st) {
+    double v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {  // loads of 4 cells in flight
+      const long long I = I0 + u * st;
+      if (I < n) v[u] = __fma_rn((double)e[I], is, x[I]);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const long long I = I0 + u * st;
+      if (I < n) {
+        x[I] = v[u];
+        const unsigned long long ub = (unsigned long long)__double_as_longlong(v[u]) & 0x7FFFFFFFFFFFFFFFULL;
+        mx = ub > mx ? ub : mx;
+      }
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -511,7 +544,13 @@ void launch_maxabs2(const double* x, const double* b, long long n, double* ds, c
 }
 
 void launch_update_scaled_max(double* x, const float* e, double* ds, long long n, cudaStream_t s) {
-  k_update_scaled_max<<<kMxParts, kMxThreads, 0, s>>>(x, e, ds, n, ds);
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  }
+  k_update_scaled_max<<<nsm * 8, kMxThreads, 0, s>>>(x, e, ds, n, ds);
 }
 
 void launch_resid_fused(int kind, double* r, const double* x, const double* b, const double* d, const uint8_t* m,
