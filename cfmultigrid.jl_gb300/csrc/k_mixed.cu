@@ -263,7 +263,9 @@ constexpr int kIntRows = 32;  // rows per warp task
 
 struct StripSpace {
   long long len;   // array length
-  long long row0;  // linear index of column 0 of the first row
+  long long row0;  // linear index of column 0 of the first row (of the first plane)
+  long long n2;    // plane stride (7-point: the k +- 1 neighbours)
+  int nplanes;     // planes of the index space (1 in 2D)
   int c0, ncols;   // columns of the index space: c0 .. c0+ncols-1 (0-based linear offsets in a row)
   int nrows;       // rows of the index space
   int nstrips;     // ceil(ncols / 32)
@@ -283,17 +285,20 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __rest
   const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   const int nchunks = (sp.nrows + kIntRows - 1) / kIntRows;
-  const long long ntasks = (long long)sp.nstrips * nchunks;
+  const long long per_plane = (long long)sp.nstrips * nchunks;
+  const long long ntasks = per_plane * sp.nplanes;
   float hi = 0.f, lo = 0.f;  // double-float sum of f^2
   __int128 s1 = 0;
   for (long long task = warp0; task < ntasks; task += nwarps) {
-    const int strip = (int)(task % sp.nstrips);
-    const int chunk = (int)(task / sp.nstrips);
+    const int plane = (int)(task / per_plane);
+    const long long pt = task - plane * per_plane;
+    const int strip = (int)(pt % sp.nstrips);
+    const int chunk = (int)(pt / sp.nstrips);
     const int c = sp.c0 + strip * 32 + lane;  // this lane's column
     const bool col_ok = c < sp.c0 + sp.ncols;
     const int ra = chunk * kIntRows, rb = min(ra + kIntRows, sp.nrows);
     // rows ra-1 and ra
-    long long I = sp.row0 + (long long)ra * sp.n1 + c;
+    long long I = sp.row0 + plane * sp.n2 + (long long)ra * sp.n1 + c;
     // loads are clamped to the array: lanes past the index space and the
     // rows above the first / below the last output row may reach past its
     // ends, where the values are never used
@@ -324,14 +329,23 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __rest
     raw(I + sp.n1, nc, ne);
     double nb = col_ok ? b[I] : 0.0;
     int nd = col_ok ? dq[I] : -1;
+    double nlo = 0.0, nhi = 0.0;  // 7-point: x of the planes below and above
+    if (KIND == OPK_RESID7 && col_ok) {
+      nlo = x[I - sp.n2];
+      nhi = x[I + sp.n2];
+    }
     for (int r = ra; r < rb; ++r, I += sp.n1) {
       conv_row(nc, ne, Wp, Cp, Ep);
-      const double cb = nb;
+      const double cb = nb, clo = nlo, chi = nhi;
       const int d = nd;
       if (r + 1 < rb) {
         raw(I + 2 * sp.n1, nc, ne);
         nb = col_ok ? b[I + sp.n1] : 0.0;
         nd = col_ok ? dq[I + sp.n1] : -1;
+        if (KIND == OPK_RESID7 && col_ok) {
+          nlo = x[I + sp.n1 - sp.n2];
+          nhi = x[I + sp.n1 + sp.n2];
+        }
       }
       if (col_ok) {
         long long R = 0;
@@ -339,6 +353,8 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __rest
           const long long B = to_fix(cb, k);
           if (KIND == OPK_RESID9)
             R = (long long)d * C0 + 4 * B - 2 * (((W0 + E0) + Cm) + Cp) - (((Wm + Em) + Wp) + Ep);
+          else if (KIND == OPK_RESID7)
+            R = (long long)d * C0 + B - ((((W0 + E0) + Cm) + Cp) + (to_fix(clo, k) + to_fix(chi, k)));
           else
             R = (long long)d * C0 + B - (((W0 + E0) + Cm) + Cp);
         }
@@ -388,11 +404,20 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __rest
 
 bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t* dq, const Geom& g, const Box& bx,
                         const double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s) {
-  if (g.tz != 1) return false;
   StripSpace sp;
   sp.n1 = g.n1;
+  sp.n2 = g.n2;
   sp.len = g.len;
-  if (kind == OPK_RESID5) {  // linear range 1+n1 .. len-n1: rows 2..ty-1, every column
+  sp.nplanes = 1;
+  if (kind == OPK_RESID7) {  // interior box ic x jc x kc (rloop3d!)
+    sp.row0 = (long long)(bx.j0 - 1) * g.n1 + (long long)(bx.k0 - 1) * g.n2;
+    sp.c0 = bx.i0 - 1;
+    sp.ncols = bx.i1 - bx.i0 + 1;
+    sp.nrows = bx.j1 - bx.j0 + 1;
+    sp.nplanes = bx.k1 - bx.k0 + 1;
+  } else if (g.tz != 1) {
+    return false;
+  } else if (kind == OPK_RESID5) {  // linear range 1+n1 .. len-n1: rows 2..ty-1, every column
     sp.row0 = g.n1;
     sp.c0 = 0;
     sp.ncols = g.tx;
@@ -405,7 +430,7 @@ bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t
   } else {
     return false;
   }
-  if (sp.nrows <= 0 || sp.ncols <= 0) return false;
+  if (sp.nrows <= 0 || sp.ncols <= 0 || sp.nplanes <= 0) return false;
   sp.nstrips = (sp.ncols + 31) / 32;
 #define CFMG_INT2(K)                                                                                        \
   if (kind == K) {                                                                                          \
@@ -417,6 +442,7 @@ bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t
   }
   CFMG_INT2(OPK_RESID5)
   CFMG_INT2(OPK_RESID9)
+  CFMG_INT2(OPK_RESID7)
 #undef CFMG_INT2
   return false;
 }

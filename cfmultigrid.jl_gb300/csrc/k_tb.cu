@@ -193,22 +193,8 @@ __device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) {
 
 constexpr int kT3W = 128, kT3H = 64;  // tile
 constexpr int kT3Tx = 64, kT3Ty = 16, kT3Rows = 4;
-constexpr int kT3S = kT3W + 4;  // shared row: x[c] at c + 1, c = -1 .. 128 (stride kept even)
+constexpr int kT3Half = kT3W / 2;
 
-__device__ __forceinline__ float2 p_sub(float2 a, float2 b) {
-  F2U x, y, r;
-  x.f = a;
-  y.f = b;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.u) : "l"(x.u), "l"(y.u));
-  return r.f;
-}
-
-// The tile's rows live in shared memory shifted by one column, so that the
-// 64-bit word l of a row holds (x[2l-1], x[2l]): the west/centre pair of
-// the thread's even cell, and word l+1 the centre/east pair of its odd
-// cell. A row is then two 64-bit loads per thread with no register moves
-// for the faces and diagonals; the (centre, centre) pair of the two cells
-// is assembled once per row.
 template <int ST, int NITE>
 __device__ __forceinline__ void tb3_tile(const float* __restrict__ x, float* __restrict__ xo,
                                          const float* __restrict__ b, const float* __restrict__ w, float cff, int tx,
@@ -216,8 +202,8 @@ __device__ __forceinline__ void tb3_tile(const float* __restrict__ x, float* __r
                                          float* smem) {
   constexpr int H = 2 * NITE;
   constexpr int CW = kT3W - 2 * H, CH = kT3H - 2 * H;
-  float* P0 = smem;  // [kT3H][kT3S]
-  float* P1 = smem + kT3H * kT3S;
+  float* P0 = smem;              // [kT3H][even | odd]
+  float* P1 = smem + kT3H * kT3W;
   const int lx = threadIdx.x;
   const int r0 = threadIdx.y * kT3Rows;
   const int gi0 = ui0 + bx * CW - H + 2 * lx;  // 1-based global column of the even cell
@@ -239,11 +225,8 @@ __device__ __forceinline__ void tb3_tile(const float* __restrict__ x, float* __r
       ww[e] = in ? w[I] : 0.f;
       if (gi >= ui0 && gi <= ui1 && gj >= uj0 && gj <= uj1) inU |= 1u << (2 * r + e);
     }
-    float* row = P0 + (r0 + r) * kT3S;
-    row[2 * lx + 1] = v[0];
-    row[2 * lx + 2] = v[1];
-    if (lx == 0) row[0] = 0.f;                 // x[-1]
-    if (lx == kT3Tx - 1) row[kT3W + 1] = 0.f;  // x[128]
+    P0[(r0 + r) * kT3W + lx] = v[0];
+    P0[(r0 + r) * kT3W + kT3Half + lx] = v[1];
     B[r] = make_float2(bb[0], bb[1]);
     NW[r] = make_float2(-ww[0], -ww[1]);
   }
@@ -251,60 +234,55 @@ __device__ __forceinline__ void tb3_tile(const float* __restrict__ x, float* __r
   const int ti0 = ui0 + bx * CW - H, tj0 = uj0 + by * CH - H;  // tile origin
   const bool tile_in_u = ti0 >= ui0 && ti0 + kT3W - 1 <= ui1 && tj0 >= uj0 && tj0 + kT3H - 1 <= uj1;
   const float2 cff2 = make_float2(cff, cff);
+  const int lw = lx > 0 ? lx - 1 : 0, le = lx < kT3Half - 1 ? lx + 1 : kT3Half - 1;
 #pragma unroll 1
   for (int s = 0; s < 2 * NITE; ++s) {
     const float* src = (s & 1) ? P1 : P0;
     float* dst = (s & 1) ? P0 : P1;
-    // a row: L = (x[2l-1], x[2l]), R = (x[2l+1], x[2l+2]), C = (x[2l], x[2l+1]);
-    // rows outside the tile are clamped (their values are never used by a
-    // valid cell)
-    auto ld = [&](int rr, float2& Lv, float2& Rv, float2& Cv) {
+    // (west, even, odd, east) of a row; rows outside the tile are clamped
+    auto ld = [&](int rr, float& wv, float& av, float& bv, float& ev) {
       rr = rr < 0 ? 0 : (rr >= kT3H ? kT3H - 1 : rr);
-      const float2* row = reinterpret_cast<const float2*>(src + rr * kT3S);
-      Lv = row[lx];
-      Rv = row[lx + 1];
-      Cv = make_float2(Lv.y, Rv.x);
+      const float* row = src + rr * kT3W;
+      av = row[lx];
+      bv = row[kT3Half + lx];
+      wv = row[kT3Half + lw];
+      ev = row[le];
     };
-    float2 Lm, Rm, Cm, L0, R0, C0;
-    ld(r0 - 1, Lm, Rm, Cm);
-    ld(r0, L0, R0, C0);
+    float wm, am, bm, em, w0, a0, b0, e0;
+    ld(r0 - 1, wm, am, bm, em);
+    ld(r0, w0, a0, b0, e0);
 #pragma unroll
     for (int r = 0; r < kT3Rows; ++r) {
-      float2 Lp, Rp, Cp;
-      ld(r0 + r + 1, Lp, Rp, Cp);
-      // faces ((W + E) + S) + N, S = row j-1: (W, E) of the two cells = (L, R)
-      float2 f = p_add(L0, R0);
-      f = p_add(f, Cm);
-      f = p_add(f, Cp);
+      float wp, ap, bp, ep;
+      ld(r0 + r + 1, wp, ap, bp, ep);
+      // faces ((W + E) + S) + N, S = row j-1
+      float2 f = p_add(make_float2(w0, a0), make_float2(b0, e0));
+      f = p_add(f, make_float2(am, bm));
+      f = p_add(f, make_float2(ap, bp));
       float2 t;
       if (ST == 5) {
-        t = p_sub(B[r], f);  // b - s4
+        t = p_add(B[r], make_float2(-f.x, -f.y));  // b - s4
       } else {
         // diagonals in the order (i-1,j-1), (i+1,j-1), (i-1,j+1), (i+1,j+1)
-        float2 d = p_add(Lm, Rm);
-        d = p_add(d, Lp);
-        d = p_add(d, Rp);
+        float2 d = p_add(make_float2(wm, am), make_float2(bm, em));
+        d = p_add(d, make_float2(wp, ap));
+        d = p_add(d, make_float2(bp, ep));
         t = p_fma(f, make_float2(-0.5f, -0.5f), B[r]);
         t = p_fma(d, make_float2(-0.25f, -0.25f), t);
       }
       // cff*c - w*t: the two products packed, their sum in scalar adds
       // (ptxas fuses a packed mul and a packed add into one FMA even with
       // an explicit rounding modifier; a GPU probe showed 1-4 ulp changes)
-      const float2 m1 = p_mul(cff2, C0), m2 = p_mul(NW[r], t);
-      float ox = __fadd_rn(m1.x, m2.x), oy = __fadd_rn(m1.y, m2.y);
+      const float2 m1 = p_mul(cff2, make_float2(a0, b0)), m2 = p_mul(NW[r], t);
+      float2 o = make_float2(__fadd_rn(m1.x, m2.x), __fadd_rn(m1.y, m2.y));
       if (!tile_in_u) {
-        if (!(inU >> (2 * r) & 1u)) ox = C0.x;
-        if (!(inU >> (2 * r + 1) & 1u)) oy = C0.y;
+        if (!(inU >> (2 * r) & 1u)) o.x = a0;
+        if (!(inU >> (2 * r + 1) & 1u)) o.y = b0;
       }
-      float* drow = dst + (r0 + r) * kT3S;
-      drow[2 * lx + 1] = ox;
-      drow[2 * lx + 2] = oy;
-      Lm = L0; Rm = R0; Cm = C0;
-      L0 = Lp; R0 = Rp; C0 = Cp;
-    }
-    if (lx == 0 || lx == kT3Tx - 1) {  // the tile's edge words stay defined
-#pragma unroll
-      for (int r = 0; r < kT3Rows; ++r) dst[(r0 + r) * kT3S + (lx == 0 ? 0 : kT3W + 1)] = 0.f;
+      dst[(r0 + r) * kT3W + lx] = o.x;
+      dst[(r0 + r) * kT3W + kT3Half + lx] = o.y;
+      wm = w0; am = a0; bm = b0; em = e0;
+      w0 = wp; a0 = ap; b0 = bp; e0 = ep;
     }
     __syncthreads();
   }
@@ -318,7 +296,7 @@ __device__ __forceinline__ void tb3_tile(const float* __restrict__ x, float* __r
       const int lc = 2 * lx + e;
       if (lc >= H && lc < kT3W - H && (inU >> (2 * r + e) & 1u)) {
         const long long I = plane + (long long)(gi0 + e - 1) + (long long)tx * (gj0 + r - 1);
-        xo[I] = P0[lj * kT3S + lc + 1];
+        xo[I] = P0[lj * kT3W + e * kT3Half + lx];
       }
     }
   }
@@ -399,7 +377,7 @@ static void launch_tb3_n(const float* x, float* xo, const float* b, const float*
                          int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s) {
   constexpr int H = 2 * NITE;
   constexpr int CW = kT3W - 2 * H, CH = kT3H - 2 * H;
-  const size_t smem = 2 * (size_t)kT3H * kT3S * sizeof(float);
+  const size_t smem = 2 * (size_t)kT3H * kT3W * sizeof(float);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_smooth_tb3<ST, NITE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
