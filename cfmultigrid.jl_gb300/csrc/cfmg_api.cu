@@ -34,6 +34,9 @@ struct cfmg_handle {
   // captured graphs: one cycle + normresidual per cycle kind and precision
   cudaGraphExec_t graph[2][6] = {{nullptr}};
   long long graph_launches[2][6] = {{0}};
+  // whole solve loops: a graph `while` node around one iteration
+  cudaGraphExec_t sgraph[2][6] = {{nullptr}};
+  double* dhist = nullptr;  // device residual history (maxite + 1)
   long long launches = 0;      // kernels launched (graph replays count every kernel node)
   bool capturing = false;
   // device-time profile of one kernel class on one level (cfmg_profile)
@@ -1043,12 +1046,86 @@ int get_graph(cfmg_handle* h, int prec, int kind, int norm_kind, cudaGraphExec_t
 }
 
 void drop_graphs(cfmg_handle* h) {
-  for (auto& row : h->graph)
-    for (auto& g : row)
-      if (g) {
-        cudaGraphExecDestroy(g);
-        g = nullptr;
-      }
+  for (auto* tab : {&h->graph, &h->sgraph})
+    for (auto& row : *tab)
+      for (auto& g : row)
+        if (g) {
+          cudaGraphExecDestroy(g);
+          g = nullptr;
+        }
+}
+
+// The solve! loop on the device (src/gmg_solver.jl:29-39): hist[nite] = res
+// after every residual, and another iteration while res > tol and
+// nite < maxite (the count moves before the iteration runs).
+__global__ void k_loop_test(cudaGraphConditionalHandle hc, double* ds, double* hist, double tol, int maxite,
+                            int first) {
+  if (first) ds[S_NITE] = 0.0;
+  const double res = ds[S_RES];
+  const int nite = (int)ds[S_NITE];
+  hist[nite] = res;
+  const bool more = res > tol && nite < maxite;
+  if (more) ds[S_NITE] = (double)(nite + 1);
+  cudaGraphSetConditional(hc, more ? 1u : 0u);
+}
+
+int get_solve_graph(cfmg_handle* h, int prec, int kind, int norm_kind, cudaGraphExec_t* out) {
+  cudaGraphExec_t& ge = h->sgraph[prec][kind];
+  if (ge) {
+    *out = ge;
+    return CFMG_OK;
+  }
+  if (!h->dhist) CUDA_OK(h, cudaMalloc((void**)&h->dhist, sizeof(double) * (size_t)(h->d.maxite + 1)));
+  cudaGraph_t g = nullptr;
+  CUDA_OK(h, cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle hc;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&hc, g, 0, 0);
+  auto bail = [&](const char* what) {
+    cudaGraphDestroy(g);
+    return fail(h, CFMG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  };
+  if (e != cudaSuccess) return bail("conditional handle");
+  // the test of the first residual, then while (test) { iteration; test }
+  if ((e = cudaStreamBeginCaptureToGraph(h->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed)) !=
+      cudaSuccess)
+    return bail("solve capture");
+  k_loop_test<<<1, 1, 0, h->stream>>>(hc, h->dscal, h->dhist, h->d.tol, h->d.maxite, 1);
+  if ((e = cudaStreamEndCapture(h->stream, &g)) != cudaSuccess) return bail("solve capture");
+  cudaGraphNode_t first = nullptr;
+  size_t nn = 1;
+  if ((e = cudaGraphGetNodes(g, &first, &nn)) != cudaSuccess) return bail("solve graph");
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = hc;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t wnode;
+  if ((e = cudaGraphAddNode(&wnode, g, &first, nullptr, 1, &cp)) != cudaSuccess) return bail("while node");
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  if ((e = cudaStreamBeginCaptureToGraph(h->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed)) !=
+      cudaSuccess)
+    return bail("solve capture");
+  const long long before = h->launches;
+  h->capturing = true;
+  int rc = iteration(h, prec, kind, norm_kind);
+  h->capturing = false;
+  h->graph_launches[prec][kind] = h->launches - before;
+  h->launches = before;
+  if (rc == CFMG_OK) k_loop_test<<<1, 1, 0, h->stream>>>(hc, h->dscal, h->dhist, h->d.tol, h->d.maxite, 0);
+  e = cudaStreamEndCapture(h->stream, &body);
+  if (rc != CFMG_OK) {
+    cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return bail("solve capture");
+  e = cudaGraphInstantiate(&ge, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    ge = nullptr;
+    return fail(h, CFMG_ERR_CUDA, std::string("solve graph instantiate: ") + cudaGetErrorString(e));
+  }
+  *out = ge;
+  return CFMG_OK;
 }
 
 // ------------------------------------------------ whole-solve programs
@@ -1308,6 +1385,7 @@ int cfmg_destroy(cfmg_handle* h) {
   for (double* p : {h->adj_x, h->adj_b, h->adj_gk})
     if (p) cudaFree(p);
   if (h->dq) cudaFree(h->dq);
+  if (h->dhist) cudaFree(h->dhist);
   if (h->arena) cudaFree(h->arena);
   if (h->hscal) cudaFreeHost(h->hscal);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -1543,6 +1621,21 @@ int cfmg_solve(cfmg_handle* h, double* res_out, int* nite_out, double* history) 
     TRY(fused_residual(h));
   } else {
     TRY(normresidual_dev(h, d.norm_kind));
+  }
+  if (h->prof_cls < 0) {
+    // the whole loop as one graph launch; the history comes back at the end
+    cudaGraphExec_t sg = nullptr;
+    TRY(get_solve_graph(h, prec, d.cycle, d.norm_kind, &sg));
+    CUDA_OK(h, cudaGraphLaunch(sg, h->stream));
+    CUDA_OK(h, cudaMemcpyAsync(h->hscal, h->dscal, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync(h));
+    const int nite = (int)h->hscal[S_NITE];
+    h->launches += 2 + (long long)nite * (h->graph_launches[prec][d.cycle] + 1);
+    if (history)
+      CUDA_OK(h, cudaMemcpy(history, h->dhist, sizeof(double) * (size_t)(nite + 1), cudaMemcpyDeviceToHost));
+    *res_out = h->hscal[S_RES];
+    *nite_out = nite;
+    return CFMG_OK;
   }
   CUDA_OK(h, cudaMemcpyAsync(h->hscal, h->dscal, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   TRY(sync(h));

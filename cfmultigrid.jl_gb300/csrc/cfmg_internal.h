@@ -242,7 +242,8 @@ void launch_bcond(cudaGraphConditionalHandle hc, int* nactive, cudaStream_t s);
 
 // device scalars of a handle (dscal[])
 enum Scal { S_NORM = 0, S_RES = 1, S_NORMB = 2, S_NWET = 3, S_SCALE = 4, S_MEAN = 5, S_TMP0 = 6, S_ISCALE = 7,
-            S_NEXT = 8, S_CUR = 9, S_ICUR = 10, S_MEAN2 = 11, S_MAXX = 12, S_MAXB = 13, S_COUNT = 16 };
+            S_NEXT = 8, S_CUR = 9, S_ICUR = 10, S_MEAN2 = 11, S_MAXX = 12, S_MAXB = 13, S_NITE = 14,
+            S_COUNT = 16 };
 
 // fused FP64 steps of the mixed loop (k_mixed.cu)
 void launch_resid_fused(int kind, double* r, const double* x, const double* b, const double* d, const uint8_t* m,
