@@ -365,13 +365,34 @@ int sweep(cfmg_handle* h, int lev, int kind, const T* x, T* y, const Box* bx) {
 // topology, 2D 5- and 9-point): the result goes to the partner buffer.
 template <class T>
 bool tb_eligible(const cfmg_handle* h, int lev) {
-  if (sizeof(T) != 4 || !h->tb_on || (h->record && !h->record_tb) || xperio(h) || threed(h)) return false;
+  if (sizeof(T) != 4 || !h->tb_on || (h->record && !h->record_tb) || xperio(h)) return false;
+  if (threed(h) && (h->d.op != CFMG_LAPLACIAN || h->record)) return false;  // 3D: 7-point streaming passes
   if (h->d.op != CFMG_LAPLACIAN && h->d.op != CFMG_LAPLACIAN9) return false;
   const Level& l = h->lv[lev - 1];
   return !(h->engine_on && (long long)l.len <= engine_limit(h, CFMG_MIXED));
 }
 
+// 3D 7-point: passes of up to 2 pairs (k_tb3d.cu), x -> partner buffer
+int smooth_tb3d(cfmg_handle* h, int lev, int nite) {
+  Level& l = h->lv[lev - 1];
+  TRY(flush(h));
+  for (int left = nite; left > 0;) {
+    const int n = left > 2 ? 2 : left;
+    View<float> v = view<float>(l);
+    {
+      Launch k(h, CFMG_K_SWEEP, lev, CFMG_MIXED);
+      launch_smooth_tb3d(n, v.x, v.y, v.b, v.widiag, (float)(1.0 - h->d.omega), l.tx, l.ty, l.tz, l.nh,
+                         l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, l.nh, l.nz + l.nh + 1, h->stream);
+    }
+    l.xswap ^= 1;
+    left -= n;
+  }
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
 int smooth_tb(cfmg_handle* h, int lev, int nite) {
+  if (threed(h)) return smooth_tb3d(h, lev, nite);
   Level& l = h->lv[lev - 1];
   const int stencil = h->d.op == CFMG_LAPLACIAN9 ? 9 : 5;
   TRY(flush(h));

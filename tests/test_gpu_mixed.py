@@ -98,7 +98,7 @@ def test_mixed_matches_fp64_oracle(name):
     assert err <= 1e-6, err
 
 
-@pytest.mark.parametrize("name", ["config1_256_centers_v", "config2_512_vertices_lap9_f"])
+@pytest.mark.parametrize("name", ["config1_256_centers_v", "config2_512_vertices_lap9_f", "3d_48_centers_v"])
 def test_temporal_blocking_is_bit_identical(name):
     """The temporally blocked FP32 smoother (all sweeps of a call in one
     shared-memory pass) must give the same FP32 fields as one kernel per
@@ -112,8 +112,9 @@ def test_temporal_blocking_is_bit_identical(name):
         mg.set_option("temporal_blocking", tb)
         shape = mg.shape(1)
         custom = _mask(base, shape, mkind)
-        mg.oper[1].msk = custom
-        cfmg.setup_operators(mg)
+        if custom is not None:
+            mg.oper[1].msk = custom
+            cfmg.setup_operators(mg)
         for lev in range(1, mg.nlevels + 1):
             for f in ("x", "y", "r", "b"):
                 cfmg.set_to_zero(mg, lev, f)
