@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--ninst", type=int, default=2048, help="config4 batch size")
     ap.add_argument("--no-tune", action="store_true", help="config4: F(2,2) without the autotuner")
     ap.add_argument("--host-loop", action="store_true",
-                    help="config4: the host repeats the batched iteration (a launch list for ncu)")
+                    help="the host repeats the solve iteration instead of one graph launch per solve (for the "
+                         "ncu launch list, which does not descend into conditional graph nodes)")
     ap.add_argument("--quick", action="store_true",
                     help="mixed form only: one warm-up and one timed solve (a short run for ncu)")
     return ap.parse_args()
@@ -193,6 +194,8 @@ def run_ours(args, rank, world, local):
     sp = stream.cuda_stream
     param, vmsk, noise = W.config2(args.n, nlevels=args.nlevels or W.CONFIG2_LEVELS)
     mgm, b = make_gmg(cfmg, param, vmsk, noise, "mixed", sp)
+    if args.host_loop:
+        mgm.set_option("host_loop", 1)
     if args.quick:
         cfmg.set_to_zero(mgm, 1, "x")
         cfmg.solve(mgm)
@@ -439,6 +442,8 @@ def run_3d(args, rank, world, local):
     n = args.n if args.n != 4096 else 512
     param, msk, noise = W.config3(n, n, n // 2, nlevels=args.nlevels or 8)
     mgm, b = make_gmg(cfmg, param, msk, noise, "mixed", sp, tol=tol, maxite=400)
+    if args.host_loop:
+        mgm.set_option("host_loop", 1)
 
     def solve(mg):
         cfmg.set_to_zero(mg, 1, "x")

@@ -241,7 +241,8 @@ class Gmg:
         run in the coarse-level program engine; 0 turns it off),
         ``temporal_blocking`` (3 packed passes, 1 scalar passes, 0 off),
         ``coarsest_fp64`` (-1 auto, 0, 1), ``int_residual`` (1 fixed-point
-        level-1 residual of the mixed loop, 0 FP64 arithmetic)."""
+        level-1 residual of the mixed loop, 0 FP64 arithmetic), ``host_loop``
+        (1: the solve loop iterates from the host, one graph per iteration)."""
         self._check(self._L.cfmg_set_option(self._h, _lib.OPTIONS[name], int(value)))
 
     def set_stream(self, stream_ptr: Optional[int]):

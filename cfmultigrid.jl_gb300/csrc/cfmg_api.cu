@@ -62,6 +62,7 @@ struct cfmg_handle {
   int8_t* dq = nullptr;
   bool int_ok = false;
   bool int_on = true;
+  bool host_loop = false;  // CFMG_OPT_HOST_LOOP
   bool record = false;  // emit() records every Op (whole-solve programs) instead of running it
   bool record_tb = false;  // while recording: temporally blocked smoothing is recorded as OPK_TB Ops
 };
@@ -1643,7 +1644,7 @@ int cfmg_solve(cfmg_handle* h, double* res_out, int* nite_out, double* history) 
   } else {
     TRY(normresidual_dev(h, d.norm_kind));
   }
-  if (h->prof_cls < 0) {
+  if (h->prof_cls < 0 && !h->host_loop) {
     // the whole loop as one graph launch; the history comes back at the end
     cudaGraphExec_t sg = nullptr;
     TRY(get_solve_graph(h, prec, d.cycle, d.norm_kind, &sg));
@@ -2298,6 +2299,10 @@ int cfmg_set_option(cfmg_handle* h, int option, long long value) {
   if (option == CFMG_OPT_INT_RESIDUAL) {
     h->int_on = value != 0;
     drop_graphs(h);
+    return CFMG_OK;
+  }
+  if (option == CFMG_OPT_HOST_LOOP) {
+    h->host_loop = value != 0;
     return CFMG_OK;
   }
   if (option == CFMG_OPT_ENGINE_CELLS) {

@@ -47,8 +47,23 @@ __global__ void __launch_bounds__(kT3dThreads, 1) k_smooth_tb3d(const float* __r
   auto lvl = [&](int s, int p) { return LV + (s * 3 + ((p % 3) + 3) % 3) * kT3dPlane; };
   auto ring = [&](float* R, int p) { return R + (((p % (S + 1)) + (S + 1)) % (S + 1)) * kT3dPlane; };
   // the thread's cells: c = threadIdx.x + e * kT3dThreads, (li, lj) = (c % W, c / W)
+  // Plane p+1 is read from global memory into registers while the levels of
+  // step p compute, and stored to shared memory at the start of step p+1.
+  float rx[kT3dCells], rb[kT3dCells], rw[kT3dCells];
+  auto fetch = [&](int p) {
+#pragma unroll
+    for (int e = 0; e < kT3dCells; ++e) {
+      const int c = threadIdx.x + e * kT3dThreads;
+      const int gi = ti0 + c % kT3dW, gj = tj0 + c / kT3dW;
+      const bool in = gi >= 1 && gi <= tx && gj >= 1 && gj <= ty && p >= 1 && p <= tz;
+      const long long I = (long long)(gi - 1) + n1 * (gj - 1) + n2 * (p - 1);
+      rx[e] = in ? x[I] : 0.f;
+      rb[e] = in ? b[I] : 0.f;
+      rw[e] = in ? w[I] : 0.f;
+    }
+  };
+  fetch(ka - S);
   for (int p = ka - S; p <= kb + S; ++p) {
-    // load plane p of x (level 0), b and omega*idiag
     {
       float* X = lvl(0, p);
       float* Bp = ring(BR, p);
@@ -56,14 +71,12 @@ __global__ void __launch_bounds__(kT3dThreads, 1) k_smooth_tb3d(const float* __r
 #pragma unroll
       for (int e = 0; e < kT3dCells; ++e) {
         const int c = threadIdx.x + e * kT3dThreads;
-        const int gi = ti0 + c % kT3dW, gj = tj0 + c / kT3dW;
-        const bool in = gi >= 1 && gi <= tx && gj >= 1 && gj <= ty && p >= 1 && p <= tz;
-        const long long I = (long long)(gi - 1) + n1 * (gj - 1) + n2 * (p - 1);
-        X[c] = in ? x[I] : 0.f;
-        Bp[c] = in ? b[I] : 0.f;
-        Wp[c] = in ? w[I] : 0.f;
+        X[c] = rx[e];
+        Bp[c] = rb[e];
+        Wp[c] = rw[e];
       }
     }
+    if (p < kb + S) fetch(p + 1);
     __syncthreads();
     // level s at plane p - s, from level s-1 at planes p-s-1 .. p-s+1
 #pragma unroll

@@ -106,6 +106,9 @@ extern "C" {
 #define CFMG_OPT_INT_RESIDUAL 3 /* mixed form, closed topology, 5-, 7- and 2D 9-point operators: 1
                                    (default) computes the level-1 residual exactly in 64-bit fixed point
                                    on the integer pipes; 0 in FP64 arithmetic */
+#define CFMG_OPT_HOST_LOOP 4 /* cfmg_solve: 0 (default) runs the whole loop as one graph launch (a
+                                `while` node); 1 launches one graph per iteration from the host, which
+                                profilers that do not descend into conditional nodes can see */
 
 typedef struct cfmg_desc {
   int kase;     /* CFMG_TWOD / CFMG_THREED            (Param.case) */

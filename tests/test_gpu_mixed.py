@@ -163,3 +163,30 @@ def test_integer_residual_matches_fp64_residual(name):
     a = _wet_mean_removed(x1, w) if singular else x1 * w
     c = _wet_mean_removed(x0, w) if singular else x0 * w
     assert np.linalg.norm(a - c) <= 1e-8 * np.linalg.norm(c)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_solve_graph_matches_host_loop(precision):
+    """The whole solve! loop as one graph launch (a while node with the
+    stopping test on the device) gives the host-driven loop's history and
+    solution bit for bit."""
+    base, mkind = CASES["config1_256_centers_v"]
+    out = []
+    for host in (0, 1):
+        mg = cfmg.get_gmg(cfmg.Param(**base, tol=1e-10, maxite=40, residual_norm="l2", precision=precision,
+                                     verbose=False))
+        mg.oper[1].msk = _mask(base, mg.shape(1), mkind)
+        cfmg.setup_operators(mg)
+        for lev in range(1, mg.nlevels + 1):
+            for f in ("x", "y", "r", "b"):
+                cfmg.set_to_zero(mg, lev, f)
+        msk = mg.download(1, "msk").astype(np.float64)
+        b = np.asfortranarray(np.random.default_rng(3).standard_normal(mg.shape(1))) * msk
+        F.subtract_mean(b, msk)
+        mg.data[1].b = b
+        mg.set_option("host_loop", host)
+        res, n, hist = cfmg.solve(mg, history=True)
+        out.append((res, n, hist, mg.data[1].x))
+    assert out[0][1] == out[1][1] and out[0][0] == out[1][0]
+    assert np.array_equal(out[0][2], out[1][2])
+    assert np.array_equal(out[0][3], out[1][3])
