@@ -184,7 +184,7 @@ constexpr int kBChunk = 1024;
 constexpr int kBThreads = 256;
 // per-instance scalar block (double): see k_bfinal for their use
 enum BSlot { BS_NORMB = 0, BS_RES, BS_NITE, BS_NWET, BS_NEXT, BS_CUR, BS_ICUR, BS_MEAN, BS_T0, BS_T1, BS_ZEROX,
-             BS_MAXX, BS_MAXB, BS_HIST };
+             BS_MAXX, BS_MAXB, BS_SHIFT, BS_HIST };
 // level-1 state of one instance for the FP64 steps of its solve loop
 struct BInst {
   double *x, *b, *r, *d;
@@ -246,7 +246,7 @@ void launch_bcond(cudaGraphConditionalHandle hc, int* nactive, cudaStream_t s);
 // device scalars of a handle (dscal[])
 enum Scal { S_NORM = 0, S_RES = 1, S_NORMB = 2, S_NWET = 3, S_SCALE = 4, S_MEAN = 5, S_TMP0 = 6, S_ISCALE = 7,
             S_NEXT = 8, S_CUR = 9, S_ICUR = 10, S_MEAN2 = 11, S_MAXX = 12, S_MAXB = 13, S_NITE = 14,
-            S_COUNT = 16 };
+            S_SHIFT = 15, S_COUNT = 16 };
 
 // fused FP64 steps of the mixed loop (k_mixed.cu)
 void launch_resid_fused(int kind, double* r, const double* x, const double* b, const double* d, const uint8_t* m,

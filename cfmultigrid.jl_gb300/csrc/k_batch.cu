@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(kBThreads) k_brhs_shift(const BInst* __restric
     for (int q = 0; q < cnt; ++q) {
       const int4 en = tab[base + list[q]];
       const BInst& B = bi[en.x];
-      const float sh = (float)(B.sc[BS_MEAN] * B.sc[BS_CUR]);
+      const float sh = *reinterpret_cast<const float*>(B.sc + BS_SHIFT);  // (float)(mean * scale)
       const long long t0 = (long long)en.y * kBChunk + threadIdx.x;
       float f[U];
 #pragma unroll
@@ -415,6 +415,7 @@ __global__ void __launch_bounds__(kBThreads) k_bfinal(const BInst* __restrict__ 
     const double used = sc[BS_NEXT];
     sc[BS_CUR] = used;
     sc[BS_ICUR] = 1.0 / used;
+    *reinterpret_cast<float*>(sc + BS_SHIFT) = (float)(sc[BS_MEAN] * used);
     const double rms = sqrt(s2 / nw);
     int e = 0;
     if (rms > 0 && isfinite(rms)) frexp(rms, &e);
@@ -474,13 +475,13 @@ __global__ void __launch_bounds__(kBThreads) k_bupdate(const BInst* __restrict__
     for (int q = 0; q < cnt; ++q) {
       const int4 en = tab[base + list[q]];
       const BInst& B = bi[en.x];
-      const double is = B.sc[BS_ICUR];
+      const int pe = pow2_exponent(B.sc[BS_ICUR]);  // iscale = 2^pe
       const long long t0 = (long long)en.y * kBChunk + threadIdx.x;
       double xn[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const long long t = t0 + (long long)u * kBThreads;
-        if (t < B.len) xn[u] = __fma_rn((double)B.e32[t], is, B.x[t]);
+        if (t < B.len) xn[u] = __dadd_rn(B.x[t], f2d_pow2(B.e32[t], pe));
       }
       unsigned long long mx = 0;
 #pragma unroll

@@ -124,6 +124,8 @@ __global__ void __launch_bounds__(kMxParts) k_fused_final(const double* __restri
     if (rms > 0 && isfinite(rms)) frexp(rms, &e);
     ds[S_NEXT] = ldexp(1.0, -e);
     ds[S_MAXX] = 0.0;  // the next update collects max |x| afresh
+    // the wet mean in units of the right-hand side, as an FP32 value
+    *reinterpret_cast<float*>(ds + S_SHIFT) = (float)(ds[S_MEAN2] * used);
   }
 }
 
@@ -448,12 +450,12 @@ bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t
 }
 
 // cell-centred second pass: b32 = r32 = msk ? b32 - mean * scale : 0 with
-// ms[0] = S_MEAN2 and ms[1] = S_CUR
+// ms = ds + S_MEAN2 (the FP32 shift sits in S_SHIFT, made once by k_fused_final)
 __global__ void k_rhs32_shift(const uint8_t* __restrict__ m, const double* __restrict__ ms, float* __restrict__ b32,
                               float* __restrict__ r32, long long n) {
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= n) return;
-  const float sh = (float)(ms[0] * ms[S_CUR - S_MEAN2]);
+  const float sh = *reinterpret_cast<const float*>(ms + (S_SHIFT - S_MEAN2));  // (float)(mean * scale)
   const float f = m[I] ? __fsub_rn(b32[I], sh) : 0.f;
   b32[I] = f;
   r32[I] = f;
@@ -504,7 +506,7 @@ __global__ void k_maxabs2(const double* __restrict__ x, const double* __restrict
 __global__ void __launch_bounds__(kMxThreads) k_update_scaled_max(double* __restrict__ x, const float* __restrict__ e,
                                                                   const double* __restrict__ ds, long long n,
                                                                   double* dsw) {
-  const double is = ds[S_ICUR];
+  const int pe = pow2_exponent(ds[S_ICUR]);  // iscale = 2^pe
   unsigned long long mx = 0;
   const long long st = (long long)gridDim.x * blockDim.x;
   for (long long I0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; I0 < n; I0 += 4 * st) {
@@ -512,7 +514,7 @@ __global__ void __launch_bounds__(kMxThreads) k_update_scaled_max(double* __rest
 #pragma unroll
     for (int u = 0; u < 4; ++u) {  // loads of 4 cells in flight
       const long long I = I0 + u * st;
-      if (I < n) v[u] = __fma_rn((double)e[I], is, x[I]);
+      if (I < n) v[u] = __dadd_rn(x[I], f2d_pow2(e[I], pe));
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {

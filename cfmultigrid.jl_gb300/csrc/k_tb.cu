@@ -390,7 +390,7 @@ static void launch_tb3_n(const float* x, float* xo, const float* b, const float*
 template <int ST, int NITE>
 static void launch_tb_n(int version, const float* x, float* xo, const float* b, const float* w, float cff, int tx,
                         int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s) {
-  if (version == 3) {
+  if (version >= 3) {
     launch_tb3_n<ST, NITE>(x, xo, b, w, cff, tx, ty, nz, ui0, ui1, uj0, uj1, s);
     return;
   }

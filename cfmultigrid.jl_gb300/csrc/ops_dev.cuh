@@ -383,6 +383,24 @@ __device__ __forceinline__ long long to_fix(double v, int k) {
   return u < 0 ? -r : r;
 }
 
+// e * 2^p as a double, exactly, with integer operations on the bits of the
+// float (the FP64 pipe then only adds: x + e*2^p rounds once, as
+// fma((double)e, 2^p, x) does). Zero, subnormal, infinite and NaN e, and a
+// result outside the normal range, take the FP64 path.
+__device__ __forceinline__ double f2d_pow2(float e, int p) {
+  const unsigned u = __float_as_uint(e);
+  const int ex = (int)((u >> 23) & 0xffu);
+  const int dex = ex - 127 + 1023 + p;
+  if (ex == 0 || ex == 255 || dex <= 0 || dex >= 2047) return __dmul_rn((double)e, ldexp(1.0, p));
+  const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) | ((unsigned long long)dex << 52) |
+                                  ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+// the exponent p of a power of two 2^p held in a double
+__device__ __forceinline__ int pow2_exponent(double v) {
+  return (int)(((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ffULL) - 1023;
+}
+
 // ------------------------------------------------------------------ halo
 // fill! for :xperio (src/halo.jl:6-9) on one (j,k) line. Each statement's
 // right-hand columns are read before any is written, as Julia's sliced

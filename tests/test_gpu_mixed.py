@@ -105,7 +105,8 @@ def test_temporal_blocking_is_bit_identical(name):
     sweep, hence the same solve bit for bit."""
     base, mkind = CASES[name]
     out = []
-    for tb in (3, 1, 0):  # packed FP32x2 passes, scalar passes, one kernel per sweep
+    # packed FP32x2 passes (+ 3D streaming passes), scalar passes, one kernel per sweep
+    for tb in (4 if base.get("case") == "threed" else 3, 1, 0):
         mg = cfmg.get_gmg(cfmg.Param(**base, tol=1e-10, maxite=40, residual_norm="l2", precision="mixed",
                                      verbose=False))
         mg.set_option("engine_cells", 2000)  # keep the fine levels out of the engine
