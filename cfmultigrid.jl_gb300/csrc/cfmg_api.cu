@@ -2059,7 +2059,7 @@ int lockstep_build(cfmg_batch* b) {
       B.ncols = B.box.i1 - B.box.i0 + 1;
       B.nrows = B.box.j1 - B.box.j0 + 1;
     }
-    B.nstrips = (B.ncols + 31) / 32;
+    B.nstrips = (B.ncols + kBIntCols - 1) / kBIntCols;
     B.neumann = !vertices(h);
     B.norm_kind = h->d.norm_kind;
     B.maxite = h->d.maxite;

@@ -236,6 +236,7 @@ void launch_bfinal(const BInst* bi, const long long* cstart, int ninst, const do
                    int* nactive, cudaStream_t s);
 // integer residual: warp tasks {instance, strip, row chunk, 0}, partials 2 per task
 constexpr int kBIntRows = 32;
+constexpr int kBIntCols = 30;  // output columns of a warp strip (lanes 1..30)
 void launch_bres_int(int kind, bool neumann, const BInst* bi, const int4* ttab, long long ntasks, const int* active,
                      double* partials, cudaStream_t s);
 void launch_brhs_shift(const BInst* bi, const int4* tab, long long nchunks, const int* active, cudaStream_t s);

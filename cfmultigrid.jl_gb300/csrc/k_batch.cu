@@ -262,41 +262,30 @@ __global__ void __launch_bounds__(kBThreads) k_bres_int(const BInst* __restrict_
     const float fm = (float)ldexp(scale, -(k + q));
     const long long n1 = B.g.n1, len = B.len;
     const double* __restrict__ x = B.x;
-    const int c = B.c0 + en.y * 32 + lane;
-    const bool col_ok = c < B.c0 + B.ncols;
+    const int c = B.c0 + en.y * kBIntCols + lane - 1;  // lanes 1..30 own the strip
+    const bool col_ok = lane >= 1 && lane <= kBIntCols && c < B.c0 + B.ncols;
     const int ra = en.z * kBIntRows, rb = min(ra + kBIntRows, B.nrows);
     auto at = [&](long long J) { return x[J < 0 ? 0 : (J >= len ? len - 1 : J)]; };
-    auto raw = [&](long long Ir, double& xc, double& xe) {
-      xc = at(Ir);
-      xe = at(lane == 0 ? Ir - 1 : (lane == 31 ? Ir + 1 : Ir));
-    };
-    auto conv_row = [&](double xc, double xev, long long& W, long long& C, long long& E) {
+    auto conv_row = [&](double xc, long long& W, long long& C, long long& E) {
       C = to_fix(xc, k);
-      const long long xe = to_fix(xev, k);
       W = __shfl_up_sync(0xffffffffu, C, 1);
       E = __shfl_down_sync(0xffffffffu, C, 1);
-      if (lane == 0) W = xe;
-      if (lane == 31) E = xe;
     };
     long long I = B.row0 + (long long)ra * n1 + c;
     long long Wm, Cm, Em, W0, C0, E0, Wp, Cp, Ep;
-    double rc, re;
-    raw(I - n1, rc, re);
-    conv_row(rc, re, Wm, Cm, Em);
-    raw(I, rc, re);
-    conv_row(rc, re, W0, C0, E0);
-    double nc, ne;  // one row of look-ahead (see k_resid_int2d)
-    raw(I + n1, nc, ne);
+    conv_row(at(I - n1), Wm, Cm, Em);
+    conv_row(at(I), W0, C0, E0);
+    double nc = at(I + n1);  // one row of look-ahead (see k_resid_int2d)
     double nb = col_ok ? B.b[I] : 0.0;
     int nd = col_ok ? B.dq[I] : -1;
     float hi = 0.f, lo = 0.f;
     __int128 s1 = 0;
     for (int r = ra; r < rb; ++r, I += n1) {
-      conv_row(nc, ne, Wp, Cp, Ep);
+      conv_row(nc, Wp, Cp, Ep);
       const double cb = nb;
       const int d = nd;
       if (r + 1 < rb) {
-        raw(I + 2 * n1, nc, ne);
+        nc = at(I + 2 * n1);
         nb = col_ok ? B.b[I + n1] : 0.0;
         nd = col_ok ? B.dq[I + n1] : -1;
       }
@@ -475,13 +464,14 @@ __global__ void __launch_bounds__(kBThreads) k_bupdate(const BInst* __restrict__
     for (int q = 0; q < cnt; ++q) {
       const int4 en = tab[base + list[q]];
       const BInst& B = bi[en.x];
-      const int pe = pow2_exponent(B.sc[BS_ICUR]);  // iscale = 2^pe
+      const double is = B.sc[BS_ICUR];
+      const int pe = pow2_exponent(is);  // iscale = 2^pe
       const long long t0 = (long long)en.y * kBChunk + threadIdx.x;
       double xn[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const long long t = t0 + (long long)u * kBThreads;
-        if (t < B.len) xn[u] = __dadd_rn(B.x[t], f2d_pow2(B.e32[t], pe));
+        if (t < B.len) xn[u] = __dadd_rn(B.x[t], f2d_pow2(B.e32[t], pe, is));
       }
       unsigned long long mx = 0;
 #pragma unroll

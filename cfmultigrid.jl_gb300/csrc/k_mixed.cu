@@ -252,16 +252,17 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int(const double* __restri
   }
 }
 
-// 2D levels (one layer): the same residual with every x converted once.
-// A warp owns a strip of 32 consecutive linear indices of a row and walks
-// down RH rows, keeping the converted rows j-1, j, j+1 in registers; the
-// west and east neighbours come from the adjacent lanes (lane 0 and lane
-// 31 convert the one value beyond the strip, x[I-1] and x[I+32], which is
-// also what the linear 5-point range needs at the ends of a row). The
+// Strips of rows (2D, and 3D plane by plane): the same residual with every
+// x converted once. A warp owns 30 consecutive linear indices of a row
+// (lanes 1..30; lanes 0 and 31 hold the values on either side, which at the
+// ends of a row are the wrap-around neighbours of the linear 5-point range)
+// and walks down the rows, keeping the converted rows j-1, j, j+1 in
+// registers; the west and east neighbours come from the adjacent lanes. The
 // residual norm is summed from the FP32 right-hand-side values f = r*scale
 // (exact squares via FMA, double-float accumulation per thread, FP64
 // across threads), so the FP64 pipe does one conversion a cell.
 constexpr int kIntRows = 32;  // rows per warp task
+constexpr int kIntCols = 30;  // output columns per warp strip
 
 struct StripSpace {
   long long len;   // array length
@@ -296,8 +297,10 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __rest
     const long long pt = task - plane * per_plane;
     const int strip = (int)(pt % sp.nstrips);
     const int chunk = (int)(pt / sp.nstrips);
-    const int c = sp.c0 + strip * 32 + lane;  // this lane's column
-    const bool col_ok = c < sp.c0 + sp.ncols;
+    // lanes 1..30 own the strip's 30 columns; lanes 0 and 31 hold the
+    // columns on either side, so every x is converted by exactly one lane
+    const int c = sp.c0 + strip * kIntCols + lane - 1;  // this lane's column
+    const bool col_ok = lane >= 1 && lane <= kIntCols && c < sp.c0 + sp.ncols;
     const int ra = chunk * kIntRows, rb = min(ra + kIntRows, sp.nrows);
     // rows ra-1 and ra
     long long I = sp.row0 + plane * sp.n2 + (long long)ra * sp.n1 + c;
@@ -305,30 +308,17 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __rest
     // rows above the first / below the last output row may reach past its
     // ends, where the values are never used
     auto at = [&](long long J) { return x[J < 0 ? 0 : (J >= sp.len ? sp.len - 1 : J)]; };
-    // raw loads of a row: x at this lane, and the one value beyond the strip
-    // for lanes 0 / 31 (others load their own x again)
-    auto raw = [&](long long Ir, double& xc, double& xe) {
-      xc = at(Ir);
-      xe = at(lane == 0 ? Ir - 1 : (lane == 31 ? Ir + 1 : Ir));
-    };
-    auto conv_row = [&](double xc, double xev, long long& W, long long& C, long long& E) {
+    auto conv_row = [&](double xc, long long& W, long long& C, long long& E) {
       C = to_fix(xc, k);
-      const long long xe = to_fix(xev, k);
       W = __shfl_up_sync(0xffffffffu, C, 1);
       E = __shfl_down_sync(0xffffffffu, C, 1);
-      if (lane == 0) W = xe;
-      if (lane == 31) E = xe;
     };
     long long Wm, Cm, Em, W0, C0, E0, Wp, Cp, Ep;
-    double rc, re;
-    raw(I - sp.n1, rc, re);
-    conv_row(rc, re, Wm, Cm, Em);
-    raw(I, rc, re);
-    conv_row(rc, re, W0, C0, E0);
+    conv_row(at(I - sp.n1), Wm, Cm, Em);
+    conv_row(at(I), W0, C0, E0);
     // one row of look-ahead: the raw x of row r+1 and b, dq of row r are in
     // flight while row r-1 is computed
-    double nc, ne;
-    raw(I + sp.n1, nc, ne);
+    double nc = at(I + sp.n1);
     double nb = col_ok ? b[I] : 0.0;
     int nd = col_ok ? dq[I] : -1;
     double nlo = 0.0, nhi = 0.0;  // 7-point: x of the planes below and above
@@ -337,11 +327,11 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __rest
       nhi = x[I + sp.n2];
     }
     for (int r = ra; r < rb; ++r, I += sp.n1) {
-      conv_row(nc, ne, Wp, Cp, Ep);
+      conv_row(nc, Wp, Cp, Ep);
       const double cb = nb, clo = nlo, chi = nhi;
       const int d = nd;
       if (r + 1 < rb) {
-        raw(I + 2 * sp.n1, nc, ne);
+        nc = at(I + 2 * sp.n1);
         nb = col_ok ? b[I + sp.n1] : 0.0;
         nd = col_ok ? dq[I + sp.n1] : -1;
         if (KIND == OPK_RESID7 && col_ok) {
@@ -433,7 +423,7 @@ bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t
     return false;
   }
   if (sp.nrows <= 0 || sp.ncols <= 0 || sp.nplanes <= 0) return false;
-  sp.nstrips = (sp.ncols + 31) / 32;
+  sp.nstrips = (sp.ncols + kIntCols - 1) / kIntCols;
 #define CFMG_INT2(K)                                                                                        \
   if (kind == K) {                                                                                          \
     if (neumann)                                                                                            \
@@ -506,7 +496,8 @@ __global__ void k_maxabs2(const double* __restrict__ x, const double* __restrict
 __global__ void __launch_bounds__(kMxThreads) k_update_scaled_max(double* __restrict__ x, const float* __restrict__ e,
                                                                   const double* __restrict__ ds, long long n,
                                                                   double* dsw) {
-  const int pe = pow2_exponent(ds[S_ICUR]);  // iscale = 2^pe
+  const double is = ds[S_ICUR];
+  const int pe = pow2_exponent(is);  // iscale = 2^pe
   unsigned long long mx = 0;
   const long long st = (long long)gridDim.x * blockDim.x;
   for (long long I0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; I0 < n; I0 += 4 * st) {
@@ -514,7 +505,7 @@ __global__ void __launch_bounds__(kMxThreads) k_update_scaled_max(double* __rest
 #pragma unroll
     for (int u = 0; u < 4; ++u) {  // loads of 4 cells in flight
       const long long I = I0 + u * st;
-      if (I < n) v[u] = __dadd_rn(x[I], f2d_pow2(e[I], pe));
+      if (I < n) v[u] = __dadd_rn(x[I], f2d_pow2(e[I], pe, is));
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {

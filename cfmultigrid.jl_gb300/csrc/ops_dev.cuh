@@ -385,13 +385,15 @@ __device__ __forceinline__ long long to_fix(double v, int k) {
 
 // e * 2^p as a double, exactly, with integer operations on the bits of the
 // float (the FP64 pipe then only adds: x + e*2^p rounds once, as
-// fma((double)e, 2^p, x) does). Zero, subnormal, infinite and NaN e, and a
-// result outside the normal range, take the FP64 path.
-__device__ __forceinline__ double f2d_pow2(float e, int p) {
+// fma((double)e, 2^p, x) does). Zeros keep their sign; subnormal, infinite
+// and NaN e, and a result outside the normal range, take the FP64 path
+// (s2p = 2^p as a double).
+__device__ __forceinline__ double f2d_pow2(float e, int p, double s2p) {
   const unsigned u = __float_as_uint(e);
+  if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)((unsigned long long)(u >> 31) << 63));
   const int ex = (int)((u >> 23) & 0xffu);
   const int dex = ex - 127 + 1023 + p;
-  if (ex == 0 || ex == 255 || dex <= 0 || dex >= 2047) return __dmul_rn((double)e, ldexp(1.0, p));
+  if (ex == 0 || ex == 255 || dex <= 0 || dex >= 2047) return __dmul_rn((double)e, s2p);
   const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) | ((unsigned long long)dex << 52) |
                                   ((unsigned long long)(u & 0x7fffffu) << 29);
   return __longlong_as_double((long long)bits);
