@@ -181,7 +181,9 @@ CFMG_API int cfmg_cycle(cfmg_handle* h, int kind);
 /* solve!(mg) (src/gmg_solver.jl:9-42) on the fields already on the device
  * (b and the x warm start of level 1), with desc.tol, desc.maxite,
  * desc.norm_kind and desc.precision. `history` (may be NULL) receives
- * maxite+1 entries: the residual after 0..nite cycles. */
+ * nite+1 entries (room for maxite+1): the residual after 0..nite cycles.
+ * The loop, its stopping test and the history run on the device in one
+ * graph launch (CFMG_OPT_HOST_LOOP = 1: one launch per iteration). */
 CFMG_API int cfmg_solve(cfmg_handle* h, double* res, int* nite, double* history);
 
 /* Adjoint solve: the backward pass of solve! (no counterpart in the
