@@ -636,8 +636,12 @@ def run_adjoint(args, rank, world, local):
     param, probs = W.config5(ninst=args.ninst if args.ninst != 2048 else 16, n=n)
     mg = cfmg.get_gmg(cfmg.Param(**param, tol=1e-12, maxite=80, residual_norm="l2", precision="mixed",
                                  verbose=False))
+    # the finite-difference check needs the loss far below its own differences:
+    # solves to 1e-14 there (x error ~ cond * tol) and a step of 1e-4
+    mgfd = cfmg.get_gmg(cfmg.Param(**param, tol=1e-14, maxite=120, residual_norm="l2", precision="mixed",
+                                   verbose=False))
 
-    def loss(msk, kap, b, xs):
+    def loss(msk, kap, b, xs, mg=mg):
         mg.oper[1].msk = msk
         mg.oper[1].kappa = kap
         cfmg.setup_operators(mg)
@@ -657,13 +661,14 @@ def run_adjoint(args, rank, world, local):
         (L0, gb, gk), m = loss(msk, kap, b, xs)
         times.append((time.perf_counter() - t) * 1e3)
         if k == 0:  # central finite differences along random directions, first instance
+            (_, gb, gk), m = loss(msk, kap, b, xs, mgfd)
             for _ in range(args.fd_dirs):
                 db = rng.standard_normal(b.shape) * m
                 db -= m * (db.sum() / m.sum())
                 dk = rng.standard_normal(b.shape) * m * 0.1
-                eps = 1e-5
-                lp = loss(msk, kap + eps * dk, b + eps * db, xs)[0][0]
-                lm = loss(msk, kap - eps * dk, b - eps * db, xs)[0][0]
+                eps = 1e-4
+                lp = loss(msk, kap + eps * dk, b + eps * db, xs, mgfd)[0][0]
+                lm = loss(msk, kap - eps * dk, b - eps * db, xs, mgfd)[0][0]
                 fd = (lp - lm) / (2 * eps)
                 an = float(np.sum(gb * db) + np.sum(gk * dk))
                 fd_err.append(abs(fd - an) / abs(an))
@@ -675,7 +680,8 @@ def run_adjoint(args, rank, world, local):
             "config": {"workload": f"config5: {len(probs)} x {n}^2 div(kappa grad x) = b, forward + adjoint + "
                                    f"dL/dkappa", "levels": mg.nlevels},
             "fd_check": {"directions": len(fd_err), "max_rel_err": max(fd_err) if fd_err else None,
-                         "bound": 1e-6}}
+                         "median_rel_err": float(np.median(fd_err)) if fd_err else None, "bound": 1e-6,
+                         "solve_tol": 1e-14, "step": 1e-4}}
 
 
 def dataclasses_replace(p, **kw):
