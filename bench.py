@@ -293,7 +293,7 @@ def run_ours(args, rank, world, local):
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "roofline_traffic.json")
     if os.path.exists(tpath) and args.n == 4096:
-        traffic = json.load(open(tpath)).get("k_smooth_tb3<9,3> level 1 config2 4096", {}).get("bytes")
+        traffic = json.load(open(tpath)).get("k_smooth_tb5<9,3> level 1 config2 4096", {}).get("bytes")
     # FP64 sweep of the drop-in: FP64-issue bound, reported beside it
     nl64, tl64 = profile(cfmg, mgd, "sweep", 1, "fp64", lambda: solve(mgd))
     ms_launch64 = tl64 / max(nl64, 1)
@@ -320,10 +320,10 @@ def run_ours(args, rank, world, local):
         "e2e": {"value": ms_e2e / world, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "wall_ms_per_step": wall_e2e},
         "gpu_launches": launches,
-        "roofline": {"kernel": "k_smooth_tb3<9,3>: packed FP32 9-point smoothing pass (6 Jacobi sweeps), level 1",
+        "roofline": {"kernel": "k_smooth_tb5<9,3>: packed FP32 9-point smoothing pass (6 Jacobi sweeps), level 1",
                      "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
-                     "traffic": traffic, "traffic_source": "ncu capture, profiles/k_smooth_tb3_config2_4096.md",
+                     "traffic": traffic, "traffic_source": "ncu capture, profiles/k_smooth_tb5_config2_4096.md",
                      "launches_timed": nl, "ms_per_launch": ms_launch,
                      "bytes_per_launch": bytes_per_launch, "sweeps_per_launch": sweeps_per_launch,
                      "effective_sweep_gbs": achieved * sweeps_per_launch},

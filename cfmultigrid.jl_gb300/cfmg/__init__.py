@@ -239,7 +239,8 @@ class Gmg:
     def set_option(self, name: str, value: int) -> None:
         """Tuning knobs: ``engine_cells`` (levels of at most this many cells
         run in the coarse-level program engine; 0 turns it off),
-        ``temporal_blocking`` (3 packed passes, 1 scalar passes, 0 off),
+        ``temporal_blocking`` (5 lean packed passes, 3 first packed form,
+        1 scalar passes, 0 off),
         ``coarsest_fp64`` (-1 auto, 0, 1), ``int_residual`` (1 fixed-point
         level-1 residual of the mixed loop, 0 FP64 arithmetic), ``host_loop``
         (1: the solve loop iterates from the host, one graph per iteration)."""

@@ -53,7 +53,7 @@ struct cfmg_handle {
   int pool_cap = 0, pool_used = 0;
   std::unordered_map<std::string, int> prog_cache;
   bool tb_on = true;  // temporally blocked FP32 smoothing on fine levels
-  int tb_version = 3;  // 3: packed FP32x2 passes, 1: scalar passes
+  int tb_version = 5;  // 5: lean packed FP32x2 passes, 3: first packed form, 1: scalar passes
   int coarsest_fp64 = -1;  // mixed form: -1 FP64 when the coarsest level is small, 0 never, 1 always
   // adjoint scratch (level-1 FP64 arrays, allocated on the first cfmg_adjoint)
   double *adj_x = nullptr, *adj_b = nullptr, *adj_gk = nullptr;
@@ -2293,7 +2293,8 @@ int cfmg_set_option(cfmg_handle* h, int option, long long value) {
     return CFMG_OK;
   }
   if (option == CFMG_OPT_TEMPORAL_BLOCKING) {
-    if (value < 0 || value > 4 || value == 2) return fail(h, CFMG_ERR_ARG, "temporal_blocking must be 0, 1, 3 or 4");
+    if (value < 0 || value > 5 || value == 2)
+      return fail(h, CFMG_ERR_ARG, "temporal_blocking must be 0, 1, 3, 4 or 5");
     h->tb_on = value != 0;
     if (value) h->tb_version = (int)value;
     drop_graphs(h);

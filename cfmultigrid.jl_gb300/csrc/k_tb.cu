@@ -312,6 +312,182 @@ __global__ void __launch_bounds__(kT3Tx * kT3Ty, 1) k_smooth_tb3(const float* __
                      (int)blockIdx.z, smem);
 }
 
+// ---------------------------------------------------------------------
+// Lean packed form: the tb3 layout (even and odd planes per row) with pad
+// rows and pad columns, so that every shared load of a row is one base
+// register plus an immediate and no index is clamped; several rows per
+// thread; the sum (west + east) of each row formed once, where it starts
+// the faces of the row as centre, ((W + E) + S) + N, and the diagonals of
+// the row as south neighbour, ((SW + SE) + NW) + NE; and b - s4 formed as
+// fma(s4, -1, b), whose product is exact. Tiles whose loaded region lies
+// inside U with 8-byte aligned pairs (all but the boundary tiles) load and
+// store through row pointers with 64-bit accesses and no per-cell tests.
+constexpr int kT5W = 128, kT5Tx = 64;
+constexpr int kT5Half = 66;              // one plane of a row: pad, 64 cells, pad
+constexpr int kT5Row = 2 * kT5Half;      // even plane then odd plane
+// one buffer of a TY x ROWS tile: pad row, TY*ROWS rows, pad row
+template <int TY, int ROWS>
+__host__ __device__ constexpr int t5_plane() { return (TY * ROWS + 2) * kT5Row; }
+
+template <int ST, int ROWS, bool ALL_U>
+__device__ __forceinline__ void tb5_sweep(const float* __restrict__ src, float* __restrict__ dst,
+                                          const float2 (&B)[ROWS], const float2 (&WT)[ROWS], float2 cff2,
+                                          unsigned inU) {
+  // src, dst: padded row r0 (tile row r0 - 1) at this thread's column k;
+  // even cell 2k at +1, odd cell 2k+1 at +kT5Half+1, the west neighbour of
+  // the even cell (odd 2k-1) at +kT5Half, the east neighbour of the odd
+  // cell (even 2k+2) at +2
+  float wv = src[kT5Half], av = src[1], bv = src[kT5Half + 1], ev = src[2];
+  float2 sm = p_add(make_float2(wv, av), make_float2(bv, ev)), Cm = make_float2(av, bv);
+  src += kT5Row;
+  wv = src[kT5Half]; av = src[1]; bv = src[kT5Half + 1]; ev = src[2];
+  float2 s0 = p_add(make_float2(wv, av), make_float2(bv, ev)), C0 = make_float2(av, bv);
+#pragma unroll
+  for (int r = 0; r < ROWS; ++r) {
+    src += kT5Row;
+    wv = src[kT5Half]; av = src[1]; bv = src[kT5Half + 1]; ev = src[2];
+    const float2 Cp = make_float2(av, bv), NWp = make_float2(wv, av), NEp = make_float2(bv, ev);
+    // faces ((W + E) + S) + N, S = row j-1
+    float2 f = p_add(s0, Cm);
+    f = p_add(f, Cp);
+    float2 t;
+    if (ST == 5) {
+      t = p_fma(f, make_float2(-1.f, -1.f), B[r]);  // b - s4
+    } else {
+      // diagonals in the order (i-1,j-1), (i+1,j-1), (i-1,j+1), (i+1,j+1)
+      float2 d = p_add(sm, NWp);
+      d = p_add(d, NEp);
+      t = p_fma(f, make_float2(-0.5f, -0.5f), B[r]);
+      t = p_fma(d, make_float2(-0.25f, -0.25f), t);
+    }
+    // cff*c - w*t: the two products packed, their difference in scalar
+    const float2 m1 = p_mul(cff2, C0), m2 = p_mul(WT[r], t);
+    float2 o = make_float2(__fsub_rn(m1.x, m2.x), __fsub_rn(m1.y, m2.y));
+    if (!ALL_U) {
+      if (!(inU >> (2 * r) & 1u)) o.x = C0.x;
+      if (!(inU >> (2 * r + 1) & 1u)) o.y = C0.y;
+    }
+    dst += kT5Row;
+    dst[1] = o.x;
+    dst[kT5Half + 1] = o.y;
+    sm = s0; Cm = C0;
+    s0 = p_add(NWp, NEp);
+    C0 = Cp;
+  }
+}
+
+template <int ST, int NITE, int TY, int ROWS, int MINB>
+__global__ void __launch_bounds__(kT5Tx * TY, MINB) k_smooth_tb5(const float* __restrict__ x, float* __restrict__ xo,
+                                                                 const float* __restrict__ b,
+                                                                 const float* __restrict__ w, float cff, int tx,
+                                                                 int ty, int ui0, int ui1, int uj0, int uj1) {
+  extern __shared__ float smem[];
+  constexpr int H = 2 * NITE, TH = TY * ROWS;
+  constexpr int CW = kT5W - 2 * H, CH = TH - 2 * H;
+  float* P0 = smem;
+  float* P1 = smem + t5_plane<TY, ROWS>();
+  const int lx = threadIdx.x;
+  const int r0 = threadIdx.y * ROWS;  // first tile row of this thread
+  const int ti0 = ui0 + (int)blockIdx.x * CW - H, tj0 = uj0 + (int)blockIdx.y * CH - H;  // tile origin (1-based)
+  const int gi0 = ti0 + 2 * lx;  // global column of the even cell
+  // linear index of the thread's even cell in its first row (may lie
+  // outside the array for boundary tiles: used only under the bounds tests)
+  const long long I0 = (long long)tx * ty * blockIdx.z + (long long)(gi0 - 1) + (long long)tx * (tj0 + r0 - 1);
+  const bool tile_in_u = ti0 >= ui0 && ti0 + kT5W - 1 <= ui1 && tj0 >= uj0 && tj0 + TH - 1 <= uj1;
+  // the parity of I0 is the same for every thread of the tile
+  const bool fast = tile_in_u && ((I0 | tx) & 1) == 0;
+  float2 B[ROWS], WT[ROWS];
+  unsigned inU = ~0u;  // bit 2r + e: cell in U
+  float* prow = P0 + (r0 + 1) * kT5Row + lx;  // padded row r0 + 1 = tile row r0
+  if (fast) {
+    const float2* xp = reinterpret_cast<const float2*>(x + I0);
+    const float2* bp = reinterpret_cast<const float2*>(b + I0);
+    const float2* wp = reinterpret_cast<const float2*>(w + I0);
+    const int st = tx >> 1;
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+      const float2 v = __ldg(xp + r * st);
+      B[r] = __ldg(bp + r * st);
+      WT[r] = __ldg(wp + r * st);
+      prow[r * kT5Row + 1] = v.x;
+      prow[r * kT5Row + kT5Half + 1] = v.y;
+    }
+  } else {
+    inU = 0;
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+      const int gj = tj0 + r0 + r;
+      const bool row_in = gj >= 1 && gj <= ty, row_u = gj >= uj0 && gj <= uj1;
+      float v[2], bb[2], ww[2];
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int gi = gi0 + e;
+        const bool in = row_in && gi >= 1 && gi <= tx;
+        const long long I = I0 + (long long)r * tx + e;
+        v[e] = in ? x[I] : 0.f;
+        bb[e] = in ? b[I] : 0.f;
+        ww[e] = in ? w[I] : 0.f;
+        if (row_u && gi >= ui0 && gi <= ui1) inU |= 1u << (2 * r + e);
+      }
+      prow[r * kT5Row + 1] = v[0];
+      prow[r * kT5Row + kT5Half + 1] = v[1];
+      B[r] = make_float2(bb[0], bb[1]);
+      WT[r] = make_float2(ww[0], ww[1]);
+    }
+  }
+  // zero the pads that are read: the pad rows, the even plane's east pad
+  // and the odd plane's west pad (values read only by the tile's edge cells)
+  if (threadIdx.y == 0) {
+    for (int c = lx; c < kT5Row; c += kT5Tx) {
+      P0[c] = P1[c] = 0.f;
+      P0[(TH + 1) * kT5Row + c] = P1[(TH + 1) * kT5Row + c] = 0.f;
+    }
+  }
+  if (lx < 2) {
+    const int c = kT5Half - 1 + lx;
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) P0[(r0 + r + 1) * kT5Row + c] = P1[(r0 + r + 1) * kT5Row + c] = 0.f;
+  }
+  __syncthreads();
+  const float2 cff2 = make_float2(cff, cff);
+  const int base = r0 * kT5Row + lx;
+#pragma unroll 1
+  for (int s = 0; s < 2 * NITE; ++s) {
+    const float* src = ((s & 1) ? P1 : P0) + base;
+    float* dst = ((s & 1) ? P0 : P1) + base;
+    if (tile_in_u)
+      tb5_sweep<ST, ROWS, true>(src, dst, B, WT, cff2, inU);
+    else
+      tb5_sweep<ST, ROWS, false>(src, dst, B, WT, cff2, inU);
+    __syncthreads();
+  }
+  // 2*NITE sweeps: the result is in P0; write the core cells of U
+  if (fast) {
+    // H is even: the pair's two cells are both core columns or neither
+    if (2 * lx >= H && 2 * lx < kT5W - H) {
+      float2* op = reinterpret_cast<float2*>(xo + I0);
+      const int st = tx >> 1;
+#pragma unroll
+      for (int r = 0; r < ROWS; ++r) {
+        const int lj = r0 + r;
+        if (lj >= H && lj < TH - H) op[r * st] = make_float2(prow[r * kT5Row + 1], prow[r * kT5Row + kT5Half + 1]);
+      }
+    }
+    return;
+  }
+#pragma unroll
+  for (int r = 0; r < ROWS; ++r) {
+    const int lj = r0 + r;
+    if (lj < H || lj >= TH - H) continue;
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int lc = 2 * lx + e;
+      if (lc >= H && lc < kT5W - H && (inU >> (2 * r + e) & 1u))
+        xo[I0 + (long long)r * tx + e] = prow[r * kT5Row + e * kT5Half + 1];
+    }
+  }
+}
+
 template <int ST, int NITE>
 __global__ void __launch_bounds__(kTbW * kTbTy, 1) k_smooth_tb(const float* __restrict__ x, float* __restrict__ xo,
                                                                const float* __restrict__ b,
@@ -387,9 +563,32 @@ static void launch_tb3_n(const float* x, float* xo, const float* b, const float*
   k_smooth_tb3<ST, NITE><<<grid, dim3(kT3Tx, kT3Ty, 1), smem, s>>>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1);
 }
 
+template <int ST, int NITE, int TY, int ROWS, int MINB>
+static void launch_tb5_n(const float* x, float* xo, const float* b, const float* w, float cff, int tx, int ty,
+                         int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s) {
+  constexpr int H = 2 * NITE;
+  constexpr int CW = kT5W - 2 * H, CH = TY * ROWS - 2 * H;
+  const size_t smem = 2 * (size_t)t5_plane<TY, ROWS>() * sizeof(float);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_smooth_tb5<ST, NITE, TY, ROWS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    attr = true;
+  }
+  dim3 grid((unsigned)((ui1 - ui0 + CW) / CW), (unsigned)((uj1 - uj0 + CH) / CH), (unsigned)nz);
+  k_smooth_tb5<ST, NITE, TY, ROWS, MINB>
+      <<<grid, dim3(kT5Tx, TY, 1), smem, s>>>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1);
+}
+
 template <int ST, int NITE>
 static void launch_tb_n(int version, const float* x, float* xo, const float* b, const float* w, float cff, int tx,
                         int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s) {
+  if (version >= 5) {
+    // 8 x 6 rows per tile, 2 CTAs per SM (measured best at 4096^2 down to
+    // the 262^2 coarsest level of 20 pairs, which runs as 99 tiles)
+    launch_tb5_n<ST, NITE, 8, 6, 2>(x, xo, b, w, cff, tx, ty, nz, ui0, ui1, uj0, uj1, s);
+    return;
+  }
   if (version >= 3) {
     launch_tb3_n<ST, NITE>(x, xo, b, w, cff, tx, ty, nz, ui0, ui1, uj0, uj1, s);
     return;

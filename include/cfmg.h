@@ -101,9 +101,11 @@ extern "C" {
                                     coarsest level holds at most 1/16 of CFMG_OPT_ENGINE_CELLS cells,
                                     0 never (FP32), 1 always */
 #define CFMG_OPT_TEMPORAL_BLOCKING 1 /* FP32 smoothing of fine 2D levels runs all sweeps of a call in
-                                        shared-memory passes: 3 (default) two columns per thread in packed
-                                        FP32x2 arithmetic, 1 one column per thread; 4 as 3, plus streaming
-                                        passes for 3D 7-point levels; 0: one kernel per sweep */
+                                        shared-memory passes: 5 (default) two columns per thread in packed
+                                        FP32x2 arithmetic with padded tiles and vector loads, 3 the first
+                                        packed form, 1 one column per thread; 4 as 3, plus streaming passes
+                                        for 3D 7-point levels; 0: one kernel per sweep. All give the same
+                                        bits. */
 #define CFMG_OPT_INT_RESIDUAL 3 /* mixed form, closed topology, 5-, 7- and 2D 9-point operators: 1
                                    (default) computes the level-1 residual exactly in 64-bit fixed point
                                    on the integer pipes; 0 in FP64 arithmetic */

@@ -105,8 +105,8 @@ def test_temporal_blocking_is_bit_identical(name):
     sweep, hence the same solve bit for bit."""
     base, mkind = CASES[name]
     out = []
-    # packed FP32x2 passes (+ 3D streaming passes), scalar passes, one kernel per sweep
-    for tb in (4 if base.get("case") == "threed" else 3, 1, 0):
+    # packed FP32x2 passes (lean and first form; 3D: + streaming passes), scalar passes, one kernel per sweep
+    for tb in ((4, 1, 0) if base.get("case") == "threed" else (5, 3, 1, 0)):
         mg = cfmg.get_gmg(cfmg.Param(**base, tol=1e-10, maxite=40, residual_norm="l2", precision="mixed",
                                      verbose=False))
         mg.set_option("engine_cells", 2000)  # keep the fine levels out of the engine
@@ -125,7 +125,7 @@ def test_temporal_blocking_is_bit_identical(name):
         mg.data[1].b = b
         res, n, hist = cfmg.solve(mg, history=True)
         out.append((hist, mg.data[1].x))
-    for k in (1, 2):
+    for k in range(1, len(out)):
         assert np.array_equal(out[0][0], out[k][0]), k
         assert np.array_equal(out[0][1], out[k][1]), k
 
