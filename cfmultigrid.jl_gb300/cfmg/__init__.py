@@ -243,7 +243,9 @@ class Gmg:
         1 scalar passes, 0 off),
         ``coarsest_fp64`` (-1 auto, 0, 1), ``int_residual`` (1 fixed-point
         level-1 residual of the mixed loop, 0 FP64 arithmetic), ``host_loop``
-        (1: the solve loop iterates from the host, one graph per iteration)."""
+        (1: the solve loop iterates from the host, one graph per iteration),
+        ``fused_descent`` (1: the last pre-smoothing pass of a descent step
+        also forms and restricts the residual, 0: separate kernels)."""
         self._check(self._L.cfmg_set_option(self._h, _lib.OPTIONS[name], int(value)))
 
     def set_stream(self, stream_ptr: Optional[int]):

@@ -53,6 +53,7 @@ struct cfmg_handle {
   int pool_cap = 0, pool_used = 0;
   std::unordered_map<std::string, int> prog_cache;
   bool tb_on = true;  // temporally blocked FP32 smoothing on fine levels
+  bool fuse_on = true;  // V-cycle descent: residual and restriction in the last pre-smoothing pass
   int tb_version = 5;  // 5: lean packed FP32x2 passes, 3: first packed form, 1: scalar passes
   int coarsest_fp64 = -1;  // mixed form: -1 FP64 when the coarsest level is small, 0 never, 1 always
   // adjoint scratch (level-1 FP64 arrays, allocated on the first cfmg_adjoint)
@@ -583,17 +584,64 @@ int coarsest_t<float>(cfmg_handle* h, int nite) {
 }
 
 // ------------------------------------------------------------------ cycles
+// One descent step of a cycle at lev: pre-smoothing, residual, restriction
+// of r to the coarse b, coarse x zeroed (src/gmg_cycles.jl:72-76). On FP32
+// levels smoothed in lean packed passes (2D, closed topology), the last
+// pass does the residual and the restriction in its epilogue.
+bool fused_descent_ok(const cfmg_handle* h, int lev) {
+  if (!h->fuse_on || h->record || h->tb_version != 5 || threed(h) || lev >= L(h)) return false;
+  if (h->d.op != CFMG_LAPLACIAN && h->d.op != CFMG_LAPLACIAN9) return false;
+  return tb_eligible<float>(h, lev) && h->lv[lev - 1].tz == 1;
+}
+
+int smooth_tb_epi(cfmg_handle* h, int lev, int nite) {
+  Level& l = h->lv[lev - 1];
+  const Level& c = h->lv[lev];
+  const int stencil = h->d.op == CFMG_LAPLACIAN9 ? 9 : 5;
+  TRY(flush(h));
+  for (int left = nite; left > 0;) {
+    const int n = left > 3 ? 3 : left;
+    View<float> v = view<float>(l);
+    {
+      Launch k(h, CFMG_K_SWEEP, lev, CFMG_MIXED);
+      if (left > 3) {
+        launch_smooth_tb(h->tb_version, stencil, n, v.x, v.y, v.b, v.widiag, (float)(1.0 - h->d.omega), l.tx, l.ty,
+                         l.tz, l.nh, l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, h->stream);
+      } else {
+        const View<float> vc = view<float>(c);
+        const Box in = interior(l), cin = interior(c);
+        TbEpi ep;
+        ep.d = v.diag; ep.m = l.msk; ep.rcoef = vc.Rcoef; ep.bc = vc.b; ep.xc = vc.x;
+        ep.ri0 = in.i0; ep.ri1 = in.i1; ep.rj0 = in.j0; ep.rj1 = in.j1;
+        ep.nh = c.nh; ep.ctx = c.tx;
+        ep.ci0 = cin.i0; ep.ci1 = cin.i1; ep.cj0 = cin.j0; ep.cj1 = cin.j1;
+        ep.pkind = vertices(h) ? 2 : 0;
+        launch_smooth_tb_epi(stencil, n, v.x, v.y, v.b, v.widiag, (float)(1.0 - h->d.omega), l.tx, l.ty, l.nh,
+                             l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, ep, h->stream);
+      }
+    }
+    l.xswap ^= 1;
+    left -= n;
+  }
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
+template <class T>
+int descend_t(cfmg_handle* h, int lev, int nite) {
+  if (sizeof(T) == 4 && fused_descent_ok(h, lev)) return smooth_tb_epi(h, lev, nite);
+  TRY(smooth_t<T>(h, lev, nite));
+  TRY(residual_t<T>(h, lev));
+  TRY(restrict_t<T>(h, lev, CFMG_R));
+  return zero_t<T>(h, lev + 1, CFMG_X);
+}
+
 // vcycle! (src/gmg_cycles.jl:67-83)
 template <class T>
 int vcycle_t(cfmg_handle* h, int lev0) {
   const cfmg_desc& d = h->d;
   const int nl = L(h);
-  for (int lev = lev0; lev <= nl - 1; ++lev) {
-    TRY(smooth_t<T>(h, lev, d.npre));
-    TRY(residual_t<T>(h, lev));
-    TRY(restrict_t<T>(h, lev, CFMG_R));
-    TRY(zero_t<T>(h, lev + 1, CFMG_X));
-  }
+  for (int lev = lev0; lev <= nl - 1; ++lev) TRY(descend_t<T>(h, lev, d.npre));
   TRY(coarsest_t<T>(h, d.ndeepest));
   for (int lev = nl - 1; lev >= lev0; --lev) {
     TRY(prolong_t<T>(h, lev));
@@ -631,21 +679,13 @@ int cycle_body(cfmg_handle* h, int kind) {
       return smooth_t<T>(h, 1, d.ndeepest);
     case CFMG_CYCLE_TWOLEV:  // twolevels! (src/gmg_cycles.jl:8-23)
       if (L(h) < 2) return fail(h, CFMG_ERR_ARG, "twolev cycle needs at least 2 levels");
-      TRY(smooth_t<T>(h, 1, d.npre));
-      TRY(residual_t<T>(h, 1));
-      TRY(restrict_t<T>(h, 1, CFMG_R));
-      TRY(zero_t<T>(h, 2, CFMG_X));
+      TRY(descend_t<T>(h, 1, d.npre));
       TRY(smooth_t<T>(h, 2, d.ndeepest));
       TRY(prolong_t<T>(h, 1));
       return smooth_t<T>(h, 1, d.npost);
     case CFMG_CYCLE_NLEV:  // nlevels! (src/gmg_cycles.jl:25-41), quirks kept
       if (L(h) < 3) return fail(h, CFMG_ERR_ARG, "nlev cycle needs at least 3 levels");
-      for (int lev = 1; lev <= 2; ++lev) {
-        TRY(smooth_t<T>(h, lev, d.npre));
-        TRY(residual_t<T>(h, lev));
-        TRY(restrict_t<T>(h, lev, CFMG_R));
-        TRY(zero_t<T>(h, lev + 1, CFMG_X));
-      }
+      for (int lev = 1; lev <= 2; ++lev) TRY(descend_t<T>(h, lev, d.npre));
       return smooth_t<T>(h, L(h), d.ndeepest);
     default:
       return fail(h, CFMG_ERR_ARG, "unknown cycle kind");
@@ -2307,6 +2347,11 @@ int cfmg_set_option(cfmg_handle* h, int option, long long value) {
   }
   if (option == CFMG_OPT_HOST_LOOP) {
     h->host_loop = value != 0;
+    return CFMG_OK;
+  }
+  if (option == CFMG_OPT_FUSED_DESCENT) {
+    h->fuse_on = value != 0;
+    drop_graphs(h);
     return CFMG_OK;
   }
   if (option == CFMG_OPT_ENGINE_CELLS) {

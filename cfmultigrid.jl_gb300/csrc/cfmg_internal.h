@@ -175,6 +175,26 @@ constexpr int kTbMaxPairs = 10;
 // version 3: two columns per thread in packed FP32x2 arithmetic; 1: one column per thread
 bool launch_smooth_tb(int version, int stencil, int nite, const float* x, float* xo, const float* b, const float* w,
                       float cff, int tx, int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s);
+// The last pass of a V-cycle's pre-smoothing with the step that follows it
+// in the same kernel (2D, single layer): the residual of the smoothed x,
+// restricted to the coarse b, and the coarse x zeroed at the same cells.
+// The residual box is the reference's for the operator (interior box for
+// the 9-point, all cells of rows 2..ty-1 for the 5-point range); r outside
+// it is 0, as in the level's r array.
+struct TbEpi {
+  const float* d;      // FP32 diag of the level
+  const uint8_t* m;    // mask of the level
+  const float* rcoef;  // FP32 Rcoef of the coarse level
+  float* bc;           // coarse b
+  float* xc;           // coarse x (current buffer)
+  int ri0, ri1, rj0, rj1;  // residual box (1-based, inclusive)
+  int nh;
+  int ctx;             // coarse row stride
+  int ci0, ci1, cj0, cj1;  // coarse interior box (1-based, inclusive)
+  int pkind;           // restriction: 0 cell centres (2 x 2 sum), 2 vertices (1-2-1 x 1-2-1)
+};
+bool launch_smooth_tb_epi(int stencil, int nite, const float* x, float* xo, const float* b, const float* w, float cff,
+                          int tx, int ty, int ui0, int ui1, int uj0, int uj1, const TbEpi& ep, cudaStream_t s);
 
 // ---- batched solver (k_batch.cu): independent 2D instances advance in
 // lockstep, one launch per step of the iteration for all of them. Every

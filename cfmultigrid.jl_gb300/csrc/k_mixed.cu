@@ -256,13 +256,23 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int(const double* __restri
 // x converted once. A warp owns 30 consecutive linear indices of a row
 // (lanes 1..30; lanes 0 and 31 hold the values on either side, which at the
 // ends of a row are the wrap-around neighbours of the linear 5-point range)
-// and walks down the rows, keeping the converted rows j-1, j, j+1 in
-// registers; the west and east neighbours come from the adjacent lanes. The
+// and walks down `rows` rows, keeping each converted row's centre and
+// west + east sum in registers; the west and east values come from the
+// adjacent lanes. Integer sums are exact, so each row's west + east sum
+// serves as the start of its faces (as centre row) and of the diagonals of
+// the rows above and below. The loop body covers 6 rows, so the rotation of
+// the row window (period 3) and of the load queue (period 2) costs no moves;
+// x is loaded two rows ahead, b and dq one row ahead of their use. The
 // residual norm is summed from the FP32 right-hand-side values f = r*scale
 // (exact squares via FMA, double-float accumulation per thread, FP64
-// across threads), so the FP64 pipe does one conversion a cell.
-constexpr int kIntRows = 32;  // rows per warp task
+// across threads), so the FP64 pipe does one conversion a cell. The grid is
+// one wave of warps, each taking several equal tasks.
+//
+// x is the level-1 array of the handle's arena. The lanes around the index
+// space read up to 31 elements before its start and after its end, into the
+// device scalars before it and into y after it; those values are not used.
 constexpr int kIntCols = 30;  // output columns per warp strip
+constexpr int kIntUnroll = 6;  // rows per loop body; rows per task is a multiple
 
 struct StripSpace {
   long long len;   // array length
@@ -271,7 +281,8 @@ struct StripSpace {
   int nplanes;     // planes of the index space (1 in 2D)
   int c0, ncols;   // columns of the index space: c0 .. c0+ncols-1 (0-based linear offsets in a row)
   int nrows;       // rows of the index space
-  int nstrips;     // ceil(ncols / 32)
+  int nstrips;     // ceil(ncols / kIntCols)
+  int rows;        // rows per warp task (a multiple of kIntUnroll)
   long long n1;
 };
 
@@ -287,9 +298,10 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __rest
   const int lane = threadIdx.x & 31;
   const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  const int nchunks = (sp.nrows + kIntRows - 1) / kIntRows;
+  const int nchunks = (sp.nrows + sp.rows - 1) / sp.rows;
   const long long per_plane = (long long)sp.nstrips * nchunks;
   const long long ntasks = per_plane * sp.nplanes;
+  const long long n1 = sp.n1;
   float hi = 0.f, lo = 0.f;  // double-float sum of f^2
   __int128 s1 = 0;
   for (long long task = warp0; task < ntasks; task += nwarps) {
@@ -301,68 +313,69 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __rest
     // columns on either side, so every x is converted by exactly one lane
     const int c = sp.c0 + strip * kIntCols + lane - 1;  // this lane's column
     const bool col_ok = lane >= 1 && lane <= kIntCols && c < sp.c0 + sp.ncols;
-    const int ra = chunk * kIntRows, rb = min(ra + kIntRows, sp.nrows);
-    // rows ra-1 and ra
-    long long I = sp.row0 + plane * sp.n2 + (long long)ra * sp.n1 + c;
-    // loads are clamped to the array: lanes past the index space and the
-    // rows above the first / below the last output row may reach past its
-    // ends, where the values are never used
-    auto at = [&](long long J) { return x[J < 0 ? 0 : (J >= sp.len ? sp.len - 1 : J)]; };
-    auto conv_row = [&](double xc, long long& W, long long& C, long long& E) {
-      C = to_fix(xc, k);
-      W = __shfl_up_sync(0xffffffffu, C, 1);
-      E = __shfl_down_sync(0xffffffffu, C, 1);
-    };
-    long long Wm, Cm, Em, W0, C0, E0, Wp, Cp, Ep;
-    conv_row(at(I - sp.n1), Wm, Cm, Em);
-    conv_row(at(I), W0, C0, E0);
-    // one row of look-ahead: the raw x of row r+1 and b, dq of row r are in
-    // flight while row r-1 is computed
-    double nc = at(I + sp.n1);
-    double nb = col_ok ? b[I] : 0.0;
-    int nd = col_ok ? dq[I] : -1;
-    double nlo = 0.0, nhi = 0.0;  // 7-point: x of the planes below and above
+    const int ra = chunk * sp.rows, rb = min(ra + sp.rows, sp.nrows);
+    const long long I0 = sp.row0 + plane * sp.n2 + (long long)ra * n1 + c;  // row ra, this lane
+    const double* xp = x + I0;
+    // rows ra-1 and ra converted; x of rows ra+1, ra+2 and b, dq of row ra in flight
+    long long Cm = to_fix(xp[-n1], k), C0 = to_fix(xp[0], k);
+    long long rsm = __shfl_up_sync(0xffffffffu, Cm, 1) + __shfl_down_sync(0xffffffffu, Cm, 1);
+    long long rs0 = __shfl_up_sync(0xffffffffu, C0, 1) + __shfl_down_sync(0xffffffffu, C0, 1);
+    double xa = xp[n1];
+    double xb = ra + 2 <= rb ? xp[2 * n1] : 0.0;
+    double ba = col_ok ? b[I0] : 0.0;
+    int da = col_ok ? dq[I0] : -1;
+    double za = 0.0, zb = 0.0;  // 7-point: x of the planes below and above, row ra
     if (KIND == OPK_RESID7 && col_ok) {
-      nlo = x[I - sp.n2];
-      nhi = x[I + sp.n2];
+      za = xp[-sp.n2];
+      zb = xp[sp.n2];
     }
-    for (int r = ra; r < rb; ++r, I += sp.n1) {
-      conv_row(nc, Wp, Cp, Ep);
-      const double cb = nb, clo = nlo, chi = nhi;
-      const int d = nd;
-      if (r + 1 < rb) {
-        nc = at(I + 2 * sp.n1);
-        nb = col_ok ? b[I + sp.n1] : 0.0;
-        nd = col_ok ? dq[I + sp.n1] : -1;
-        if (KIND == OPK_RESID7 && col_ok) {
-          nlo = x[I + sp.n1 - sp.n2];
-          nhi = x[I + sp.n1 + sp.n2];
-        }
-      }
-      if (col_ok) {
-        long long R = 0;
-        if (d >= 0) {
+    for (int r0 = ra; r0 < rb; r0 += kIntUnroll) {
+#pragma unroll
+      for (int u = 0; u < kIntUnroll; ++u) {
+        const int r = r0 + u;
+        if (r < rb) {  // uniform across the warp
+          const long long I = I0 + (long long)(r - ra) * n1;
+          // row r+1 converted; row r+3 of x and row r+1 of b, dq requested
+          const long long Cp = to_fix(xa, k);
+          const long long rsp = __shfl_up_sync(0xffffffffu, Cp, 1) + __shfl_down_sync(0xffffffffu, Cp, 1);
+          const double cb = ba, clo = za, chi = zb;
+          const int d = da;
+          xa = xb;
+          if (r + 3 <= rb) xb = x[I + 3 * n1];
+          if (r + 1 < rb) {
+            ba = col_ok ? b[I + n1] : 0.0;
+            da = col_ok ? dq[I + n1] : -1;
+            if (KIND == OPK_RESID7 && col_ok) {
+              za = x[I + n1 - sp.n2];
+              zb = x[I + n1 + sp.n2];
+            }
+          }
           const long long B = to_fix(cb, k);
+          long long R;
           if (KIND == OPK_RESID9)
-            R = (long long)d * C0 + 4 * B - 2 * (((W0 + E0) + Cm) + Cp) - (((Wm + Em) + Wp) + Ep);
+            R = (long long)d * C0 + 4 * B - 2 * (rs0 + Cm + Cp) - (rsm + rsp);
           else if (KIND == OPK_RESID7)
-            R = (long long)d * C0 + B - ((((W0 + E0) + Cm) + Cp) + (to_fix(clo, k) + to_fix(chi, k)));
+            R = (long long)d * C0 + B - (rs0 + Cm + Cp + to_fix(clo, k) + to_fix(chi, k));
           else
-            R = (long long)d * C0 + B - (((W0 + E0) + Cm) + Cp);
+            R = (long long)d * C0 + B - (rs0 + Cm + Cp);
+          R = d >= 0 ? R : 0LL;  // dry cells and lanes outside the strip
+          const float f = __fmul_rn(__ll2float_rn(R), fm);
+          if (col_ok) {
+            b32[I] = f;
+            if (!NEUMANN && r32) r32[I] = f;
+          }
+          if (NEUMANN) s1 += (__int128)R;
+          // p + e = f^2 exactly; (hi, lo) += p + e by TwoSum (explicit _rn
+          // operations: a contracted hi + f*f would break the error terms);
+          // f = 0 outside the strip adds exactly nothing
+          const float p = __fmul_rn(f, f), e = __fmaf_rn(f, f, -p);
+          const float sn = __fadd_rn(hi, p), bp = __fsub_rn(sn, hi);
+          lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(__fsub_rn(hi, __fsub_rn(sn, bp)), __fsub_rn(p, bp)), e));
+          hi = sn;
+          Cm = C0; rsm = rs0;
+          C0 = Cp; rs0 = rsp;
         }
-        const float f = __fmul_rn(__ll2float_rn(R), fm);
-        b32[I] = f;
-        if (NEUMANN) s1 += (__int128)R;
-        else if (r32) r32[I] = f;
-        // p + e = f^2 exactly; (hi, lo) += p + e by TwoSum (explicit _rn
-        // operations: a contracted hi + f*f would break the error terms)
-        const float p = __fmul_rn(f, f), e = __fmaf_rn(f, f, -p);
-        const float sn = __fadd_rn(hi, p), bp = __fsub_rn(sn, hi);
-        lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(__fsub_rn(hi, __fsub_rn(sn, bp)), __fsub_rn(p, bp)), e));
-        hi = sn;
       }
-      Wm = W0; Cm = C0; Em = E0;
-      W0 = Wp; C0 = Cp; E0 = Ep;
     }
   }
   // sum f^2 -> sum r^2 = sum f^2 / scale^2 (exact power of two)
@@ -391,7 +404,23 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __rest
     }
     partials[blockIdx.x] = u;
     partials[kMxParts + blockIdx.x] = v;
+    // the final pass reads kMxParts partials: the blocks clear the unused ones
+    for (int i = gridDim.x + blockIdx.x; i < kMxParts; i += gridDim.x) partials[i] = partials[kMxParts + i] = 0.0;
   }
+}
+
+template <int KIND, bool NEUMANN>
+static int int2d_grid() {
+  static int blocks = 0;  // one wave: resident blocks per SM x SMs, at most kMxParts
+  if (!blocks) {
+    int dev = 0, nsm = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_resid_int2d<KIND, NEUMANN>, kMxThreads, 0);
+    blocks = nsm * (per > 0 ? per : 1);
+    if (blocks > kMxParts || blocks <= 0) blocks = kMxParts;
+  }
+  return blocks;
 }
 
 bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t* dq, const Geom& g, const Box& bx,
@@ -426,10 +455,16 @@ bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t
   sp.nstrips = (sp.ncols + kIntCols - 1) / kIntCols;
 #define CFMG_INT2(K)                                                                                        \
   if (kind == K) {                                                                                          \
+    const int grid = neumann ? int2d_grid<K, true>() : int2d_grid<K, false>();                             \
+    /* about 4 tasks per warp of the wave, 6 to 96 rows each */                                             \
+    const long long warp_rows = (long long)sp.nstrips * sp.nrows * sp.nplanes;                              \
+    long long rows = warp_rows / (4LL * grid * (kMxThreads / 32));                                          \
+    rows = rows < kIntUnroll ? kIntUnroll : (rows > 96 ? 96 : rows);                                        \
+    sp.rows = (int)((rows + kIntUnroll - 1) / kIntUnroll * kIntUnroll);                                     \
     if (neumann)                                                                                            \
-      k_resid_int2d<K, true><<<kMxParts, kMxThreads, 0, s>>>(x, b, dq, sp, ds, b32, r32, partials);          \
+      k_resid_int2d<K, true><<<grid, kMxThreads, 0, s>>>(x, b, dq, sp, ds, b32, r32, partials);             \
     else                                                                                                    \
-      k_resid_int2d<K, false><<<kMxParts, kMxThreads, 0, s>>>(x, b, dq, sp, ds, b32, r32, partials);         \
+      k_resid_int2d<K, false><<<grid, kMxThreads, 0, s>>>(x, b, dq, sp, ds, b32, r32, partials);            \
     return true;                                                                                            \
   }
   CFMG_INT2(OPK_RESID5)

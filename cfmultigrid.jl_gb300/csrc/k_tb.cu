@@ -376,16 +376,66 @@ __device__ __forceinline__ void tb5_sweep(const float* __restrict__ src, float* 
   }
 }
 
-template <int ST, int NITE, int TY, int ROWS, int MINB>
+// Residual of the smoothed tile for the thread's cells (epilogue of a
+// pre-smoothing pass): r = msk * ((d*x + b) - s4) for the 5-point operator,
+// msk * fma(diags, -1/4, fma(s4, -1/2, d*x + b)) for the 9-point one, the
+// arithmetic of the reference's residual kernels; 0 outside the residual box.
+template <int ST, int ROWS>
+__device__ __forceinline__ void tb5_resid(const float* __restrict__ src, float* __restrict__ dst,
+                                          const float2 (&B)[ROWS], const float2* __restrict__ Ds,
+                                          const ushort* __restrict__ Ms, unsigned inbox) {
+  float wv = src[kT5Half], av = src[1], bv = src[kT5Half + 1], ev = src[2];
+  float2 sm = p_add(make_float2(wv, av), make_float2(bv, ev)), Cm = make_float2(av, bv);
+  src += kT5Row;
+  wv = src[kT5Half]; av = src[1]; bv = src[kT5Half + 1]; ev = src[2];
+  float2 s0 = p_add(make_float2(wv, av), make_float2(bv, ev)), C0 = make_float2(av, bv);
+#pragma unroll
+  for (int r = 0; r < ROWS; ++r) {
+    src += kT5Row;
+    wv = src[kT5Half]; av = src[1]; bv = src[kT5Half + 1]; ev = src[2];
+    const float2 Cp = make_float2(av, bv), NWp = make_float2(wv, av), NEp = make_float2(bv, ev);
+    float2 f = p_add(s0, Cm);
+    f = p_add(f, Cp);
+    const float2 dr = Ds[r * kT5Tx];
+    float2 v = make_float2(__fadd_rn(__fmul_rn(dr.x, C0.x), B[r].x), __fadd_rn(__fmul_rn(dr.y, C0.y), B[r].y));
+    if (ST == 5) {
+      v = make_float2(__fsub_rn(v.x, f.x), __fsub_rn(v.y, f.y));
+    } else {
+      float2 dg = p_add(sm, NWp);
+      dg = p_add(dg, NEp);
+      v = p_fma(f, make_float2(-0.5f, -0.5f), v);
+      v = p_fma(dg, make_float2(-0.25f, -0.25f), v);
+    }
+    const unsigned mr = Ms[r * kT5Tx];
+    const uint8_t m0 = (uint8_t)(mr & 0xffu), m1 = (uint8_t)(mr >> 8);
+    float rx = mask_mul(m0, v.x), ry = mask_mul(m1, v.y);
+    rx = (inbox >> (2 * r) & 1u) ? rx : 0.f;
+    ry = (inbox >> (2 * r + 1) & 1u) ? ry : 0.f;
+    dst += kT5Row;
+    dst[1] = rx;
+    dst[kT5Half + 1] = ry;
+    sm = s0; Cm = C0;
+    s0 = p_add(NWp, NEp);
+    C0 = Cp;
+  }
+}
+
+template <int ST, int NITE, int TY, int ROWS, int MINB, bool EPI>
 __global__ void __launch_bounds__(kT5Tx * TY, MINB) k_smooth_tb5(const float* __restrict__ x, float* __restrict__ xo,
                                                                  const float* __restrict__ b,
                                                                  const float* __restrict__ w, float cff, int tx,
-                                                                 int ty, int ui0, int ui1, int uj0, int uj1) {
+                                                                 int ty, int ui0, int ui1, int uj0, int uj1,
+                                                                 TbEpi ep) {
   extern __shared__ float smem[];
-  constexpr int H = 2 * NITE, TH = TY * ROWS;
+  // with the epilogue the core is 2 cells narrower: r is needed one cell
+  // beyond it, and x one cell beyond that
+  constexpr int H = 2 * NITE + (EPI ? 2 : 0), TH = TY * ROWS;
   constexpr int CW = kT5W - 2 * H, CH = TH - 2 * H;
   float* P0 = smem;
   float* P1 = smem + t5_plane<TY, ROWS>();
+  // epilogue only: diag and mask of the tile, one float2 / two bytes per thread and row
+  float2* Dsm = reinterpret_cast<float2*>(smem + 2 * t5_plane<TY, ROWS>());
+  ushort* Msm = reinterpret_cast<ushort*>(Dsm + TH * kT5Tx);
   const int lx = threadIdx.x;
   const int r0 = threadIdx.y * ROWS;  // first tile row of this thread
   const int ti0 = ui0 + (int)blockIdx.x * CW - H, tj0 = uj0 + (int)blockIdx.y * CH - H;  // tile origin (1-based)
@@ -411,6 +461,10 @@ __global__ void __launch_bounds__(kT5Tx * TY, MINB) k_smooth_tb5(const float* __
       WT[r] = __ldg(wp + r * st);
       prow[r * kT5Row + 1] = v.x;
       prow[r * kT5Row + kT5Half + 1] = v.y;
+      if constexpr (EPI) {
+        Dsm[(r0 + r) * kT5Tx + lx] = __ldg(reinterpret_cast<const float2*>(ep.d + I0) + r * st);
+        Msm[(r0 + r) * kT5Tx + lx] = __ldg(reinterpret_cast<const ushort*>(ep.m + I0) + r * st);
+      }
     }
   } else {
     inU = 0;
@@ -433,6 +487,20 @@ __global__ void __launch_bounds__(kT5Tx * TY, MINB) k_smooth_tb5(const float* __
       prow[r * kT5Row + kT5Half + 1] = v[1];
       B[r] = make_float2(bb[0], bb[1]);
       WT[r] = make_float2(ww[0], ww[1]);
+      if constexpr (EPI) {
+        float dd[2];
+        unsigned mm[2];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const int gi = gi0 + e;
+          const bool in = row_in && gi >= 1 && gi <= tx;
+          const long long I = I0 + (long long)r * tx + e;
+          dd[e] = in ? ep.d[I] : 0.f;
+          mm[e] = in ? ep.m[I] : 0u;
+        }
+        Dsm[(r0 + r) * kT5Tx + lx] = make_float2(dd[0], dd[1]);
+        Msm[(r0 + r) * kT5Tx + lx] = (ushort)(mm[0] | (mm[1] << 8));
+      }
     }
   }
   // zero the pads that are read: the pad rows, the even plane's east pad
@@ -460,6 +528,67 @@ __global__ void __launch_bounds__(kT5Tx * TY, MINB) k_smooth_tb5(const float* __
     else
       tb5_sweep<ST, ROWS, false>(src, dst, B, WT, cff2, inU);
     __syncthreads();
+  }
+  if constexpr (EPI) {
+    // residual of the smoothed x into P1 (free now), then its restriction.
+    // coarse cell (ii, jj) takes fine cell (2(ii-nh-1)+nh+1, likewise j) as
+    // its anchor; the thread owning an anchor in the core restricts it. Its
+    // Rcoef values are requested first, so that they arrive during the
+    // residual pass.
+    const int nh = ep.nh;
+    const int ea = (nh + 1 - ti0) & 1;  // anchor column within the thread's pair
+    const int lc = 2 * lx + ea, gi = ti0 + lc;
+    const int ii = ((gi - nh - 1) >> 1) + nh + 1;
+    const bool col_a = lc >= H && lc < kT5W - H && ii >= ep.ci0 && ii <= ep.ci1;
+    const int pr = (nh + 1 - tj0 - r0) & 1;  // anchor rows of the thread: r = pr, pr + 2, ...
+    float rc[ROWS];
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+      rc[r] = 0.f;
+      const int lj = r0 + r;
+      const int jj = ((tj0 + lj - nh - 1) >> 1) + nh + 1;
+      if (col_a && (r & 1) == pr && lj >= H && lj < TH - H && jj >= ep.cj0 && jj <= ep.cj1)
+        rc[r] = __ldg(ep.rcoef + (long long)(ii - 1) + (long long)ep.ctx * (jj - 1));
+    }
+    unsigned inbox = 0;
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+      const int gj = tj0 + r0 + r;
+      const bool row_in = gj >= ep.rj0 && gj <= ep.rj1;
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int gie = gi0 + e;
+        if (row_in && gie >= ep.ri0 && gie <= ep.ri1) inbox |= 1u << (2 * r + e);
+      }
+    }
+    tb5_resid<ST, ROWS>(P0 + base, P1 + base, B, Dsm + r0 * kT5Tx + lx, Msm + r0 * kT5Tx + lx, inbox);
+    __syncthreads();
+    if (col_a) {
+      auto R = [&](int lj, int c) { return P1[(lj + 1) * kT5Row + (c & 1) * kT5Half + (c >> 1) + 1]; };
+#pragma unroll
+      for (int r = 0; r < ROWS; ++r) {
+        if ((r & 1) != pr) continue;
+        const int lj = r0 + r;
+        const int jj = ((tj0 + lj - nh - 1) >> 1) + nh + 1;
+        if (lj < H || lj >= TH - H || jj < ep.cj0 || jj > ep.cj1) continue;
+        float sr;
+        if (ep.pkind == 2) {  // restriction_vertices!: 1-2-1 x 1-2-1, left fold
+          sr = __fmaf_rn(R(lj - 1, lc), 2.f, R(lj - 1, lc - 1));
+          sr = __fadd_rn(sr, R(lj - 1, lc + 1));
+          sr = __fmaf_rn(R(lj, lc - 1), 2.f, sr);
+          sr = __fmaf_rn(R(lj, lc), 4.f, sr);
+          sr = __fmaf_rn(R(lj, lc + 1), 2.f, sr);
+          sr = __fadd_rn(sr, R(lj + 1, lc - 1));
+          sr = __fmaf_rn(R(lj + 1, lc), 2.f, sr);
+          sr = __fadd_rn(sr, R(lj + 1, lc + 1));
+        } else {  // 2 x 2 block of cell centres
+          sr = __fadd_rn(__fadd_rn(__fadd_rn(R(lj, lc), R(lj, lc + 1)), R(lj + 1, lc)), R(lj + 1, lc + 1));
+        }
+        const long long C = (long long)(ii - 1) + (long long)ep.ctx * (jj - 1);
+        ep.bc[C] = __fmul_rn(rc[r], sr);
+        ep.xc[C] = 0.f;
+      }
+    }
   }
   // 2*NITE sweeps: the result is in P0; write the core cells of U
   if (fast) {
@@ -563,21 +692,22 @@ static void launch_tb3_n(const float* x, float* xo, const float* b, const float*
   k_smooth_tb3<ST, NITE><<<grid, dim3(kT3Tx, kT3Ty, 1), smem, s>>>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1);
 }
 
-template <int ST, int NITE, int TY, int ROWS, int MINB>
+template <int ST, int NITE, int TY, int ROWS, int MINB, bool EPI>
 static void launch_tb5_n(const float* x, float* xo, const float* b, const float* w, float cff, int tx, int ty,
-                         int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s) {
-  constexpr int H = 2 * NITE;
+                         int nz, int ui0, int ui1, int uj0, int uj1, const TbEpi& ep, cudaStream_t s) {
+  constexpr int H = 2 * NITE + (EPI ? 2 : 0);
   constexpr int CW = kT5W - 2 * H, CH = TY * ROWS - 2 * H;
-  const size_t smem = 2 * (size_t)t5_plane<TY, ROWS>() * sizeof(float);
+  const size_t smem = 2 * (size_t)t5_plane<TY, ROWS>() * sizeof(float) +
+                      (EPI ? (size_t)TY * ROWS * kT5Tx * (sizeof(float2) + sizeof(ushort)) : 0);
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_smooth_tb5<ST, NITE, TY, ROWS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_smooth_tb5<ST, NITE, TY, ROWS, MINB, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
     attr = true;
   }
   dim3 grid((unsigned)((ui1 - ui0 + CW) / CW), (unsigned)((uj1 - uj0 + CH) / CH), (unsigned)nz);
-  k_smooth_tb5<ST, NITE, TY, ROWS, MINB>
-      <<<grid, dim3(kT5Tx, TY, 1), smem, s>>>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1);
+  k_smooth_tb5<ST, NITE, TY, ROWS, MINB, EPI>
+      <<<grid, dim3(kT5Tx, TY, 1), smem, s>>>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1, ep);
 }
 
 template <int ST, int NITE>
@@ -586,7 +716,7 @@ static void launch_tb_n(int version, const float* x, float* xo, const float* b, 
   if (version >= 5) {
     // 8 x 6 rows per tile, 2 CTAs per SM (measured best at 4096^2 down to
     // the 262^2 coarsest level of 20 pairs, which runs as 99 tiles)
-    launch_tb5_n<ST, NITE, 8, 6, 2>(x, xo, b, w, cff, tx, ty, nz, ui0, ui1, uj0, uj1, s);
+    launch_tb5_n<ST, NITE, 8, 6, 2, false>(x, xo, b, w, cff, tx, ty, nz, ui0, ui1, uj0, uj1, TbEpi{}, s);
     return;
   }
   if (version >= 3) {
@@ -619,6 +749,20 @@ bool launch_smooth_tb(int version, int stencil, int nite, const float* x, float*
   CFMG_TB(9, 1) CFMG_TB(9, 2) CFMG_TB(9, 3) CFMG_TB(9, 4) CFMG_TB(9, 5)
   CFMG_TB(9, 6) CFMG_TB(9, 7) CFMG_TB(9, 8) CFMG_TB(9, 9) CFMG_TB(9, 10)
 #undef CFMG_TB
+  return false;
+}
+
+bool launch_smooth_tb_epi(int stencil, int nite, const float* x, float* xo, const float* b, const float* w, float cff,
+                          int tx, int ty, int ui0, int ui1, int uj0, int uj1, const TbEpi& ep, cudaStream_t s) {
+  // 8 x 6 rows as the plain passes (64-row tiles measured slower: 15.1 against 14.3 ms per config-2 solve)
+#define CFMG_TBE(ST, N)                                                                              \
+  if (stencil == ST && nite == N) {                                                                  \
+    launch_tb5_n<ST, N, 8, 6, 2, true>(x, xo, b, w, cff, tx, ty, 1, ui0, ui1, uj0, uj1, ep, s);     \
+    return true;                                                                                     \
+  }
+  CFMG_TBE(5, 1) CFMG_TBE(5, 2) CFMG_TBE(5, 3)
+  CFMG_TBE(9, 1) CFMG_TBE(9, 2) CFMG_TBE(9, 3)
+#undef CFMG_TBE
   return false;
 }
 

@@ -366,20 +366,17 @@ __device__ __forceinline__ void d_prolong(T* xf, const T* x, const T* coef, cons
 
 // ------------------------------------------------------- fixed point
 // Integer form of the mixed loop's level-1 residual (k_mixed.cu, k_batch.cu).
-// round(v * 2^k) for |v| 2^k < 2^59; zero and subnormal v give 0
+// round(v * 2^k) for |v| 2^k < 2^59, ties away from zero; zero and
+// subnormal v give 0. Branch-free: with M = m << 10 (m the 53-bit
+// significand, v = m 2^(ex-1075)), round(m 2^sh) = ((M >> (t-1)) + 1) >> 1
+// for t = 10 - sh: the range bound keeps sh <= 5, so t >= 5, and t is
+// capped at 64, where the result is 0 as for any shift past the significand.
 __device__ __forceinline__ long long to_fix(double v, int k) {
   const long long u = __double_as_longlong(v);
   const int ex = (int)(((unsigned long long)u >> 52) & 0x7ffULL);
-  const long long m = (u & 0x000FFFFFFFFFFFFFLL) | 0x0010000000000000LL;
-  const int sh = ex - 1075 + k;  // v = m 2^(ex-1075)
-  long long r;
-  if (sh >= 0) {
-    r = m << sh;
-  } else {
-    const int s = -sh;  // round half up on the magnitude
-    r = s <= 64 ? ((m >> (s - 1)) + 1) >> 1 : 0;
-  }
-  r = ex ? r : 0;
+  const unsigned long long M = (((unsigned long long)u & 0x000FFFFFFFFFFFFFULL) | 0x0010000000000000ULL) << 10;
+  const int t = min(max(1085 - ex - k, 1), 64);
+  const long long r = ex ? (long long)(((M >> (t - 1)) + 1ULL) >> 1) : 0LL;
   return u < 0 ? -r : r;
 }
 

@@ -112,6 +112,10 @@ extern "C" {
 #define CFMG_OPT_HOST_LOOP 4 /* cfmg_solve: 0 (default) runs the whole loop as one graph launch (a
                                 `while` node); 1 launches one graph per iteration from the host, which
                                 profilers that do not descend into conditional nodes can see */
+#define CFMG_OPT_FUSED_DESCENT 5 /* mixed form, 2D closed topology, lean packed passes: 1 (default)
+                                    the last pre-smoothing pass of a cycle's descent step also forms
+                                    the residual, restricts it to the coarse b and zeroes the coarse x;
+                                    0 separate kernels. Both give the same bits. */
 
 typedef struct cfmg_desc {
   int kase;     /* CFMG_TWOD / CFMG_THREED            (Param.case) */

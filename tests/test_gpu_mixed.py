@@ -101,16 +101,21 @@ def test_mixed_matches_fp64_oracle(name):
 @pytest.mark.parametrize("name", ["config1_256_centers_v", "config2_512_vertices_lap9_f", "3d_48_centers_v"])
 def test_temporal_blocking_is_bit_identical(name):
     """The temporally blocked FP32 smoother (all sweeps of a call in one
-    shared-memory pass) must give the same FP32 fields as one kernel per
-    sweep, hence the same solve bit for bit."""
+    shared-memory pass), and its form whose last pre-smoothing pass also
+    forms and restricts the residual, must give the same FP32 fields as one
+    kernel per operator, hence the same solve bit for bit."""
     base, mkind = CASES[name]
     out = []
-    # packed FP32x2 passes (lean and first form; 3D: + streaming passes), scalar passes, one kernel per sweep
-    for tb in ((4, 1, 0) if base.get("case") == "threed" else (5, 3, 1, 0)):
+    # packed FP32x2 passes (lean form with and without the fused residual and
+    # restriction, first form; 3D: + streaming passes), scalar passes, one
+    # kernel per sweep
+    runs = ((4, 1), (1, 1), (0, 1)) if base.get("case") == "threed" else ((5, 1), (5, 0), (3, 1), (1, 1), (0, 1))
+    for tb, fuse in runs:
         mg = cfmg.get_gmg(cfmg.Param(**base, tol=1e-10, maxite=40, residual_norm="l2", precision="mixed",
                                      verbose=False))
         mg.set_option("engine_cells", 2000)  # keep the fine levels out of the engine
         mg.set_option("temporal_blocking", tb)
+        mg.set_option("fused_descent", fuse)
         shape = mg.shape(1)
         custom = _mask(base, shape, mkind)
         if custom is not None:
