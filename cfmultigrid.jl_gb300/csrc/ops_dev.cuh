@@ -385,15 +385,25 @@ __device__ __forceinline__ long long to_fix(double v, int k) {
 // fma((double)e, 2^p, x) does). Zeros keep their sign; subnormal, infinite
 // and NaN e, and a result outside the normal range, take the FP64 path
 // (s2p = 2^p as a double).
+// the FP64 product for the rare e that the bit assembly does not cover; out
+// of line, so that it stays a branch that only warps holding such an e take
+// (inline, the compiler predicates it and every cell pays the FP64 pipe)
+static __device__ __noinline__ double f2d_pow2_slow(float e, double s2p) { return __dmul_rn((double)e, s2p); }
 __device__ __forceinline__ double f2d_pow2(float e, int p, double s2p) {
+  // zero and normal e by integer operations on the bits, with no branch:
+  // a divergent branch here had the compiler issue the caller's FP64 add on
+  // both paths
   const unsigned u = __float_as_uint(e);
-  if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)((unsigned long long)(u >> 31) << 63));
+  const unsigned long long sgn = (unsigned long long)(u >> 31) << 63;
   const int ex = (int)((u >> 23) & 0xffu);
   const int dex = ex - 127 + 1023 + p;
-  if (ex == 0 || ex == 255 || dex <= 0 || dex >= 2047) return __dmul_rn((double)e, s2p);
-  const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) | ((unsigned long long)dex << 52) |
-                                  ((unsigned long long)(u & 0x7fffffu) << 29);
-  return __longlong_as_double((long long)bits);
+  const bool zero = (u & 0x7fffffffu) == 0u;
+  const bool normal = ex != 0 && ex != 255 && dex > 0 && dex < 2047;
+  const unsigned long long bits =
+      sgn | ((unsigned long long)(unsigned)dex << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
+  double v = __longlong_as_double((long long)(zero ? sgn : bits));
+  if (!zero && !normal) v = f2d_pow2_slow(e, s2p);
+  return v;
 }
 // the exponent p of a power of two 2^p held in a double
 __device__ __forceinline__ int pow2_exponent(double v) {

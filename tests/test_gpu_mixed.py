@@ -26,6 +26,17 @@ CASES = {
 }
 
 
+# larger cases for the bit-identity tests only (no oracle solve): several
+# waves of tiles per pass, so that an ordering fault between tiles shows
+BIG_CASES = {
+    "config2_2048_vertices_lap9_f": (dict(nx=2048, ny=2048, nz=1, case="twod", location="vertices",
+                                          operator="laplacian9", cycle="f", npre=3, npost=3, omega=0.8,
+                                          nlevels=5), "disk"),
+    "config1_1024_centers_v": (dict(nx=1024, ny=1024, nz=1, case="twod", cycle="v", npre=2, npost=2, omega=0.8,
+                                    nlevels=6), "disk"),
+}
+
+
 def _mask(p, shape, kind):
     if kind is None:
         return None
@@ -98,13 +109,14 @@ def test_mixed_matches_fp64_oracle(name):
     assert err <= 1e-6, err
 
 
-@pytest.mark.parametrize("name", ["config1_256_centers_v", "config2_512_vertices_lap9_f", "3d_48_centers_v"])
+@pytest.mark.parametrize("name", ["config1_256_centers_v", "config2_512_vertices_lap9_f", "3d_48_centers_v",
+                                  "config2_2048_vertices_lap9_f", "config1_1024_centers_v"])
 def test_temporal_blocking_is_bit_identical(name):
     """The temporally blocked FP32 smoother (all sweeps of a call in one
     shared-memory pass), and its form whose last pre-smoothing pass also
     forms and restricts the residual, must give the same FP32 fields as one
     kernel per operator, hence the same solve bit for bit."""
-    base, mkind = CASES[name]
+    base, mkind = {**CASES, **BIG_CASES}[name]
     out = []
     # packed FP32x2 passes (lean form with and without the fused residual and
     # restriction, first form; 3D: + streaming passes), scalar passes, one
