@@ -278,7 +278,9 @@ def run_ours(args, rank, world, local):
 
     # roofline: the level-1 FP32 smoothing pass of the mixed form (one
     # temporally blocked launch runs all 2*npre sweeps of a smoothing call),
-    # timed per launch with CUDA events on the library's stream in one solve
+    # timed per launch with CUDA events on the library's stream in one solve;
+    # the post-smoothing passes (the pre-smoothing ones are fused descent
+    # passes, reported beside it)
     nl, tl = profile(cfmg, mgm, "sweep", 1, "mixed", lambda: solve(mgm))
     g1 = mgm.levels[1]
     box_cells = (g1.nx + 2) * (g1.ny + 2) * g1.nz  # the update box U = [nh, nx+nh+1]^2
@@ -294,6 +296,16 @@ def run_ours(args, rank, world, local):
     tpath = os.path.join(ROOT, "profiles", "roofline_traffic.json")
     if os.path.exists(tpath) and args.n == 4096:
         traffic = json.load(open(tpath)).get("k_smooth_tb5<9,3> level 1 config2 4096", {}).get("bytes")
+    # the fused descent pass of level 1 (pre-smoothing + residual + restriction
+    # to level 2 + zeroed level-2 x): algorithmic bytes x, b, omega*idiag, diag
+    # read and x written (20 B), the mask (1 B) per fine cell, Rcoef read and
+    # b, x written (12 B) per coarse cell
+    nld, tld = profile(cfmg, mgm, "descent", 1, "mixed", lambda: solve(mgm))
+    g2 = mgm.levels[2]
+    coarse_cells = g2.nx * g2.ny * g2.nz
+    bytes_descent = 21.0 * box_cells + 12.0 * coarse_cells
+    ms_descent = tld / max(nld, 1)
+    ach_descent = bytes_descent / (ms_descent * 1e-3) / 1e9 if ms_descent > 0 else 0.0
     # FP64 sweep of the drop-in: FP64-issue bound, reported beside it
     nl64, tl64 = profile(cfmg, mgd, "sweep", 1, "fp64", lambda: solve(mgd))
     ms_launch64 = tl64 / max(nl64, 1)
@@ -327,6 +339,10 @@ def run_ours(args, rank, world, local):
                      "launches_timed": nl, "ms_per_launch": ms_launch,
                      "bytes_per_launch": bytes_per_launch, "sweeps_per_launch": sweeps_per_launch,
                      "effective_sweep_gbs": achieved * sweeps_per_launch},
+        "fused_descent": {"kernel": "k_smooth_tb5<9,3,...,EPI>: level-1 pre-smoothing pass with the residual, "
+                                    "its restriction and the zeroed coarse x",
+                          "launches_timed": nld, "ms_per_launch": ms_descent, "bytes_per_launch": bytes_descent,
+                          "achieved_gbs": ach_descent, "frac": ach_descent / hbm_peak},
         "roofline_fp64_sweep": {"kernel": "FP64 9-point Jacobi sweep, level 1 (drop-in)", "ms_per_launch": ms_launch64,
                                 "effective_gbs": ach64, "bound": "fp64 issue (DADD/DMUL at 506 Gop/s measured)"},
         "clocks": clocks,

@@ -40,7 +40,8 @@ OPTIONS = {"engine_cells": 0, "temporal_blocking": 1, "coarsest_fp64": 2, "int_r
            "fused_descent": 5}
 BATCH_OPTIONS = {"host_loop": 0}
 KERNEL_CLASSES = {"sweep": 0, "residual": 1, "restrict": 2, "prolong": 3, "norm": 4, "fill": 5, "convert": 6,
-                  "engine": 7}
+                  "engine": 7,
+                  "descent": 8}
 
 
 class Desc(ctypes.Structure):

@@ -603,7 +603,7 @@ int smooth_tb_epi(cfmg_handle* h, int lev, int nite) {
     const int n = left > 3 ? 3 : left;
     View<float> v = view<float>(l);
     {
-      Launch k(h, CFMG_K_SWEEP, lev, CFMG_MIXED);
+      Launch k(h, left > 3 ? CFMG_K_SWEEP : CFMG_K_DESCENT, lev, CFMG_MIXED);
       if (left > 3) {
         launch_smooth_tb(h->tb_version, stencil, n, v.x, v.y, v.b, v.widiag, (float)(1.0 - h->d.omega), l.tx, l.ty,
                          l.tz, l.nh, l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, h->stream);

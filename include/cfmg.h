@@ -92,6 +92,7 @@ extern "C" {
 #define CFMG_K_FILL 5
 #define CFMG_K_CONVERT 6  /* FP64 <-> FP32 transfers of the mixed form */
 #define CFMG_K_ENGINE 7   /* one launch of the coarse-level program engine */
+#define CFMG_K_DESCENT 8  /* a smoothing pass that also forms and restricts the residual (fused descent step) */
 
 /* options for cfmg_set_option */
 #define CFMG_OPT_ENGINE_CELLS 0 /* FP32 levels of at most this many cells (tx*ty*tz), FP64
