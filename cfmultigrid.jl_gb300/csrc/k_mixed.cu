@@ -329,54 +329,56 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __rest
       za = xp[-sp.n2];
       zb = xp[sp.n2];
     }
-    for (int r0 = ra; r0 < rb; r0 += kIntUnroll) {
-#pragma unroll
-      for (int u = 0; u < kIntUnroll; ++u) {
-        const int r = r0 + u;
-        if (r < rb) {  // uniform across the warp
-          const long long I = I0 + (long long)(r - ra) * n1;
-          // row r+1 converted; row r+3 of x and row r+1 of b, dq requested
-          const long long Cp = to_fix(xa, k);
-          const long long rsp = __shfl_up_sync(0xffffffffu, Cp, 1) + __shfl_down_sync(0xffffffffu, Cp, 1);
-          const double cb = ba, clo = za, chi = zb;
-          const int d = da;
-          xa = xb;
-          if (r + 3 <= rb) xb = x[I + 3 * n1];
-          if (r + 1 < rb) {
-            ba = col_ok ? b[I + n1] : 0.0;
-            da = col_ok ? dq[I + n1] : -1;
-            if (KIND == OPK_RESID7 && col_ok) {
-              za = x[I + n1 - sp.n2];
-              zb = x[I + n1 + sp.n2];
-            }
-          }
-          const long long B = to_fix(cb, k);
-          long long R;
-          if (KIND == OPK_RESID9)
-            R = (long long)d * C0 + 4 * B - 2 * (rs0 + Cm + Cp) - (rsm + rsp);
-          else if (KIND == OPK_RESID7)
-            R = (long long)d * C0 + B - (rs0 + Cm + Cp + to_fix(clo, k) + to_fix(chi, k));
-          else
-            R = (long long)d * C0 + B - (rs0 + Cm + Cp);
-          R = d >= 0 ? R : 0LL;  // dry cells and lanes outside the strip
-          const float f = __fmul_rn(__ll2float_rn(R), fm);
-          if (col_ok) {
-            b32[I] = f;
-            if (!NEUMANN && r32) r32[I] = f;
-          }
-          if (NEUMANN) s1 += (__int128)R;
-          // p + e = f^2 exactly; (hi, lo) += p + e by TwoSum (explicit _rn
-          // operations: a contracted hi + f*f would break the error terms);
-          // f = 0 outside the strip adds exactly nothing
-          const float p = __fmul_rn(f, f), e = __fmaf_rn(f, f, -p);
-          const float sn = __fadd_rn(hi, p), bp = __fsub_rn(sn, hi);
-          lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(__fsub_rn(hi, __fsub_rn(sn, bp)), __fsub_rn(p, bp)), e));
-          hi = sn;
-          Cm = C0; rsm = rs0;
-          C0 = Cp; rs0 = rsp;
+    // one row of the strip (r < rb): the rotation of the row window is the
+    // last step, so in the unguarded 6-row groups it costs no register moves
+    auto row_step = [&](int r) {
+      const long long I = I0 + (long long)(r - ra) * n1;
+      // row r+1 converted; row r+3 of x and row r+1 of b, dq requested
+      const long long Cp = to_fix(xa, k);
+      const long long rsp = __shfl_up_sync(0xffffffffu, Cp, 1) + __shfl_down_sync(0xffffffffu, Cp, 1);
+      const double cb = ba, clo = za, chi = zb;
+      const int d = da;
+      xa = xb;
+      if (r + 3 <= rb) xb = x[I + 3 * n1];
+      if (r + 1 < rb) {
+        ba = col_ok ? b[I + n1] : 0.0;
+        da = col_ok ? dq[I + n1] : -1;
+        if (KIND == OPK_RESID7 && col_ok) {
+          za = x[I + n1 - sp.n2];
+          zb = x[I + n1 + sp.n2];
         }
       }
+      const long long B = to_fix(cb, k);
+      long long R;
+      if (KIND == OPK_RESID9)
+        R = (long long)d * C0 + 4 * B - 2 * (rs0 + Cm + Cp) - (rsm + rsp);
+      else if (KIND == OPK_RESID7)
+        R = (long long)d * C0 + B - (rs0 + Cm + Cp + to_fix(clo, k) + to_fix(chi, k));
+      else
+        R = (long long)d * C0 + B - (rs0 + Cm + Cp);
+      R = d >= 0 ? R : 0LL;  // dry cells and lanes outside the strip
+      const float f = __fmul_rn(__ll2float_rn(R), fm);
+      if (col_ok) {
+        b32[I] = f;
+        if (!NEUMANN && r32) r32[I] = f;
+      }
+      if (NEUMANN) s1 += (__int128)R;
+      // p + e = f^2 exactly; (hi, lo) += p + e by TwoSum (explicit _rn
+      // operations: a contracted hi + f*f would break the error terms);
+      // f = 0 outside the strip adds exactly nothing
+      const float p = __fmul_rn(f, f), e = __fmaf_rn(f, f, -p);
+      const float sn = __fadd_rn(hi, p), bp = __fsub_rn(sn, hi);
+      lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(__fsub_rn(hi, __fsub_rn(sn, bp)), __fsub_rn(p, bp)), e));
+      hi = sn;
+      Cm = C0; rsm = rs0;
+      C0 = Cp; rs0 = rsp;
+    };
+    int r0 = ra;
+    for (; r0 + kIntUnroll <= rb; r0 += kIntUnroll) {
+#pragma unroll
+      for (int u = 0; u < kIntUnroll; ++u) row_step(r0 + u);
     }
+    for (; r0 < rb; ++r0) row_step(r0);
   }
   // sum f^2 -> sum r^2 = sum f^2 / scale^2 (exact power of two)
   const double s2d = ((double)hi + (double)lo) / (scale * scale);
