@@ -169,10 +169,11 @@ bool launch_smooth_tb3d(int nite, const float* x, float* xo, const float* b, con
 // temporally blocked FP32 smoother (k_tb.cu): nite pairs of 5- or 9-point
 // sweeps over the box U in one pass, x -> xo; false if nite is not
 // 1..kTbMaxPairs. A pass of p pairs recomputes a halo of 2p cells around each
-// 128 x 72 tile: 3 pairs suit large levels, longer passes cut the launches
-// of the many-pair coarsest solves.
+// tile: 3 pairs suit large levels, longer passes cut the launches of the
+// many-pair coarsest solves.
 constexpr int kTbMaxPairs = 10;
-// version 3: two columns per thread in packed FP32x2 arithmetic; 1: one column per thread
+// version 5: lean packed FP32x2 passes (128 x 48 tiles); 3 (and 4): the first
+// packed form; 1: one column per thread
 bool launch_smooth_tb(int version, int stencil, int nite, const float* x, float* xo, const float* b, const float* w,
                       float cff, int tx, int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s);
 // The last pass of a V-cycle's pre-smoothing with the step that follows it

@@ -3,13 +3,16 @@
 //
 // One smoothing call of the reference (nite pairs of sweeps,
 // src/laplacian.jl:95-112, src/laplacian9.jl:2-47) reads and writes the
-// whole level 2*nite times. Here a CTA loads 128 x 72 tiles of x, b and
-// omega*idiag into shared memory once, runs all
-// 2*nite sweeps on it, each sweep valid on a region one cell narrower than
-// the last, and writes the 128-2H x 72-2H core (H = 2*nite) to the
-// level's other x buffer: the tiles overlap, so the update cannot be in
-// place. HBM traffic drops from 16 B per cell and sweep to about 21 B per
-// cell for the whole call.
+// whole level 2*nite times. Here a CTA loads a tile of x, b and
+// omega*idiag once, runs all 2*nite sweeps on it in shared memory, each
+// sweep valid on a region one cell narrower than the last, and writes the
+// tile's core (a halo of H = 2*nite cells trimmed) to the level's other x
+// buffer: the tiles overlap, so the update cannot be in place. HBM traffic
+// drops from 16 B per cell and sweep to about 21 B per cell for the whole
+// call. Three forms: the lean packed form (k_smooth_tb5, 128 x 48 tiles,
+// the default, with an optional residual/restriction epilogue), the first
+// packed form (k_smooth_tb3, 128 x 64) and the scalar form (k_smooth_tb,
+// 128 x 72, also the batched solver's tile).
 //
 // Correctness rests on the mixed form's invariant: in the FP32 correction
 // fields every cell outside the wet interior holds 0 and has
