@@ -528,8 +528,8 @@ __global__ void k_maxabs2(const double* __restrict__ x, const double* __restrict
 }
 
 // x += e * iscale, with max |x| of the result into ds[S_MAXX] (reset by the
-// fused pass's final reduction): a fixed grid of kMxParts blocks, one
-// atomic per block
+// fused pass's final reduction): a grid-stride pass of 4 blocks per SM,
+// one atomic per block
 __global__ void __launch_bounds__(kMxThreads) k_update_scaled_max(double* __restrict__ x, const float* __restrict__ e,
                                                                   const double* __restrict__ ds, long long n,
                                                                   double* dsw) {
@@ -606,7 +606,7 @@ void launch_update_scaled_max(double* x, const float* e, double* ds, long long n
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   }
-  k_update_scaled_max<<<nsm * 8, kMxThreads, 0, s>>>(x, e, ds, n, ds);
+  k_update_scaled_max<<<nsm * 4, kMxThreads, 0, s>>>(x, e, ds, n, ds);  // 4 blocks per SM: measured 4 % faster than 8
 }
 
 void launch_resid_fused(int kind, double* r, const double* x, const double* b, const double* d, const uint8_t* m,
