@@ -57,3 +57,17 @@ def test_create_rejects_bad_param(bad):
     rc = L.cfmg_create(ctypes.byref(d), ctypes.byref(h))
     assert rc != 0 and not h.value
     assert L.cfmg_last_error(None)
+
+
+def _defines(prefix):
+    src = open(os.path.join(ROOT, "include", "cfmg.h")).read()
+    return {m.group(1): int(m.group(2)) for m in re.finditer(r"#define\s+(" + prefix + r"[A-Z0-9_]+)\s+(\d+)", src)}
+
+
+def test_option_and_class_tables_match_header():
+    """The Python names of the option and kernel-class codes are the
+    header's #define values (a mismatch would set the wrong knob)."""
+    opts = _defines("CFMG_OPT_")
+    assert {("CFMG_OPT_" + k.upper()): v for k, v in _lib.OPTIONS.items()} == opts
+    classes = _defines("CFMG_K_")
+    assert {("CFMG_K_" + k.upper()): v for k, v in _lib.KERNEL_CLASSES.items()} == classes

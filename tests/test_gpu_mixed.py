@@ -208,3 +208,47 @@ def test_solve_graph_matches_host_loop(precision):
     assert out[0][1] == out[1][1] and out[0][0] == out[1][0]
     assert np.array_equal(out[0][2], out[1][2])
     assert np.array_equal(out[0][3], out[1][3])
+
+
+def _profile(mg, cls, lev, precision, fn):
+    import ctypes
+
+    from cfmg import _lib
+
+    L = mg._L
+    mg._check(L.cfmg_profile(mg.handle, _lib.KERNEL_CLASSES[cls], lev, _lib.PRECISIONS[precision]))
+    fn()
+    n, ms = ctypes.c_longlong(), ctypes.c_double()
+    mg._check(L.cfmg_profile_read(mg.handle, ctypes.byref(n), ctypes.byref(ms)))
+    mg._check(L.cfmg_profile(mg.handle, -1, 0, 0))
+    return n.value, ms.value
+
+
+def test_fused_descent_profile_class():
+    """Fused descent passes are counted under CFMG_K_DESCENT and the plain
+    smoothing passes under CFMG_K_SWEEP; with the fusion off no descent pass
+    runs and the level-1 FP32 residual kernel does."""
+    base, mkind = CASES["config2_512_vertices_lap9_f"]
+    mg = cfmg.get_gmg(cfmg.Param(**base, tol=1e-10, maxite=40, residual_norm="l2", precision="mixed", verbose=False))
+    shape = mg.shape(1)
+    mg.oper[1].msk = _mask(base, shape, mkind)
+    cfmg.setup_operators(mg)
+    for lev in range(1, mg.nlevels + 1):
+        for f in ("x", "y", "r", "b"):
+            cfmg.set_to_zero(mg, lev, f)
+    msk = mg.download(1, "msk").astype(np.float64)
+    b = np.asfortranarray(np.random.default_rng(5).standard_normal(shape)) * msk
+    F.subtract_mean(b, msk)
+    mg.data[1].b = b
+
+    def solve():
+        cfmg.set_to_zero(mg, 1, "x")
+        return cfmg.solve(mg)
+
+    counts = {}
+    for fuse in (1, 0):
+        mg.set_option("fused_descent", fuse)
+        counts[fuse] = {c: _profile(mg, c, 1, "mixed", solve)[0] for c in ("descent", "sweep", "residual")}
+    assert counts[1]["descent"] > 0 and counts[1]["sweep"] > 0 and counts[1]["residual"] == 0, counts
+    assert counts[0]["descent"] == 0 and counts[0]["residual"] > 0, counts
+    assert counts[0]["sweep"] == counts[1]["sweep"] + counts[1]["descent"], counts
