@@ -513,7 +513,14 @@ int restrict_t(cfmg_handle* h, int lev, int field) {
 
 // mg.prolongation[lev]: x of lev += Pcoef * P(x of lev+1), then fill!
 template <class T>
-int prolong_t(cfmg_handle* h, int lev) {
+int zero_t(cfmg_handle* h, int lev, int field);
+
+// onto_zero: the fine x is known to hold +0 (zeroed and not written since),
+// so a standalone launch writes x = +0 + P x_coarse without reading it; the
+// caller then skips zeroing it. A level of the program engine is zeroed here
+// and prolonged as usual.
+template <class T>
+int prolong_t(cfmg_handle* h, int lev, bool onto_zero = false) {
   const Level& f = h->lv[lev - 1];
   const Level& c = h->lv[lev];
   View<T> vf = view<T>(f);
@@ -538,6 +545,10 @@ int prolong_t(cfmg_handle* h, int lev) {
     np_k = f.kc1 - f.kc0 + 1;
   }
   op.n = (long long)op.np_i * op.np_j * np_k;
+  if (onto_zero) {
+    if (!h->record && !(h->engine_on && (long long)f.len <= engine_limit(h, pc<T>()))) op.assign = 1;
+    else TRY(zero_t<T>(h, lev, CFMG_X));
+  }
   TRY(emit(h, op));
   return fill_if<T>(h, lev, vf.x);
 }
@@ -650,9 +661,11 @@ int vcycle_t(cfmg_handle* h, int lev0) {
   return CFMG_OK;
 }
 
-// fcycle! (src/gmg_cycles.jl:85-100)
+// fcycle! (src/gmg_cycles.jl:85-100). x1_zero: level 1's x holds +0 and
+// was not zeroed by the caller; nothing before the last prolongation touches
+// it, so that prolongation writes it without reading.
 template <class T>
-int fcycle_t(cfmg_handle* h) {
+int fcycle_t(cfmg_handle* h, bool x1_zero = false) {
   const int nl = L(h);
   for (int lev = 1; lev <= nl - 1; ++lev) {
     TRY(restrict_t<T>(h, lev, lev > 1 ? CFMG_B : CFMG_R));
@@ -660,21 +673,22 @@ int fcycle_t(cfmg_handle* h) {
   }
   TRY(coarsest_t<T>(h, h->d.ndeepest));
   for (int lev = nl - 1; lev >= 1; --lev) {
-    TRY(prolong_t<T>(h, lev));
+    TRY(prolong_t<T>(h, lev, lev == 1 && x1_zero));
     TRY(vcycle_t<T>(h, lev));
   }
   return CFMG_OK;
 }
 
+// x1_zero (F-cycle only): level 1's x is known to be +0, see fcycle_t
 template <class T>
-int cycle_body(cfmg_handle* h, int kind) {
+int cycle_body(cfmg_handle* h, int kind, bool x1_zero = false) {
   const cfmg_desc& d = h->d;
   switch (kind) {
     case CFMG_CYCLE_V:
     case CFMG_CYCLE_VREC:  // vcycle_recursive! is vcycle! when not verbose (src/gmg_cycles.jl:43-66)
       return vcycle_t<T>(h, 1);
     case CFMG_CYCLE_F:
-      return fcycle_t<T>(h);
+      return fcycle_t<T>(h, x1_zero);
     case CFMG_CYCLE_ONELEV:  // onelevel! (src/gmg_cycles.jl:3-6)
       return smooth_t<T>(h, 1, d.ndeepest);
     case CFMG_CYCLE_TWOLEV:  // twolevels! (src/gmg_cycles.jl:8-23)
@@ -693,8 +707,8 @@ int cycle_body(cfmg_handle* h, int kind) {
 }
 
 template <class T>
-int cycle_t(cfmg_handle* h, int kind) {
-  TRY(cycle_body<T>(h, kind));
+int cycle_t(cfmg_handle* h, int kind, bool x1_zero = false) {
+  TRY(cycle_body<T>(h, kind, x1_zero));
   return flush(h);
 }
 
@@ -1035,10 +1049,14 @@ __global__ void init_scale(double* ds) {
 
 int mixed_iteration(cfmg_handle* h, int kind) {
   for (Level& l : h->lv) l.xswap = 0;  // every FP32 x is zeroed before use in the cycle
+  // the F-cycle's first write of level 1's x is its last prolongation: the
+  // x buffer (+0 outside the wet interior in both buffers) is assigned
+  // there, not zeroed first
+  const bool lazy = kind == CFMG_CYCLE_F;
   if (fused_ok(h)) {  // the right-hand side was made by the previous fused pass
     const Level& l1 = h->lv[0];
-    TRY(zero_t<float>(h, 1, CFMG_X));
-    TRY(cycle_t<float>(h, kind));
+    if (!lazy) TRY(zero_t<float>(h, 1, CFMG_X));
+    TRY(cycle_t<float>(h, kind, lazy));
     {
       Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED);
       if (int_path(h)) launch_update_scaled_max(l1.x, view<float>(l1).x, h->dscal, (long long)l1.len, h->stream);
@@ -1058,9 +1076,9 @@ int mixed_iteration(cfmg_handle* h, int kind) {
     k_scale_from_norm<<<1, kNormParts, 0, h->stream>>>(h->dscal, h->partials, kNormParts, remove_mean);
     k_rhs32<<<nb, 256, 0, h->stream>>>(l1.r, l1.msk, h->dscal, l1.b32, l1.r32, n);
   }
-  TRY(zero_t<float>(h, 1, CFMG_X));
+  if (!lazy) TRY(zero_t<float>(h, 1, CFMG_X));
   LAUNCH_OK(h);
-  TRY(cycle_t<float>(h, kind));
+  TRY(cycle_t<float>(h, kind, lazy));
   {
     Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED);
     k_update<<<nb, 256, 0, h->stream>>>(l1.x, view<float>(l1).x, h->dscal, n);

@@ -89,7 +89,7 @@ void launch_restrict(int kind, const T* xf, T* bc, const T* Rcoef, const Geom& g
 // are the fine level's nx, ny, nz and [kf0, kf1] its k-range of parents.
 template <class T>
 void launch_prolong(int kind, T* xf, const T* xc, const T* Pcoef, const Geom& gf, const Geom& gc, int nxf, int nyf,
-                    int nzf, int kf0, int kf1, cudaStream_t s);
+                    int nzf, int kf0, int kf1, bool assign, cudaStream_t s);
 template <class T>
 void launch_fill_xperio(T* x, const Geom& g, cudaStream_t s);
 // norm: deterministic sum of msk*x^2 (FP64 accumulation) over the whole
@@ -151,6 +151,7 @@ struct Op {
   double tol;
   int s0, s1, s2, maxite, norm_kind;
   int inst;  // batched solver: the instance the Op belongs to
+  int assign;  // standalone prolongation onto a fine x known to be +0: written, not read
 };
 // scalar block of a whole-solve program
 enum SolveSlot { SS_NORMB = 0, SS_NR, SS_RES, SS_NITE, SS_NWET, SS_MEAN, SS_SCALE, SS_ISCALE, SS_T0, SS_T1,

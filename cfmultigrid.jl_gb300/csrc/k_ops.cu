@@ -147,14 +147,14 @@ __global__ void __launch_bounds__(kThreads) k_restrict(const T* __restrict__ x, 
 
 // Thread per fine parent (i, j, k) = (nh+1+2p, nh+1+2q, ...); each parent
 // updates its 4 (2D) or 8 (3D) children, which no other thread touches.
-template <class T, int KIND>
+template <class T, int KIND, bool ASSIGN>
 __global__ void __launch_bounds__(kThreads) k_prolong(T* __restrict__ xf, const T* __restrict__ x,
                                                       const T* __restrict__ coef, Geom gf, Geom gc, int np_i,
                                                       int np_j, int kf0, int kf1, int np_k) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const int qj = blockIdx.y * blockDim.y + threadIdx.y;
   const int qk = blockIdx.z;
-  if (p < np_i && qj < np_j && qk < np_k) d_prolong<T, KIND>(xf, x, coef, gf, gc, p, qj, qk, kf0);
+  if (p < np_i && qj < np_j && qk < np_k) d_prolong<T, KIND, ASSIGN>(xf, x, coef, gf, gc, p, qj, qk, kf0);
 }
 
 // ------------------------------------------------------------------- halo
@@ -294,7 +294,7 @@ void launch_restrict(int kind, const T* xf, T* bc, const T* Rcoef, const Geom& g
 }
 template <class T>
 void launch_prolong(int kind, T* xf, const T* xc, const T* Pcoef, const Geom& gf, const Geom& gc, int nxf, int nyf,
-                    int nzf, int kf0, int kf1, cudaStream_t s) {
+                    int nzf, int kf0, int kf1, bool assign, cudaStream_t s) {
   // parents: i = nh+1 : 2 : nx+nh (likewise j, and k in 3D)
   const int np_i = (nxf + 1) / 2, np_j = (nyf + 1) / 2;
   const bool threed = (kind == 1 || kind == 3);
@@ -302,12 +302,21 @@ void launch_prolong(int kind, T* xf, const T* xc, const T* Pcoef, const Geom& gf
   if (np_i <= 0 || np_j <= 0 || np_k <= 0) return;
   dim3 blk(64, 4, 1);
   dim3 grid((unsigned)((np_i + 63) / 64), (unsigned)((np_j + 3) / 4), (unsigned)np_k);
+#define CFMG_PRO(K)                                                                                       \
+  case K:                                                                                                 \
+    if (assign)                                                                                           \
+      k_prolong<T, K, true><<<grid, blk, 0, s>>>(xf, xc, Pcoef, gf, gc, np_i, np_j, kf0, kf1, np_k);      \
+    else                                                                                                  \
+      k_prolong<T, K, false><<<grid, blk, 0, s>>>(xf, xc, Pcoef, gf, gc, np_i, np_j, kf0, kf1, np_k);     \
+    break;
   switch (kind) {
-    case 0: k_prolong<T, 0><<<grid, blk, 0, s>>>(xf, xc, Pcoef, gf, gc, np_i, np_j, kf0, kf1, np_k); break;
-    case 1: k_prolong<T, 1><<<grid, blk, 0, s>>>(xf, xc, Pcoef, gf, gc, np_i, np_j, kf0, kf1, np_k); break;
-    case 2: k_prolong<T, 2><<<grid, blk, 0, s>>>(xf, xc, Pcoef, gf, gc, np_i, np_j, kf0, kf1, np_k); break;
-    default: k_prolong<T, 3><<<grid, blk, 0, s>>>(xf, xc, Pcoef, gf, gc, np_i, np_j, kf0, kf1, np_k); break;
+    CFMG_PRO(0)
+    CFMG_PRO(1)
+    CFMG_PRO(2)
+    default:
+    CFMG_PRO(3)
   }
+#undef CFMG_PRO
 }
 template <class T>
 void launch_fill_xperio(T* x, const Geom& g, cudaStream_t s) {
@@ -341,7 +350,7 @@ void launch_norm(const T* x, const uint8_t* m, size_t n, double* partials, doubl
   template void launch_restrict<T>(int, const T*, T*, const T*, const Geom&, const Geom&, const Box&,            \
                                    cudaStream_t);                                                                \
   template void launch_prolong<T>(int, T*, const T*, const T*, const Geom&, const Geom&, int, int, int, int, int, \
-                                  cudaStream_t);                                                                 \
+                                  bool, cudaStream_t);                                                           \
   template void launch_fill_xperio<T>(T*, const Geom&, cudaStream_t);                                            \
   template void launch_norm<T>(const T*, const uint8_t*, size_t, double*, double*, const double*, int, cudaStream_t);
 
@@ -396,7 +405,7 @@ static void launch_op_t(const Op& op, cudaStream_t s) {
       const bool t3 = (kind == 1 || kind == 3);
       // launch_prolong derives the parent counts from (nx, ny, nz) of the fine level
       launch_prolong<T>(kind, y, x, (const T*)op.coef, op.g, op.gc, 2 * op.np_i, 2 * op.np_j,
-                        t3 ? 2 * (op.kf1 - op.kf0 + 1) : 1, op.kf0, op.kf1, s);
+                        t3 ? 2 * (op.kf1 - op.kf0 + 1) : 1, op.kf0, op.kf1, op.assign != 0, s);
       break;
     }
     case OPK_FILL: launch_fill_xperio<T>(y, op.g, s); break;

@@ -294,7 +294,9 @@ __device__ __forceinline__ T square3(const T* x, long long C, long long di, long
 // other parent touches. Kinds as in d_restrict: pcloop2d!
 // (src/RP_on_centers.jl:146-163), pcloop3d! (:84-104), pvloop2d!
 // (src/RP_on_vertices.jl:117-137), prolongation_vertices! (:34-72).
-template <class T, int KIND>
+// ASSIGN: the fine x is known to hold +0 at every updated cell, so it is
+// not read: x = +0 + coef*v gives the same value and the same zero sign.
+template <class T, int KIND, bool ASSIGN = false>
 __device__ __forceinline__ void d_prolong(T* xf, const T* x, const T* coef, const Geom& gf, const Geom& gc, int p,
                                           int q, int qk, int kf0) {
   typedef Ar<T> A;
@@ -312,7 +314,7 @@ __device__ __forceinline__ void d_prolong(T* xf, const T* x, const T* coef, cons
       for (int di = 0; di <= 1; ++di) {
         T bb = square3(x, C, (long long)(2 * di - 1), (2 * dj - 1) * c1, 0LL);
         long long Fi = F + di + dj * f1;
-        xf[Fi] = A::add(xf[Fi], A::mul(coef[Fi], A::add(bb, x9)));
+        xf[Fi] = A::add(ASSIGN ? T(0) : xf[Fi], A::mul(coef[Fi], A::add(bb, x9)));
       }
   } else if (KIND == 1) {
     const int k = nh + 1 + 2 * qk;
@@ -328,24 +330,25 @@ __device__ __forceinline__ void d_prolong(T* xf, const T* x, const T* coef, cons
         T bb = A::mul(square3(x, C, ddi, ddj, 0LL), T(3));
         T c = square3(x, C, ddi, ddj, c2);
         long long F0 = F + di + dj * f1, F1 = F0 + f2;
-        xf[F0] = A::add(xf[F0], A::mul(coef[F0], A::add(A::add(bb, a), x28)));
-        xf[F1] = A::add(xf[F1], A::mul(coef[F1], A::add(A::add(bb, c), x28)));
+        xf[F0] = A::add(ASSIGN ? T(0) : xf[F0], A::mul(coef[F0], A::add(A::add(bb, a), x28)));
+        xf[F1] = A::add(ASSIGN ? T(0) : xf[F1], A::mul(coef[F1], A::add(A::add(bb, c), x28)));
       }
   } else if (KIND == 2) {
     const int k = kf0 + qk;
     const long long C = lin(gc, ic, jc, k), F = lin(gf, i, j, k);
     const T x00 = x[C], x10 = x[C + 1], x01 = x[C + c1], x11 = x[C + 1 + c1];
-    xf[F] = A::add(xf[F], A::mul(coef[F], x00));
-    xf[F + 1] = A::add(xf[F + 1], A::mul(coef[F + 1], A::add(x00, x10)));
-    xf[F + f1] = A::add(xf[F + f1], A::mul(coef[F + f1], A::add(x00, x01)));
-    xf[F + 1 + f1] = A::add(xf[F + 1 + f1], A::mul(coef[F + 1 + f1], A::add(A::add(A::add(x00, x10), x01), x11)));
+    xf[F] = A::add(ASSIGN ? T(0) : xf[F], A::mul(coef[F], x00));
+    xf[F + 1] = A::add(ASSIGN ? T(0) : xf[F + 1], A::mul(coef[F + 1], A::add(x00, x10)));
+    xf[F + f1] = A::add(ASSIGN ? T(0) : xf[F + f1], A::mul(coef[F + f1], A::add(x00, x01)));
+    xf[F + 1 + f1] =
+        A::add(ASSIGN ? T(0) : xf[F + 1 + f1], A::mul(coef[F + 1 + f1], A::add(A::add(A::add(x00, x10), x01), x11)));
   } else {
     const int k = nh + 1 + 2 * qk;
     const int kc = f2c(k, nh);
     const long long C = lin(gc, ic, jc, kc), F = lin(gf, i, j, k);
     const T x000 = x[C], x100 = x[C + 1], x010 = x[C + c1], x001 = x[C + c2];
     const T x110 = x[C + 1 + c1], x101 = x[C + 1 + c2], x011 = x[C + c1 + c2], x111 = x[C + 1 + c1 + c2];
-    auto upd = [&](long long Fi, T v) { xf[Fi] = A::add(xf[Fi], A::mul(coef[Fi], v)); };
+    auto upd = [&](long long Fi, T v) { xf[Fi] = A::add(ASSIGN ? T(0) : xf[Fi], A::mul(coef[Fi], v)); };
     upd(F, x000);
     upd(F + 1, A::add(x000, x100));
     upd(F + f1, A::add(x000, x010));
