@@ -661,19 +661,24 @@ int vcycle_t(cfmg_handle* h, int lev0) {
   return CFMG_OK;
 }
 
-// fcycle! (src/gmg_cycles.jl:85-100). x1_zero: level 1's x holds +0 and
-// was not zeroed by the caller; nothing before the last prolongation touches
-// it, so that prolongation writes it without reading.
+// fcycle! (src/gmg_cycles.jl:85-100). The descent zeroes x on levels
+// 2..nl. In the FP32 correction cycle of a closed topology (every cell
+// outside the wet interior +0 in both x buffers), nothing reads x on levels
+// 2..nl-1 before the ascent's prolongation onto them, so those levels are
+// not zeroed and that prolongation writes +0 + P x_coarse without reading
+// (the same values). x1_zero: level 1's x holds +0 likewise (the caller's
+// mixed iteration leaves it unzeroed).
 template <class T>
 int fcycle_t(cfmg_handle* h, bool x1_zero = false) {
   const int nl = L(h);
+  const bool lazy = sizeof(T) == 4 && !xperio(h);
   for (int lev = 1; lev <= nl - 1; ++lev) {
     TRY(restrict_t<T>(h, lev, lev > 1 ? CFMG_B : CFMG_R));
-    TRY(zero_t<T>(h, lev + 1, CFMG_X));
+    if (!lazy || lev + 1 == nl) TRY(zero_t<T>(h, lev + 1, CFMG_X));  // the coarsest solve reads it
   }
   TRY(coarsest_t<T>(h, h->d.ndeepest));
   for (int lev = nl - 1; lev >= 1; --lev) {
-    TRY(prolong_t<T>(h, lev, lev == 1 && x1_zero));
+    TRY(prolong_t<T>(h, lev, lev >= 2 ? lazy : x1_zero));
     TRY(vcycle_t<T>(h, lev));
   }
   return CFMG_OK;
@@ -1052,7 +1057,7 @@ int mixed_iteration(cfmg_handle* h, int kind) {
   // the F-cycle's first write of level 1's x is its last prolongation: the
   // x buffer (+0 outside the wet interior in both buffers) is assigned
   // there, not zeroed first
-  const bool lazy = kind == CFMG_CYCLE_F;
+  const bool lazy = kind == CFMG_CYCLE_F && !xperio(h);
   if (fused_ok(h)) {  // the right-hand side was made by the previous fused pass
     const Level& l1 = h->lv[0];
     if (!lazy) TRY(zero_t<float>(h, 1, CFMG_X));
