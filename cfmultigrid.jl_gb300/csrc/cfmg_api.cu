@@ -367,7 +367,9 @@ int sweep(cfmg_handle* h, int lev, int kind, const T* x, T* y, const Box* bx) {
 // topology, 2D 5- and 9-point): the result goes to the partner buffer.
 template <class T>
 bool tb_eligible(const cfmg_handle* h, int lev) {
-  if (sizeof(T) != 4 || !h->tb_on || (h->record && !h->record_tb) || xperio(h)) return false;
+  if (sizeof(T) != 4 || !h->tb_on || (h->record && !h->record_tb)) return false;
+  // x-periodic: the lean packed passes of the 2D 5-point operator (standalone launches)
+  if (xperio(h) && (h->record || h->tb_version != 5 || threed(h) || h->d.op != CFMG_LAPLACIAN)) return false;
   // 3D: 7-point streaming passes, opt-in (CFMG_OPT_TEMPORAL_BLOCKING = 4): at
   // 512 x 512 x 256 a 4-sweep pass measured 1.0-1.3 ms, no faster than
   // four single-sweep kernels at 66 % of HBM
@@ -401,6 +403,23 @@ int smooth_tb(cfmg_handle* h, int lev, int nite) {
   Level& l = h->lv[lev - 1];
   const int stencil = h->d.op == CFMG_LAPLACIAN9 ? 9 : 5;
   TRY(flush(h));
+  if (xperio(h)) {  // periodic tiles over the interior columns, then fill! of the result
+    const int per = nite > 3 ? kTbMaxPairs : 3;
+    for (int left = nite; left > 0;) {
+      const int n = left > per ? per : left;
+      View<float> v = view<float>(l);
+      {
+        Launch k(h, CFMG_K_SWEEP, lev, CFMG_MIXED);
+        launch_smooth_tb_periodic(n, v.x, v.y, v.b, v.widiag, (float)(1.0 - h->d.omega), l.tx, l.ty, l.tz,
+                                  l.nh + 1, l.nx + l.nh, l.nh, l.ny + l.nh + 1, h->stream);
+      }
+      l.xswap ^= 1;
+      left -= n;
+      TRY(fill_if<float>(h, lev, view<float>(l).x));
+    }
+    LAUNCH_OK(h);
+    return CFMG_OK;
+  }
   // up to 3 pairs per pass (kTbMaxPairs for a long smoothing such as the
   // coarsest solve's; the batched solver's blocked kernel takes up to 3)
   const int per = (nite > 3 && !h->record) ? kTbMaxPairs : 3;
@@ -600,7 +619,7 @@ int coarsest_t<float>(cfmg_handle* h, int nite) {
 // levels smoothed in lean packed passes (2D, closed topology), the last
 // pass does the residual and the restriction in its epilogue.
 bool fused_descent_ok(const cfmg_handle* h, int lev) {
-  if (!h->fuse_on || h->record || h->tb_version != 5 || threed(h) || lev >= L(h)) return false;
+  if (!h->fuse_on || h->record || h->tb_version != 5 || threed(h) || xperio(h) || lev >= L(h)) return false;
   if (h->d.op != CFMG_LAPLACIAN && h->d.op != CFMG_LAPLACIAN9) return false;
   return tb_eligible<float>(h, lev) && h->lv[lev - 1].tz == 1;
 }

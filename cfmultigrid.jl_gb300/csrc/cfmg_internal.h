@@ -177,6 +177,11 @@ constexpr int kTbMaxPairs = 10;
 // packed form; 1: one column per thread
 bool launch_smooth_tb(int version, int stencil, int nite, const float* x, float* xo, const float* b, const float* w,
                       float cff, int tx, int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s);
+// the lean packed passes for the x-periodic topology, 5-point operator: the
+// tiles cover the interior columns [ui0, ui1] and read the periodic images
+// of the columns beside them; the caller fills the halo columns afterwards
+bool launch_smooth_tb_periodic(int nite, const float* x, float* xo, const float* b, const float* w, float cff,
+                               int tx, int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s);
 // The last pass of a V-cycle's pre-smoothing with the step that follows it
 // in the same kernel (2D, single layer): the residual of the smoothed x,
 // restricted to the coarse b, and the coarse x zeroed at the same cells.

@@ -423,7 +423,12 @@ __device__ __forceinline__ void tb5_resid(const float* __restrict__ src, float* 
   }
 }
 
-template <int ST, int NITE, int TY, int ROWS, int MINB, bool EPI>
+// PER (x-periodic topology, 5-point): the tiles cover the interior columns
+// [ui0, ui1] = [nh+1, nx+nh], and a tile column outside them reads its
+// periodic image, so the sweeps see the periodic domain. With nh >= 2 that
+// is what the reference's interior gets from its linear-range sweeps with a
+// fill! after each pair; the caller fills the halo columns after the pass.
+template <int ST, int NITE, int TY, int ROWS, int MINB, bool EPI, bool PER = false>
 __global__ void __launch_bounds__(kT5Tx * TY, MINB) k_smooth_tb5(const float* __restrict__ x, float* __restrict__ xo,
                                                                  const float* __restrict__ b,
                                                                  const float* __restrict__ w, float cff, int tx,
@@ -446,9 +451,10 @@ __global__ void __launch_bounds__(kT5Tx * TY, MINB) k_smooth_tb5(const float* __
   // linear index of the thread's even cell in its first row (may lie
   // outside the array for boundary tiles: used only under the bounds tests)
   const long long I0 = (long long)tx * ty * blockIdx.z + (long long)(gi0 - 1) + (long long)tx * (tj0 + r0 - 1);
-  const bool tile_in_u = ti0 >= ui0 && ti0 + kT5W - 1 <= ui1 && tj0 >= uj0 && tj0 + TH - 1 <= uj1;
+  const bool cols_in = ti0 >= ui0 && ti0 + kT5W - 1 <= ui1, rows_in = tj0 >= uj0 && tj0 + TH - 1 <= uj1;
+  const bool tile_in_u = rows_in && (PER || cols_in);  // periodic: every column is updated
   // the parity of I0 is the same for every thread of the tile
-  const bool fast = tile_in_u && ((I0 | tx) & 1) == 0;
+  const bool fast = rows_in && cols_in && ((I0 | tx) & 1) == 0;
   float2 B[ROWS], WT[ROWS];
   unsigned inU = ~0u;  // bit 2r + e: cell in U
   float* prow = P0 + (r0 + 1) * kT5Row + lx;  // padded row r0 + 1 = tile row r0
@@ -478,13 +484,18 @@ __global__ void __launch_bounds__(kT5Tx * TY, MINB) k_smooth_tb5(const float* __
       float v[2], bb[2], ww[2];
 #pragma unroll
       for (int e = 0; e < 2; ++e) {
-        const int gi = gi0 + e;
+        int gi = gi0 + e;
+        long long I = I0 + (long long)r * tx + e;
+        if (PER) {  // the periodic image among the interior columns
+          const int nx = ui1 - ui0 + 1, gm = ui0 + (((gi - ui0) % nx) + nx) % nx;
+          I += gm - gi;
+          gi = gm;
+        }
         const bool in = row_in && gi >= 1 && gi <= tx;
-        const long long I = I0 + (long long)r * tx + e;
         v[e] = in ? x[I] : 0.f;
         bb[e] = in ? b[I] : 0.f;
         ww[e] = in ? w[I] : 0.f;
-        if (row_u && gi >= ui0 && gi <= ui1) inU |= 1u << (2 * r + e);
+        if (row_u && (PER || (gi >= ui0 && gi <= ui1))) inU |= 1u << (2 * r + e);
       }
       prow[r * kT5Row + 1] = v[0];
       prow[r * kT5Row + kT5Half + 1] = v[1];
@@ -614,7 +625,7 @@ __global__ void __launch_bounds__(kT5Tx * TY, MINB) k_smooth_tb5(const float* __
 #pragma unroll
     for (int e = 0; e < 2; ++e) {
       const int lc = 2 * lx + e;
-      if (lc >= H && lc < kT5W - H && (inU >> (2 * r + e) & 1u))
+      if (lc >= H && lc < kT5W - H && (inU >> (2 * r + e) & 1u) && (!PER || gi0 + e <= ui1))
         xo[I0 + (long long)r * tx + e] = prow[r * kT5Row + e * kT5Half + 1];
     }
   }
@@ -695,7 +706,7 @@ static void launch_tb3_n(const float* x, float* xo, const float* b, const float*
   k_smooth_tb3<ST, NITE><<<grid, dim3(kT3Tx, kT3Ty, 1), smem, s>>>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1);
 }
 
-template <int ST, int NITE, int TY, int ROWS, int MINB, bool EPI>
+template <int ST, int NITE, int TY, int ROWS, int MINB, bool EPI, bool PER = false>
 static void launch_tb5_n(const float* x, float* xo, const float* b, const float* w, float cff, int tx, int ty,
                          int nz, int ui0, int ui1, int uj0, int uj1, const TbEpi& ep, cudaStream_t s) {
   constexpr int H = 2 * NITE + (EPI ? 2 : 0);
@@ -704,12 +715,12 @@ static void launch_tb5_n(const float* x, float* xo, const float* b, const float*
                       (EPI ? (size_t)TY * ROWS * kT5Tx * (sizeof(float2) + sizeof(ushort)) : 0);
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_smooth_tb5<ST, NITE, TY, ROWS, MINB, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
+    cudaFuncSetAttribute(k_smooth_tb5<ST, NITE, TY, ROWS, MINB, EPI, PER>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = true;
   }
   dim3 grid((unsigned)((ui1 - ui0 + CW) / CW), (unsigned)((uj1 - uj0 + CH) / CH), (unsigned)nz);
-  k_smooth_tb5<ST, NITE, TY, ROWS, MINB, EPI>
+  k_smooth_tb5<ST, NITE, TY, ROWS, MINB, EPI, PER>
       <<<grid, dim3(kT5Tx, TY, 1), smem, s>>>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1, ep);
 }
 
@@ -752,6 +763,19 @@ bool launch_smooth_tb(int version, int stencil, int nite, const float* x, float*
   CFMG_TB(9, 1) CFMG_TB(9, 2) CFMG_TB(9, 3) CFMG_TB(9, 4) CFMG_TB(9, 5)
   CFMG_TB(9, 6) CFMG_TB(9, 7) CFMG_TB(9, 8) CFMG_TB(9, 9) CFMG_TB(9, 10)
 #undef CFMG_TB
+  return false;
+}
+
+bool launch_smooth_tb_periodic(int nite, const float* x, float* xo, const float* b, const float* w, float cff,
+                               int tx, int ty, int nz, int ui0, int ui1, int uj0, int uj1, cudaStream_t s) {
+#define CFMG_TBP(N)                                                                                    \
+  if (nite == N) {                                                                                     \
+    launch_tb5_n<5, N, 8, 6, 2, false, true>(x, xo, b, w, cff, tx, ty, nz, ui0, ui1, uj0, uj1, TbEpi{}, s); \
+    return true;                                                                                       \
+  }
+  CFMG_TBP(1) CFMG_TBP(2) CFMG_TBP(3) CFMG_TBP(4) CFMG_TBP(5)
+  CFMG_TBP(6) CFMG_TBP(7) CFMG_TBP(8) CFMG_TBP(9) CFMG_TBP(10)
+#undef CFMG_TBP
   return false;
 }
 
