@@ -13,8 +13,8 @@
  *   mg.restriction[lev](mg, lev, field), mg.prolongation[lev](mg, lev)
  * (src/gmg_types.jl:128-131, bound in src/gmg_setup.jl:86-101), plus
  * solve!, norm, set_to_zero! and fill!. Each entry point below names the
- * Julia function it replaces. The Julia glue that binds them with ccall
- * is shown in INTEGRATION.md.
+ * Julia function it replaces; a Julia host binds them with ccall, one
+ * closure per table entry, and a solve! method that calls cfmg_solve.
  *
  * Arrays crossing the ABI use the reference layout: one column-major
  * (i fastest) array of tx*ty*tz entries per level and field, with
@@ -194,8 +194,8 @@ CFMG_API int cfmg_cycle(cfmg_handle* h, int kind);
 CFMG_API int cfmg_solve(cfmg_handle* h, double* res, int* nite, double* history);
 
 /* Adjoint solve: the backward pass of solve! (no counterpart in the
- * reference; a Julia host exposes it as a ChainRulesCore rrule, see
- * INTEGRATION.md). After a forward cfmg_solve, with the cotangent
+ * reference; a Julia host exposes it as the pullback of a ChainRulesCore
+ * rrule for solve!). After a forward cfmg_solve, with the cotangent
  * g = dL/dx of level 1 (reference layout, host or device pointer), solves
  * A lam = g with the same cycle, arithmetic and stopping rule (A is
  * symmetric) and writes dL/db = lam to grad_b and, for CFMG_VARCOEF,
