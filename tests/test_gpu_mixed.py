@@ -37,6 +37,15 @@ BIG_CASES = {
     # x-periodic, wet everywhere: the blocked passes' tiles wrap across the seam
     "2d_xperio_512_centers_v": (dict(nx=512, ny=256, nz=1, case="twod", topology="xperio", cycle="v", npre=2,
                                      npost=2, omega=0.8, nlevels=5), None),
+    # odd widths: no tile takes the aligned vector path
+    "2d_odd_301x203_vertices_lap9_f": (dict(nx=301, ny=203, nz=1, case="twod", location="vertices",
+                                            operator="laplacian9", cycle="f", npre=3, npost=3, omega=0.8,
+                                            nlevels=5), "disk"),
+    "2d_odd_301x203_centers_v": (dict(nx=301, ny=203, nz=1, case="twod", cycle="v", npre=2, npost=2, omega=0.8,
+                                      nlevels=5), "disk"),
+    # two :twod layers (one launch covers both; no fused descent)
+    "2d_twolayer_256_centers_v": (dict(nx=256, ny=256, nz=2, case="twod", cycle="v", npre=2, npost=2, omega=0.8,
+                                       nlevels=5), "disk"),
 }
 
 
@@ -114,7 +123,8 @@ def test_mixed_matches_fp64_oracle(name):
 
 @pytest.mark.parametrize("name", ["config1_256_centers_v", "config2_512_vertices_lap9_f", "3d_48_centers_v",
                                   "config2_2048_vertices_lap9_f", "config1_1024_centers_v", "2d_xperio_vertices_v",
-                                  "2d_xperio_512_centers_v"])
+                                  "2d_xperio_512_centers_v", "2d_odd_301x203_vertices_lap9_f",
+                                  "2d_odd_301x203_centers_v", "2d_twolayer_256_centers_v"])
 def test_temporal_blocking_is_bit_identical(name):
     """The temporally blocked FP32 smoother (all sweeps of a call in one
     shared-memory pass), and its form whose last pre-smoothing pass also
