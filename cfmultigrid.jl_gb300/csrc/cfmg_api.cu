@@ -1043,7 +1043,8 @@ int fused_residual(cfmg_handle* h) {
     }
     if (neumann) {
       Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED);
-      launch_rhs32_shift(l1.msk, h->dscal + S_MEAN2, l1.b32, l1.r32, (long long)l1.len, h->stream);
+      launch_rhs32_shift(l1.msk, h->dscal + S_MEAN2, l1.b32, h->d.cycle == CFMG_CYCLE_F ? l1.r32 : nullptr,
+                         (long long)l1.len, h->stream);
     }
     LAUNCH_OK(h);
     return CFMG_OK;

@@ -485,7 +485,7 @@ __global__ void k_rhs32_shift(const uint8_t* __restrict__ m, const double* __res
   const float sh = *reinterpret_cast<const float*>(ms + (S_SHIFT - S_MEAN2));  // (float)(mean * scale)
   const float f = m[I] ? __fsub_rn(b32[I], sh) : 0.f;
   b32[I] = f;
-  r32[I] = f;
+  if (r32) r32[I] = f;  // only the F-cycle restricts level 1's r before forming it
 }
 
 // dq from diag and msk; *ok is cleared when a wet cell's Q*diag is not an
