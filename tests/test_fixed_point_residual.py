@@ -64,3 +64,60 @@ def test_fixed_point_residual_is_closer_to_exact_than_fp64():
     err_fp = abs(float((fp - ex) / ex))
     err_fx = abs(float((fx - ex) / ex))
     assert err_fx < err_fp / 4, (err_fx, err_fp)
+
+
+def _bits(v):
+    import struct
+
+    return struct.unpack("<Q", struct.pack("<d", v))[0]
+
+
+def _to_fix_branching(v, k):
+    """round(v 2^k) as first defined: a left shift for sh >= 0, else round
+    half up on the magnitude; zero and subnormal v give 0."""
+    u = _bits(v)
+    ex = (u >> 52) & 0x7FF
+    m = (u & 0x000FFFFFFFFFFFFF) | 0x0010000000000000
+    sh = ex - 1075 + k
+    if sh >= 0:
+        r = m << sh
+    else:
+        s = -sh
+        r = (((m >> (s - 1)) + 1) >> 1) if s <= 64 else 0
+    r = r if ex else 0
+    return -r if u >> 63 else r
+
+
+def _to_fix_branchfree(v, k):
+    """The kernels' form (ops_dev.cuh to_fix): M = m << 10, t = clamp(10 -
+    sh, 1, 64), r = ((M >> (t-1)) + 1) >> 1."""
+    u = _bits(v)
+    ex = (u >> 52) & 0x7FF
+    M = ((u & 0x000FFFFFFFFFFFFF) | 0x0010000000000000) << 10
+    t = min(max(1085 - ex - k, 1), 64)
+    r = (((M >> (t - 1)) + 1) >> 1) if ex else 0
+    return -r if u >> 63 else r
+
+
+def test_branch_free_conversion_matches_definition():
+    """The branch-free fixed-point conversion of the integer residual
+    kernels gives round(v 2^k) exactly as the branching definition over the
+    whole range they use (|v| 2^k < 2^58), ties, subnormals and zeros
+    included, and matches the exact rational rounding."""
+    rng = np.random.default_rng(7)
+    for E in range(-60, 61, 7):
+        k = 58 - E
+        vals = list(rng.uniform(-1, 1, 400) * 2.0 ** E)
+        vals += list(rng.standard_normal(100) * 2.0 ** (E - rng.integers(1, 90, 100)))
+        vals += [0.0, -0.0, 2.0 ** (E - 1), -(2.0 ** (E - 1)), 2.0 ** E * (1 - 2.0 ** -53), 5e-324, -5e-324,
+                 2.0 ** (E - 59), 3 * 2.0 ** (E - 60), -3 * 2.0 ** (E - 60)]  # the last three: ties and a half
+        for v in vals:
+            v = float(v)
+            if abs(v) >= 2.0 ** E:
+                continue
+            a, c = _to_fix_branching(v, k), _to_fix_branchfree(v, k)
+            assert a == c, (v, k, a, c)
+            exact = Fraction(v) * Fraction(2) ** k
+            if _bits(v) & 0x7FF0000000000000:  # normal: round half away from zero
+                ref = math.floor(abs(exact) + Fraction(1, 2))
+                assert c == (ref if v >= 0 else -ref), (v, k, c, ref)
