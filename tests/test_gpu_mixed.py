@@ -21,6 +21,13 @@ CASES = {
                                          operator="laplacian9", cycle="f", npre=3, npost=3, omega=0.8,
                                          nlevels=7), "disk"),
     "3d_48_centers_v": (dict(nx=48, ny=48, nz=48, case="threed", cycle="v", npre=2, npost=2, omega=0.8), None),
+    # 3D vertex-centred (Dirichlet) operators: the 7-point one takes the
+    # streaming blocked passes when asked, the 19-point one always runs its
+    # one pair of sweeps per call as separate kernels
+    "3d_32_vertices_v": (dict(nx=32, ny=32, nz=32, case="threed", location="vertices", cycle="v", npre=2,
+                              npost=2, omega=0.8), None),
+    "3d_32_vertices_lap9_v": (dict(nx=32, ny=32, nz=32, case="threed", location="vertices",
+                                   operator="laplacian9", cycle="v", npre=2, npost=2, omega=0.8), None),
     "2d_xperio_vertices_v": (dict(nx=64, ny=64, nz=1, case="twod", location="vertices", topology="xperio",
                                   cycle="v", npre=2, npost=2, omega=0.9, ndeepest=60), None),
 }
@@ -124,7 +131,7 @@ def test_mixed_matches_fp64_oracle(name):
 @pytest.mark.parametrize("name", ["config1_256_centers_v", "config2_512_vertices_lap9_f", "3d_48_centers_v",
                                   "config2_2048_vertices_lap9_f", "config1_1024_centers_v", "2d_xperio_vertices_v",
                                   "2d_xperio_512_centers_v", "2d_odd_301x203_vertices_lap9_f",
-                                  "2d_odd_301x203_centers_v", "2d_twolayer_256_centers_v"])
+                                  "2d_odd_301x203_centers_v", "2d_twolayer_256_centers_v", "3d_32_vertices_v"])
 def test_temporal_blocking_is_bit_identical(name):
     """The temporally blocked FP32 smoother (all sweeps of a call in one
     shared-memory pass), and its form whose last pre-smoothing pass also
