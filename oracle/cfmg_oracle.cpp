@@ -1,7 +1,7 @@
 // CPU oracle for CFMultigrid.jl's geometric-multigrid path.
 //
-// TEST INFRASTRUCTURE ONLY: the checker that the CUDA product path is
-// compared against. It is loaded by tests/, by __graft_entry__.smoke() and by
+// TEST INFRASTRUCTURE ONLY: the CPU restatement that the CUDA product path
+// is compared against. It is loaded by tests/, by __graft_entry__.smoke() and by
 // the CPU-baseline leg of bench.py, never by the product.
 //
 // A plain, single-threaded FP64 restatement of the Julia reference

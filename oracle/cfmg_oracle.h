@@ -1,8 +1,8 @@
 /*
  * CPU oracle for CFMultigrid.jl's geometric-multigrid path.
  *
- * TEST INFRASTRUCTURE ONLY. This library is the checker that the CUDA
- * product path (libcfmg) is compared against. Only the test suite, the
+ * TEST INFRASTRUCTURE ONLY. This library is the CPU restatement that the
+ * CUDA product path (libcfmg) is compared against. Only the test suite, the
  * smoke check and the CPU-baseline leg of the benchmark load it. No
  * product code path calls it.
  *

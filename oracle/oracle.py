@@ -1,6 +1,6 @@
 """ctypes front end of the CPU oracle (test infrastructure only).
 
-The oracle is the checker for the CUDA product path: only tests/,
+The oracle is what the CUDA product path is compared against: only tests/,
 ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` import
 this module. It restates CFMultigrid.jl's ``Gmg`` object (src/gmg_types.jl,
 src/gmg_setup.jl, src/gmg_cycles.jl, src/gmg_solver.jl) on the CPU in FP64;
