@@ -279,9 +279,16 @@ def run_ours(args, rank, world, local):
     # roofline: the level-1 FP32 smoothing pass of the mixed form (one
     # temporally blocked launch runs all 2*npre sweeps of a smoothing call),
     # timed per launch with CUDA events on the library's stream in one solve;
-    # the post-smoothing passes (the pre-smoothing ones are fused descent
+    # the post-smoothing passes in their plain form (the solution update
+    # taken out of the last one; the pre-smoothing ones are fused descent
     # passes, reported beside it)
+    mgm.set_option("fused_update", 0)
     nl, tl = profile(cfmg, mgm, "sweep", 1, "mixed", lambda: solve(mgm))
+    mgm.set_option("fused_update", 1)
+    # the same pass with the FP64 solution update x += e * iscale (and max |x|)
+    # in its output phase, as the default solve runs it: FP32 x, b and
+    # omega*idiag read, FP64 x read and written
+    nlu, tlu = profile(cfmg, mgm, "sweep", 1, "mixed", lambda: solve(mgm))
     g1 = mgm.levels[1]
     box_cells = (g1.nx + 2) * (g1.ny + 2) * g1.nz  # the update box U = [nh, nx+nh+1]^2
     sweeps_per_launch = 2 * min(param["npre"], 3)
@@ -304,6 +311,9 @@ def run_ours(args, rank, world, local):
     g2 = mgm.levels[2]
     coarse_cells = g2.nx * g2.ny * g2.nz
     bytes_descent = 21.0 * box_cells + 12.0 * coarse_cells
+    bytes_update = 28.0 * box_cells
+    ms_update = tlu / max(nlu, 1)
+    ach_update = bytes_update / (ms_update * 1e-3) / 1e9 if ms_update > 0 else 0.0
     ms_descent = tld / max(nld, 1)
     ach_descent = bytes_descent / (ms_descent * 1e-3) / 1e9 if ms_descent > 0 else 0.0
     # FP64 sweep of the drop-in: FP64-issue bound, reported beside it
@@ -339,6 +349,10 @@ def run_ours(args, rank, world, local):
                      "launches_timed": nl, "ms_per_launch": ms_launch,
                      "bytes_per_launch": bytes_per_launch, "sweeps_per_launch": sweeps_per_launch,
                      "effective_sweep_gbs": achieved * sweeps_per_launch},
+        "fused_update": {"kernel": "k_smooth_tb5<9,3,...,UPD>: level-1 post-smoothing pass with the FP64 solution "
+                                   "update and max |x|",
+                         "launches_timed": nlu, "ms_per_launch": ms_update, "bytes_per_launch": bytes_update,
+                         "achieved_gbs": ach_update, "frac": ach_update / hbm_peak},
         "fused_descent": {"kernel": "k_smooth_tb5<9,3,...,EPI>: level-1 pre-smoothing pass with the residual, "
                                     "its restriction and the zeroed coarse x",
                           "launches_timed": nld, "ms_per_launch": ms_descent, "bytes_per_launch": bytes_descent,

@@ -245,7 +245,9 @@ class Gmg:
         level-1 residual of the mixed loop, 0 FP64 arithmetic), ``host_loop``
         (1: the solve loop iterates from the host, one graph per iteration),
         ``fused_descent`` (1: the last pre-smoothing pass of a descent step
-        also forms and restricts the residual, 0: separate kernels)."""
+        also forms and restricts the residual, 0: separate kernels),
+        ``fused_update`` (1: the cycle's last level-1 post-smoothing pass
+        also applies the FP64 solution update, 0: a separate kernel)."""
         self._check(self._L.cfmg_set_option(self._h, _lib.OPTIONS[name], int(value)))
 
     def set_stream(self, stream_ptr: Optional[int]):

@@ -54,6 +54,10 @@ struct cfmg_handle {
   std::unordered_map<std::string, int> prog_cache;
   bool tb_on = true;  // temporally blocked FP32 smoothing on fine levels
   bool fuse_on = true;  // V-cycle descent: residual and restriction in the last pre-smoothing pass
+  // mixed loop: the FP64 solution update in the cycle's last level-1
+  // post-smoothing pass (upd_on); upd_req while a cycle runs that allows it,
+  // upd_now for that pass, upd_done once it ran
+  bool upd_on = true, upd_req = false, upd_now = false, upd_done = false;
   int tb_version = 5;  // 5: lean packed FP32x2 passes, 3: first packed form, 1: scalar passes
   int coarsest_fp64 = -1;  // mixed form: -1 FP64 when the coarsest level is small, 0 never, 1 always
   // adjoint scratch (level-1 FP64 arrays, allocated on the first cfmg_adjoint)
@@ -440,13 +444,20 @@ int smooth_tb(cfmg_handle* h, int lev, int nite) {
       left -= n;
       continue;
     }
+    bool upd = false;
     {
       Launch k(h, CFMG_K_SWEEP, lev, CFMG_MIXED);
-      launch_smooth_tb(h->tb_version, stencil, n, v.x, v.y, v.b, v.widiag, (float)(1.0 - h->d.omega), l.tx, l.ty,
-                       l.tz, l.nh,
-                       l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, h->stream);
+      // the cycle's last pass on level 1 may take the FP64 solution update
+      if (h->upd_now && left == n && h->tb_version >= 5)
+        upd = launch_smooth_tb_upd(stencil, n, v.x, v.b, v.widiag, (float)(1.0 - h->d.omega), l.tx, l.ty, l.tz, l.nh,
+                                   l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, l.x, h->dscal, h->stream);
+      if (!upd)
+        launch_smooth_tb(h->tb_version, stencil, n, v.x, v.y, v.b, v.widiag, (float)(1.0 - h->d.omega), l.tx, l.ty,
+                         l.tz, l.nh,
+                         l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, h->stream);
     }
-    l.xswap ^= 1;
+    if (upd) h->upd_done = true;  // the FP32 result was not stored: the buffers stay as they were
+    else l.xswap ^= 1;
     left -= n;
   }
   LAUNCH_OK(h);
@@ -675,7 +686,12 @@ int vcycle_t(cfmg_handle* h, int lev0) {
   TRY(coarsest_t<T>(h, d.ndeepest));
   for (int lev = nl - 1; lev >= lev0; --lev) {
     TRY(prolong_t<T>(h, lev));
-    TRY(smooth_t<T>(h, lev, d.npost));
+    // level 1's post-smoothing is the cycle's last step: with upd_req its
+    // last pass may also apply the FP64 solution update
+    h->upd_now = sizeof(T) == 4 && lev == 1 && h->upd_req;
+    const int st = smooth_t<T>(h, lev, d.npost);
+    h->upd_now = false;
+    if (st != CFMG_OK) return st;
   }
   return CFMG_OK;
 }
@@ -1081,8 +1097,13 @@ int mixed_iteration(cfmg_handle* h, int kind) {
   if (fused_ok(h)) {  // the right-hand side was made by the previous fused pass
     const Level& l1 = h->lv[0];
     if (!lazy) TRY(zero_t<float>(h, 1, CFMG_X));
-    TRY(cycle_t<float>(h, kind, lazy));
-    {
+    // the update with max |x| can run in the cycle's last level-1 pass
+    h->upd_req = h->upd_on && int_path(h);
+    h->upd_done = false;
+    const int st = cycle_t<float>(h, kind, lazy);
+    h->upd_req = false;
+    if (st != CFMG_OK) return st;
+    if (!h->upd_done) {
       Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED);
       if (int_path(h)) launch_update_scaled_max(l1.x, view<float>(l1).x, h->dscal, (long long)l1.len, h->stream);
       else launch_update_scaled(l1.x, view<float>(l1).x, h->dscal + S_ICUR, (long long)l1.len, h->stream);
@@ -1721,10 +1742,16 @@ int cfmg_solve(cfmg_handle* h, double* res_out, int* nite_out, double* history) 
   LAUNCH_OK(h);
   if (prec == CFMG_MIXED && fused_ok(h)) {
     init_scale<<<1, 1, 0, h->stream>>>(h->dscal);  // the first right-hand side is scaled from |b|
-    if (int_path(h)) {  // fixed-point range of the first pass: max |x|, max |b|
+    if (int_path(h)) {
+      // fixed-point range of the first pass: max |x|, max |b|; and max |x|
+      // outside the update box U, which no update changes: each iteration's
+      // max |x| starts from it (the update in a smoothing pass sees U only)
       CUDA_OK(h, cudaMemsetAsync(h->dscal + S_MAXX, 0, 2 * sizeof(double), h->stream));
+      CUDA_OK(h, cudaMemsetAsync(h->dscal + S_MAXO, 0, sizeof(double), h->stream));
       launch_maxabs2(l1.x, l1.b, (long long)l1.len, h->dscal, h->stream);
-      h->launches += 1;
+      launch_maxabs_outside(l1.x, l1.tx, l1.ty, (long long)l1.len, l1.nh, l1.nx + l1.nh + 1, l1.nh, l1.ny + l1.nh + 1,
+                            h->dscal, h->stream);
+      h->launches += 2;
     }
     TRY(fused_residual(h));
   } else {
@@ -2394,6 +2421,11 @@ int cfmg_set_option(cfmg_handle* h, int option, long long value) {
   }
   if (option == CFMG_OPT_FUSED_DESCENT) {
     h->fuse_on = value != 0;
+    drop_graphs(h);
+    return CFMG_OK;
+  }
+  if (option == CFMG_OPT_FUSED_UPDATE) {
+    h->upd_on = value != 0;
     drop_graphs(h);
     return CFMG_OK;
   }

@@ -199,9 +199,17 @@ struct TbEpi {
   int ctx;             // coarse row stride
   int ci0, ci1, cj0, cj1;  // coarse interior box (1-based, inclusive)
   int pkind;           // restriction: 0 cell centres (2 x 2 sum), 2 vertices (1-2-1 x 1-2-1)
+  double* xd;          // solution-update form: the level's FP64 x, updated in place
+  double* ds;          // solution-update form: the handle's device scalars (S_ICUR, S_MAXX)
 };
 bool launch_smooth_tb_epi(int stencil, int nite, const float* x, float* xo, const float* b, const float* w, float cff,
                           int tx, int ty, int ui0, int ui1, int uj0, int uj1, const TbEpi& ep, cudaStream_t s);
+// The last post-smoothing pass of a mixed-precision cycle on level 1 (2D,
+// 1..3 pairs) with the FP64 solution update x += e * iscale in its output
+// phase instead of storing e; max |x| of the updated cells goes to
+// ds[S_MAXX]. False: no such form for these arguments.
+bool launch_smooth_tb_upd(int stencil, int nite, const float* x, const float* b, const float* w, float cff, int tx,
+                          int ty, int nz, int ui0, int ui1, int uj0, int uj1, double* xd, double* ds, cudaStream_t s);
 
 // ---- batched solver (k_batch.cu): independent 2D instances advance in
 // lockstep, one launch per step of the iteration for all of them. Every
@@ -274,7 +282,7 @@ void launch_bcond(cudaGraphConditionalHandle hc, int* nactive, cudaStream_t s);
 // device scalars of a handle (dscal[])
 enum Scal { S_NORM = 0, S_RES = 1, S_NORMB = 2, S_NWET = 3, S_SCALE = 4, S_MEAN = 5, S_TMP0 = 6, S_ISCALE = 7,
             S_NEXT = 8, S_CUR = 9, S_ICUR = 10, S_MEAN2 = 11, S_MAXX = 12, S_MAXB = 13, S_NITE = 14,
-            S_SHIFT = 15, S_COUNT = 16 };
+            S_SHIFT = 15, S_MAXO = 16, S_COUNT = 17 };
 
 // fused FP64 steps of the mixed loop (k_mixed.cu)
 void launch_resid_fused(int kind, double* r, const double* x, const double* b, const double* d, const uint8_t* m,
@@ -296,6 +304,8 @@ void launch_rhs32_shift(const uint8_t* m, const double* mean_scale, float* b32, 
                         cudaStream_t s);
 void launch_make_dq(const double* diag, const uint8_t* m, double Q, int8_t* dq, long long n, int* ok, cudaStream_t s);
 void launch_maxabs2(const double* x, const double* b, long long n, double* ds, cudaStream_t s);
+void launch_maxabs_outside(const double* x, int tx, int ty, long long n, int ui0, int ui1, int uj0, int uj1, double* ds,
+                           cudaStream_t s);
 void launch_update_scaled_max(double* x, const float* e, double* ds, long long n, cudaStream_t s);
 
 // message returned by cfmg_last_error(NULL) (cfmg_api.cu)

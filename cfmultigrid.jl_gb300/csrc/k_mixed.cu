@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(kMxParts) k_fused_final(const double* __restri
     int e = 0;
     if (rms > 0 && isfinite(rms)) frexp(rms, &e);
     ds[S_NEXT] = ldexp(1.0, -e);
-    ds[S_MAXX] = 0.0;  // the next update collects max |x| afresh
+    ds[S_MAXX] = ds[S_MAXO];  // the next update collects max |x| from max |x| outside U
     // the wet mean in units of the right-hand side, as an FP32 value
     *reinterpret_cast<float*>(ds + S_SHIFT) = (float)(ds[S_MEAN2] * used);
   }
@@ -527,6 +527,25 @@ __global__ void k_maxabs2(const double* __restrict__ x, const double* __restrict
   }
 }
 
+// max |x| over the cells outside the box U = [ui0, ui1] x [uj0, uj1] of
+// every layer (1-based) into ds[S_MAXO], which starts at 0
+__global__ void k_maxabs_outside(const double* __restrict__ x, int tx, int ty, long long n, int ui0, int ui1, int uj0,
+                                 int uj1, double* ds) {
+  unsigned long long mx = 0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % tx) + 1, j = (int)((t / tx) % ty) + 1;
+    if (i >= ui0 && i <= ui1 && j >= uj0 && j <= uj1) continue;
+    const unsigned long long ux = (unsigned long long)__double_as_longlong(x[t]) & 0x7FFFFFFFFFFFFFFFULL;
+    mx = ux > mx ? ux : mx;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long ox = __shfl_down_sync(0xffffffffu, mx, o);
+    mx = ox > mx ? ox : mx;
+  }
+  if ((threadIdx.x & 31) == 0 && mx) atomicMax((unsigned long long*)(ds + S_MAXO), mx);
+}
+
 // x += e * iscale, with max |x| of the result into ds[S_MAXX] (reset by the
 // fused pass's final reduction): a grid-stride pass of 4 blocks per SM,
 // one atomic per block
@@ -597,6 +616,11 @@ void launch_make_dq(const double* diag, const uint8_t* m, double Q, int8_t* dq, 
 
 void launch_maxabs2(const double* x, const double* b, long long n, double* ds, cudaStream_t s) {
   k_maxabs2<<<1024, 256, 0, s>>>(x, b, n, ds);
+}
+
+void launch_maxabs_outside(const double* x, int tx, int ty, long long n, int ui0, int ui1, int uj0, int uj1, double* ds,
+                           cudaStream_t s) {
+  k_maxabs_outside<<<1024, 256, 0, s>>>(x, tx, ty, n, ui0, ui1, uj0, uj1, ds);
 }
 
 void launch_update_scaled_max(double* x, const float* e, double* ds, long long n, cudaStream_t s) {

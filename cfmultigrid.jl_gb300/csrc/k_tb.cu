@@ -428,7 +428,13 @@ __device__ __forceinline__ void tb5_resid(const float* __restrict__ src, float* 
 // periodic image, so the sweeps see the periodic domain. With nh >= 2 that
 // is what the reference's interior gets from its linear-range sweeps with a
 // fill! after each pair; the caller fills the halo columns after the pass.
-template <int ST, int NITE, int TY, int ROWS, int MINB, bool EPI, bool PER = false>
+//
+// UPD (the last post-smoothing pass of a mixed-precision cycle on level 1):
+// the smoothed FP32 correction e is not stored; the pass applies the FP64
+// solution update x += e * iscale to the core cells of U instead, with the
+// arithmetic of k_update_scaled_max, and collects max |x| of the results
+// into ds[S_MAXX]. Outside U e is +0, so those cells keep their value.
+template <int ST, int NITE, int TY, int ROWS, int MINB, bool EPI, bool PER = false, bool UPD = false>
 __global__ void __launch_bounds__(kT5Tx * TY, MINB) k_smooth_tb5(const float* __restrict__ x, float* __restrict__ xo,
                                                                  const float* __restrict__ b,
                                                                  const float* __restrict__ w, float cff, int tx,
@@ -605,6 +611,66 @@ __global__ void __launch_bounds__(kT5Tx * TY, MINB) k_smooth_tb5(const float* __
     }
   }
   // 2*NITE sweeps: the result is in P0; write the core cells of U
+  if constexpr (UPD) {
+    const double is = ep.ds[S_ICUR];
+    const int pe = pow2_exponent(is);  // iscale = 2^pe
+    unsigned long long mx = 0;
+    auto upd = [&](double xv, float e) {
+      const double v = __dadd_rn(xv, f2d_pow2(e, pe, is));
+      const unsigned long long ub = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFULL;
+      mx = ub > mx ? ub : mx;
+      return v;
+    };
+    if (fast) {
+      if (2 * lx >= H && 2 * lx < kT5W - H) {
+        double2* xp = reinterpret_cast<double2*>(ep.xd + I0);
+        const int st = tx >> 1;
+        double2 xv[ROWS];
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {  // all loads in flight before the first use
+          const int lj = r0 + r;
+          if (lj >= H && lj < TH - H) xv[r] = xp[r * st];
+        }
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+          const int lj = r0 + r;
+          if (lj >= H && lj < TH - H)
+            xp[r * st] = make_double2(upd(xv[r].x, prow[r * kT5Row + 1]), upd(xv[r].y, prow[r * kT5Row + kT5Half + 1]));
+        }
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < ROWS; ++r) {
+        const int lj = r0 + r;
+        if (lj < H || lj >= TH - H) continue;
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const int lc = 2 * lx + e;
+          if (lc >= H && lc < kT5W - H && (inU >> (2 * r + e) & 1u) && (!PER || gi0 + e <= ui1)) {
+            const long long I = I0 + (long long)r * tx + e;
+            ep.xd[I] = upd(ep.xd[I], prow[r * kT5Row + e * kT5Half + 1]);
+          }
+        }
+      }
+    }
+    // max over the CTA, one atomic (bit patterns of non-negative doubles order like the values)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long ox = __shfl_down_sync(0xffffffffu, mx, o);
+      mx = ox > mx ? ox : mx;
+    }
+    __shared__ unsigned long long wmx[kT5Tx * TY / 32];
+    const int tid = threadIdx.y * kT5Tx + threadIdx.x;
+    if ((tid & 31) == 0) wmx[tid >> 5] = mx;
+    __syncthreads();
+    if (tid == 0) {
+      unsigned long long m = 0;
+#pragma unroll
+      for (int w = 0; w < kT5Tx * TY / 32; ++w) m = wmx[w] > m ? wmx[w] : m;
+      if (m) atomicMax(reinterpret_cast<unsigned long long*>(ep.ds + S_MAXX), m);
+    }
+    return;
+  }
   if (fast) {
     // H is even: the pair's two cells are both core columns or neither
     if (2 * lx >= H && 2 * lx < kT5W - H) {
@@ -706,7 +772,7 @@ static void launch_tb3_n(const float* x, float* xo, const float* b, const float*
   k_smooth_tb3<ST, NITE><<<grid, dim3(kT3Tx, kT3Ty, 1), smem, s>>>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1);
 }
 
-template <int ST, int NITE, int TY, int ROWS, int MINB, bool EPI, bool PER = false>
+template <int ST, int NITE, int TY, int ROWS, int MINB, bool EPI, bool PER = false, bool UPD = false>
 static void launch_tb5_n(const float* x, float* xo, const float* b, const float* w, float cff, int tx, int ty,
                          int nz, int ui0, int ui1, int uj0, int uj1, const TbEpi& ep, cudaStream_t s) {
   constexpr int H = 2 * NITE + (EPI ? 2 : 0);
@@ -715,12 +781,12 @@ static void launch_tb5_n(const float* x, float* xo, const float* b, const float*
                       (EPI ? (size_t)TY * ROWS * kT5Tx * (sizeof(float2) + sizeof(ushort)) : 0);
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_smooth_tb5<ST, NITE, TY, ROWS, MINB, EPI, PER>,
+    cudaFuncSetAttribute(k_smooth_tb5<ST, NITE, TY, ROWS, MINB, EPI, PER, UPD>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = true;
   }
   dim3 grid((unsigned)((ui1 - ui0 + CW) / CW), (unsigned)((uj1 - uj0 + CH) / CH), (unsigned)nz);
-  k_smooth_tb5<ST, NITE, TY, ROWS, MINB, EPI, PER>
+  k_smooth_tb5<ST, NITE, TY, ROWS, MINB, EPI, PER, UPD>
       <<<grid, dim3(kT5Tx, TY, 1), smem, s>>>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1, ep);
 }
 
@@ -776,6 +842,22 @@ bool launch_smooth_tb_periodic(int nite, const float* x, float* xo, const float*
   CFMG_TBP(1) CFMG_TBP(2) CFMG_TBP(3) CFMG_TBP(4) CFMG_TBP(5)
   CFMG_TBP(6) CFMG_TBP(7) CFMG_TBP(8) CFMG_TBP(9) CFMG_TBP(10)
 #undef CFMG_TBP
+  return false;
+}
+
+bool launch_smooth_tb_upd(int stencil, int nite, const float* x, const float* b, const float* w, float cff, int tx,
+                          int ty, int nz, int ui0, int ui1, int uj0, int uj1, double* xd, double* ds, cudaStream_t s) {
+  TbEpi ep{};
+  ep.xd = xd;
+  ep.ds = ds;
+#define CFMG_TBU(ST, N)                                                                                       \
+  if (stencil == ST && nite == N) {                                                                           \
+    launch_tb5_n<ST, N, 8, 6, 2, false, false, true>(x, nullptr, b, w, cff, tx, ty, nz, ui0, ui1, uj0, uj1, ep, s); \
+    return true;                                                                                              \
+  }
+  CFMG_TBU(5, 1) CFMG_TBU(5, 2) CFMG_TBU(5, 3)
+  CFMG_TBU(9, 1) CFMG_TBU(9, 2) CFMG_TBU(9, 3)
+#undef CFMG_TBU
   return false;
 }
 

@@ -117,6 +117,11 @@ extern "C" {
                                     the last pre-smoothing pass of a cycle's descent step also forms
                                     the residual, restricts it to the coarse b and zeroes the coarse x;
                                     0 separate kernels. Both give the same bits. */
+#define CFMG_OPT_FUSED_UPDATE 6 /* mixed form, 2D closed topology, integer residual, lean packed passes:
+                                   1 (default) the cycle's last level-1 post-smoothing pass also applies
+                                   the FP64 solution update x += e * iscale (and collects max |x|)
+                                   instead of storing the FP32 correction; 0 a separate kernel. Both give
+                                   the same bits. */
 
 typedef struct cfmg_desc {
   int kase;     /* CFMG_TWOD / CFMG_THREED            (Param.case) */

@@ -140,15 +140,20 @@ def test_temporal_blocking_is_bit_identical(name):
     base, mkind = {**CASES, **BIG_CASES}[name]
     out = []
     # packed FP32x2 passes (lean form with and without the fused residual and
-    # restriction, first form; 3D: + streaming passes), scalar passes, one
+    # restriction, with and without the FP64 solution update in the last
+    # level-1 pass; first form; 3D: + streaming passes), scalar passes, one
     # kernel per sweep
-    runs = ((4, 1), (1, 1), (0, 1)) if base.get("case") == "threed" else ((5, 1), (5, 0), (3, 1), (1, 1), (0, 1))
-    for tb, fuse in runs:
+    if base.get("case") == "threed":
+        runs = ((4, 1, 1), (1, 1, 1), (0, 1, 1))
+    else:
+        runs = ((5, 1, 1), (5, 1, 0), (5, 0, 1), (3, 1, 1), (1, 1, 1), (0, 1, 1))
+    for tb, fuse, upd in runs:
         mg = cfmg.get_gmg(cfmg.Param(**base, tol=1e-10, maxite=40, residual_norm="l2", precision="mixed",
                                      verbose=False))
         mg.set_option("engine_cells", 2000)  # keep the fine levels out of the engine
         mg.set_option("temporal_blocking", tb)
         mg.set_option("fused_descent", fuse)
+        mg.set_option("fused_update", upd)
         shape = mg.shape(1)
         custom = _mask(base, shape, mkind)
         if custom is not None:
@@ -273,3 +278,38 @@ def test_fused_descent_profile_class():
     assert counts[1]["descent"] > 0 and counts[1]["sweep"] > 0 and counts[1]["residual"] == 0, counts
     assert counts[0]["descent"] == 0 and counts[0]["residual"] > 0, counts
     assert counts[0]["sweep"] == counts[1]["sweep"] + counts[1]["descent"], counts
+
+
+def test_fused_update_replaces_the_update_kernel():
+    """With the FP64 solution update in the cycle's last level-1
+    post-smoothing pass, the separate update kernel (a level-1 conversion
+    launch) no longer runs, one fewer per iteration, and the solve is the
+    same bit for bit."""
+    base, mkind = CASES["config2_512_vertices_lap9_f"]
+    mg = cfmg.get_gmg(cfmg.Param(**base, tol=1e-10, maxite=40, residual_norm="l2", precision="mixed", verbose=False))
+    shape = mg.shape(1)
+    mg.oper[1].msk = _mask(base, shape, mkind)
+    cfmg.setup_operators(mg)
+    for lev in range(1, mg.nlevels + 1):
+        for f in ("x", "y", "r", "b"):
+            cfmg.set_to_zero(mg, lev, f)
+    msk = mg.download(1, "msk").astype(np.float64)
+    b = np.asfortranarray(np.random.default_rng(5).standard_normal(shape)) * msk
+    F.subtract_mean(b, msk)
+    mg.data[1].b = b
+    out = {}
+    for upd in (1, 0):
+        mg.set_option("fused_update", upd)
+        got = {}
+
+        def solve():
+            cfmg.set_to_zero(mg, 1, "x")
+            got["r"] = cfmg.solve(mg, history=True)
+
+        nconv, _ = _profile(mg, "convert", 1, "mixed", solve)
+        out[upd] = (nconv, got["r"], mg.data[1].x)
+    (c1, (r1, n1, h1), x1), (c0, (r0, n0, h0), x0) = out[1], out[0]
+    assert r1 <= 1e-10 and n1 == n0, (r1, n1, n0)
+    assert c0 - c1 == n0, (c0, c1, n0)
+    assert np.array_equal(h1, h0)
+    assert np.array_equal(x1, x0)
