@@ -1748,10 +1748,9 @@ int cfmg_solve(cfmg_handle* h, double* res_out, int* nite_out, double* history) 
       // max |x| starts from it (the update in a smoothing pass sees U only)
       CUDA_OK(h, cudaMemsetAsync(h->dscal + S_MAXX, 0, 2 * sizeof(double), h->stream));
       CUDA_OK(h, cudaMemsetAsync(h->dscal + S_MAXO, 0, sizeof(double), h->stream));
-      launch_maxabs2(l1.x, l1.b, (long long)l1.len, h->dscal, h->stream);
-      launch_maxabs_outside(l1.x, l1.tx, l1.ty, (long long)l1.len, l1.nh, l1.nx + l1.nh + 1, l1.nh, l1.ny + l1.nh + 1,
-                            h->dscal, h->stream);
-      h->launches += 2;
+      launch_maxabs2(l1.x, l1.b, (long long)l1.len, l1.tx, l1.ty, l1.nh, l1.nx + l1.nh + 1, l1.nh, l1.ny + l1.nh + 1,
+                     h->dscal, h->stream);
+      h->launches += 1;
     }
     TRY(fused_residual(h));
   } else {

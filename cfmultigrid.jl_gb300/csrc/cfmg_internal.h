@@ -303,9 +303,9 @@ bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t
 void launch_rhs32_shift(const uint8_t* m, const double* mean_scale, float* b32, float* r32, long long n,
                         cudaStream_t s);
 void launch_make_dq(const double* diag, const uint8_t* m, double Q, int8_t* dq, long long n, int* ok, cudaStream_t s);
-void launch_maxabs2(const double* x, const double* b, long long n, double* ds, cudaStream_t s);
-void launch_maxabs_outside(const double* x, int tx, int ty, long long n, int ui0, int ui1, int uj0, int uj1, double* ds,
-                           cudaStream_t s);
+// max |x|, max |b| and max |x| outside the box U of every layer (S_MAXX, S_MAXB, S_MAXO)
+void launch_maxabs2(const double* x, const double* b, long long n, int tx, int ty, int ui0, int ui1, int uj0, int uj1,
+                    double* ds, cudaStream_t s);
 void launch_update_scaled_max(double* x, const float* e, double* ds, long long n, cudaStream_t s);
 
 // message returned by cfmg_last_error(NULL) (cfmg_api.cu)

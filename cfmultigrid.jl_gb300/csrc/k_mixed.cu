@@ -506,44 +506,40 @@ __global__ void k_make_dq(const double* __restrict__ diag, const uint8_t* __rest
 }
 
 // max |x| and max |b| (as the bit patterns of non-negative doubles, which
-// order like the values) into ds[S_MAXX], ds[S_MAXB]; both start at 0
-__global__ void k_maxabs2(const double* __restrict__ x, const double* __restrict__ b, long long n, double* ds) {
-  unsigned long long mx = 0, mb = 0;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const unsigned long long ux = (unsigned long long)__double_as_longlong(x[t]) & 0x7FFFFFFFFFFFFFFFULL;
-    const unsigned long long ub = (unsigned long long)__double_as_longlong(b[t]) & 0x7FFFFFFFFFFFFFFFULL;
-    mx = ux > mx ? ux : mx;
-    mb = ub > mb ? ub : mb;
+// order like the values) into ds[S_MAXX], ds[S_MAXB], and max |x| over the
+// cells outside the box U = [ui0, ui1] x [uj0, uj1] of every layer (1-based;
+// tx, ty the array's row and plane extents) into ds[S_MAXO]; all start at 0
+__global__ void k_maxabs2(const double* __restrict__ x, const double* __restrict__ b, long long n, int tx, int ty,
+                          int ui0, int ui1, int uj0, int uj1, double* ds) {
+  unsigned long long mx = 0, mb = 0, mo = 0;
+  const long long nrows = n / tx;  // rows of all layers
+  for (long long row = blockIdx.x; row < nrows; row += gridDim.x) {
+    const int j = (int)(row % ty) + 1;
+    const bool row_u = j >= uj0 && j <= uj1;
+    const double* xr = x + row * tx;
+    const double* br = b + row * tx;
+    for (int i0 = threadIdx.x; i0 < tx; i0 += blockDim.x) {
+      const unsigned long long ux = (unsigned long long)__double_as_longlong(xr[i0]) & 0x7FFFFFFFFFFFFFFFULL;
+      const unsigned long long ub = (unsigned long long)__double_as_longlong(br[i0]) & 0x7FFFFFFFFFFFFFFFULL;
+      const bool in_u = row_u && i0 + 1 >= ui0 && i0 + 1 <= ui1;
+      mx = ux > mx ? ux : mx;
+      mb = ub > mb ? ub : mb;
+      mo = (!in_u && ux > mo) ? ux : mo;
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long ox = __shfl_down_sync(0xffffffffu, mx, o), ob = __shfl_down_sync(0xffffffffu, mb, o);
+    const unsigned long long oo = __shfl_down_sync(0xffffffffu, mo, o);
     mx = ox > mx ? ox : mx;
     mb = ob > mb ? ob : mb;
+    mo = oo > mo ? oo : mo;
   }
   if ((threadIdx.x & 31) == 0) {
     atomicMax((unsigned long long*)(ds + S_MAXX), mx);
     atomicMax((unsigned long long*)(ds + S_MAXB), mb);
+    if (mo) atomicMax((unsigned long long*)(ds + S_MAXO), mo);
   }
-}
-
-// max |x| over the cells outside the box U = [ui0, ui1] x [uj0, uj1] of
-// every layer (1-based) into ds[S_MAXO], which starts at 0
-__global__ void k_maxabs_outside(const double* __restrict__ x, int tx, int ty, long long n, int ui0, int ui1, int uj0,
-                                 int uj1, double* ds) {
-  unsigned long long mx = 0;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % tx) + 1, j = (int)((t / tx) % ty) + 1;
-    if (i >= ui0 && i <= ui1 && j >= uj0 && j <= uj1) continue;
-    const unsigned long long ux = (unsigned long long)__double_as_longlong(x[t]) & 0x7FFFFFFFFFFFFFFFULL;
-    mx = ux > mx ? ux : mx;
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long ox = __shfl_down_sync(0xffffffffu, mx, o);
-    mx = ox > mx ? ox : mx;
-  }
-  if ((threadIdx.x & 31) == 0 && mx) atomicMax((unsigned long long*)(ds + S_MAXO), mx);
 }
 
 // x += e * iscale, with max |x| of the result into ds[S_MAXX] (reset by the
@@ -614,13 +610,9 @@ void launch_make_dq(const double* diag, const uint8_t* m, double Q, int8_t* dq, 
   k_make_dq<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(diag, m, Q, dq, n, ok);
 }
 
-void launch_maxabs2(const double* x, const double* b, long long n, double* ds, cudaStream_t s) {
-  k_maxabs2<<<1024, 256, 0, s>>>(x, b, n, ds);
-}
-
-void launch_maxabs_outside(const double* x, int tx, int ty, long long n, int ui0, int ui1, int uj0, int uj1, double* ds,
-                           cudaStream_t s) {
-  k_maxabs_outside<<<1024, 256, 0, s>>>(x, tx, ty, n, ui0, ui1, uj0, uj1, ds);
+void launch_maxabs2(const double* x, const double* b, long long n, int tx, int ty, int ui0, int ui1, int uj0, int uj1,
+                    double* ds, cudaStream_t s) {
+  k_maxabs2<<<1024, 256, 0, s>>>(x, b, n, tx, ty, ui0, ui1, uj0, uj1, ds);
 }
 
 void launch_update_scaled_max(double* x, const float* e, double* ds, long long n, cudaStream_t s) {
