@@ -60,7 +60,15 @@ def parse():
                          "ncu launch list, which does not descend into conditional graph nodes)")
     ap.add_argument("--quick", action="store_true",
                     help="mixed form only: one warm-up and one timed solve (a short run for ncu)")
+    # --quick only: the earlier default forms, for ncu captures of their kernels
+    ap.add_argument("--tb", type=int, default=None, choices=[0, 1, 3, 5],
+                    help="--quick: FP32 smoothing form (temporal_blocking option; 5 is the default)")
+    ap.add_argument("--no-int", action="store_true", help="--quick: level-1 residual in FP64 arithmetic")
+    ap.add_argument("--no-fuse", action="store_true",
+                    help="--quick: no fused descent or fused solution update (plain smoothing passes)")
     args = ap.parse_args()
+    if (args.tb is not None or args.no_int or args.no_fuse) and not (args.quick and args.workload == "config2"):
+        ap.error("--tb, --no-int and --no-fuse go with --quick (config 2) only")
     if args.steps is None:
         args.steps = 30 if (args.impl == "ours" and args.workload == "config2") else 5
     return args
@@ -210,6 +218,13 @@ def run_ours(args, rank, world, local):
     mgm, b = make_gmg(cfmg, param, vmsk, noise, "mixed", sp)
     if args.host_loop:
         mgm.set_option("host_loop", 1)
+    if args.tb is not None:
+        mgm.set_option("temporal_blocking", args.tb)
+    if args.no_int:
+        mgm.set_option("int_residual", 0)
+    if args.no_fuse:
+        mgm.set_option("fused_descent", 0)
+        mgm.set_option("fused_update", 0)
     if args.quick:
         cfmg.set_to_zero(mgm, 1, "x")
         cfmg.solve(mgm)
