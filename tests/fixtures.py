@@ -16,6 +16,9 @@ CUDA library).
 from __future__ import annotations
 
 import dataclasses
+import hashlib
+import json
+import os
 from typing import Callable, Optional
 
 import numpy as np
@@ -240,6 +243,29 @@ RECTANGULAR = [
     test_rectangular("centers", 2.6e-13, 1e-14, 6),
     test_rectangular("vertices", 6.9e-13, 1e-14, 6),
 ]
+
+
+# Committed oracle solves (tests/golden/make_golden.py): the scenarios whose
+# inputs are computed exactly (point charges, gradients; no random right-hand
+# side), so that the oracle's result is fixed by IEEE arithmetic alone and is
+# the same on every host.
+GOLDEN_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "oracle_solves.json")
+
+
+def golden_scenarios():
+    return [sc for sc in KNOWN_ANSWERS + RECTANGULAR + list(ITERATION_ONLY) if "random" not in sc.name]
+
+
+def field_digest(a) -> str:
+    """SHA-256 of a field's FP64 values in column-major order, with -0
+    counted as +0 (the comparisons of fields treat the two as equal)."""
+    v = np.asarray(a, dtype=np.float64) + 0.0
+    return hashlib.sha256(np.ascontiguousarray(v.ravel(order="F")).tobytes()).hexdigest()
+
+
+def load_golden() -> dict:
+    with open(GOLDEN_PATH) as f:
+        return json.load(f)
 
 
 def prepare(mg, sc: Scenario):

@@ -5,7 +5,8 @@ every operator (sweep, residual, restriction, prolongation, halo fill) and
 the device-side setup coefficients are compared with ``array_equal``, and a
 whole solve must reproduce the oracle's iteration count, final x bit for bit
 and its residual history to 1e-12 relative (the norms' summation order is
-the only difference).
+the only difference). Where the scenario's oracle solve is committed
+(tests/golden), the solve is also checked against those values.
 """
 import math
 
@@ -23,6 +24,7 @@ HIST_RTOL = 1e-12
 # history entries against the oracle's sequential FP64 norm sums: the
 # oracle's own summation error on ~1e6 cells reaches ~3e-12
 HIST_RTOL_SEQ = 1e-11
+GOLDEN = F.load_golden()
 
 
 class GpuAdapter:
@@ -201,6 +203,12 @@ def _check_solve(sc, og, mg, r0, r1):
     # ~1e6 cells is itself off by up to a few 1e-12
     assert abs(res1 - _exact_ratio(mg)) <= 1e-13 * res1
     np.testing.assert_allclose(h1, h0, rtol=HIST_RTOL_SEQ, atol=0)
+    g = GOLDEN.get(sc.name)
+    if g is not None:  # the committed oracle solve
+        assert n1 == g["nite"]
+        assert F.field_digest(mg.data[1].x) == g["x_sha256"]
+        assert F.field_digest(mg.download(1, "r")) == g["r_sha256"]
+        np.testing.assert_allclose(h1, g["hist"], rtol=HIST_RTOL_SEQ, atol=0)
 
 
 @pytest.mark.parametrize("sc", F.KNOWN_ANSWERS + F.RECTANGULAR, ids=lambda s: s.name)

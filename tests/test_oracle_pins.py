@@ -10,24 +10,49 @@ import fixtures as F
 import oracle as O
 
 
+GOLDEN = F.load_golden()
+
+
 def _solve(sc):
     og = O.OracleGmg(sc.param)
     F.prepare(F.OracleAdapter(og), sc)
     return og, og.solve()
 
 
+def _check_golden(sc, og, res, nite, hist):
+    """The committed solve of the scenario (tests/golden), bit for bit."""
+    g = GOLDEN.get(sc.name)
+    if g is None:
+        return
+    assert nite == g["nite"] and res == g["res"]
+    assert [float(h) for h in hist] == g["hist"]
+    assert F.field_digest(og.x) == g["x_sha256"]
+    assert F.field_digest(og.field(1, "r")) == g["r_sha256"]
+
+
 @pytest.mark.parametrize("sc", F.KNOWN_ANSWERS + F.RECTANGULAR, ids=lambda s: s.name)
 def test_known_answer(sc):
-    _, (res, nite, hist) = _solve(sc)
+    og, (res, nite, hist) = _solve(sc)
     assert nite == sc.expect_ite
     assert abs(res - sc.expect_res) <= sc.atol, (res, sc.expect_res)
     assert hist[-1] == res and len(hist) == nite + 1
+    _check_golden(sc, og, res, nite, hist)
 
 
 @pytest.mark.parametrize("sc", F.ITERATION_ONLY, ids=lambda s: s.name)
 def test_iteration_count(sc):
-    _, (res, nite, _) = _solve(sc)
+    og, (res, nite, hist) = _solve(sc)
     assert nite == sc.expect_ite
+    _check_golden(sc, og, res, nite, hist)
+
+
+def test_golden_file_covers_the_scenarios():
+    """The committed solves are those of the current scenarios, with the
+    same parameters (regenerate with tests/golden/make_golden.py)."""
+    scs = {sc.name: sc for sc in F.golden_scenarios()}
+    assert set(GOLDEN) == set(scs)
+    for name, sc in scs.items():
+        assert GOLDEN[name]["param"] == sc.param, name
 
 
 def test_level_hierarchy_matches_create_levels():
