@@ -73,3 +73,22 @@ def test_default_mask_and_setup_coefficients():
     assert d[5, 5] == 4.0 and d[3, 3] == 2.0 and d[3, 5] == 3.0 and d[0, 0] == 0.0
     assert (og.field(2, "Rcoef") == og.field(2, "msk")).all()
     assert og.field(1, "Pcoef")[5, 5, 0] == 1.0 / 16
+
+
+def test_field_digest_sees_one_ulp_and_ignores_zero_sign():
+    """The digests of the committed solves change with any one-ulp change of
+    one cell, not with the sign of a zero, and not with the memory order of
+    the array."""
+    import numpy as np
+
+    rng = np.random.default_rng(0)
+    x = np.asfortranarray(rng.standard_normal((7, 5, 3)))
+    x[2, 3, 1] = 0.0
+    d = F.field_digest(x)
+    y = x.copy(order="F")
+    y[4, 1, 2] = np.nextafter(y[4, 1, 2], np.inf)
+    assert F.field_digest(y) != d
+    z = x.copy(order="F")
+    z[2, 3, 1] = -0.0
+    assert F.field_digest(z) == d
+    assert F.field_digest(np.ascontiguousarray(x)) == d
