@@ -20,6 +20,13 @@
 // not a device address. The device address is obtained once per device, with
 // that device current, by cudaGetSymbolAddress (on the entry point's first
 // call on that device; make that first call before any stream capture).
+// The cached address belongs to the CUDA context it was taken in: a device
+// reset (cudaDeviceReset, CUDA.device_reset! in Julia) destroys that context,
+// and the module, with its static array, is loaded again into the next one,
+// possibly at another address. Each call therefore compares the current
+// context's unique id (cuCtxGetId) with the one the address was taken under
+// and repeats the set-up when they differ; the first call after a reset is
+// then a set-up call too, and belongs before any stream capture as well.
 //
 // Every call shares the one array. Each chunk's partial is written before
 // it is read and only the chunks of the current call are read, so nothing
@@ -42,6 +49,14 @@ static __device__ __align__(256) double g_noalloc_partials[kStaticChunks];
 
 std::mutex g_mu;
 double* g_addr[kMaxDevices] = {nullptr};
+unsigned long long g_ctx_id[kMaxDevices] = {0};
+
+// Driver entry points reached through the runtime, so that the library does
+// not link libcuda itself (it must load on machines without a driver).
+typedef int (*PFN_ctxGetCurrent)(void**);
+typedef int (*PFN_ctxGetId)(void*, unsigned long long*);
+PFN_ctxGetCurrent g_ctx_get_current = nullptr;
+PFN_ctxGetId g_ctx_get_id = nullptr;
 
 // Block c sums msk*x^2 over elements [c*kChunk, min(n, (c+1)*kChunk)).
 __global__ void __launch_bounds__(kThreadsNA) k_chunk_partials(const double* __restrict__ x,
@@ -91,21 +106,50 @@ int fail_na(int code, const std::string& msg) {
   return code;
 }
 
-// Device address of the static scratch on the current device (set up once).
+// Unique id of the current CUDA context (0 when none is current yet).
+int current_context_id(unsigned long long* id) {
+  *id = 0;
+  if (!g_ctx_get_current || !g_ctx_get_id) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    void *f1 = nullptr, *f2 = nullptr;
+    cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+    cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+    if (e1 != cudaSuccess || e2 != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+        q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return fail_na(CFMG_ERR_CUDA, "cfmg_norm_noalloc: cuCtxGetCurrent/cuCtxGetId are not available");
+    g_ctx_get_current = (PFN_ctxGetCurrent)f1;
+    g_ctx_get_id = (PFN_ctxGetId)f2;
+  }
+  void* ctx = nullptr;
+  if (g_ctx_get_current(&ctx) != 0)
+    return fail_na(CFMG_ERR_CUDA, "cfmg_norm_noalloc: cuCtxGetCurrent failed");
+  if (ctx && g_ctx_get_id(ctx, id) != 0) return fail_na(CFMG_ERR_CUDA, "cfmg_norm_noalloc: cuCtxGetId failed");
+  return CFMG_OK;
+}
+
+// Device address of the static scratch on the current device. Set up once
+// per device and context: repeated only when the context has changed.
 int scratch_address(double** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return fail_na(CFMG_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return fail_na(CFMG_ERR_UNSUPPORTED, "device index beyond 63");
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_addr[dev]) {
+  unsigned long long ctx = 0;
+  int rc = current_context_id(&ctx);
+  if (rc != CFMG_OK) return rc;
+  if (!g_addr[dev] || ctx == 0 || ctx != g_ctx_id[dev]) {
     double* p = nullptr;
     e = cudaGetSymbolAddress((void**)&p, g_noalloc_partials);
     if (e != cudaSuccess) {
       set_global_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
       return CFMG_ERR_CUDA;
     }
+    // cudaGetSymbolAddress made the runtime's context current if none was.
+    rc = current_context_id(&ctx);
+    if (rc != CFMG_OK) return rc;
     g_addr[dev] = p;
+    g_ctx_id[dev] = ctx;
   }
   *out = g_addr[dev];
   return CFMG_OK;
@@ -119,7 +163,8 @@ using namespace cfmg;
 
 extern "C" int cfmg_norm_noalloc(const double* x, const uint8_t* msk, long long n, double* out, void* stream) {
   if (!x || !msk || !out) return fail_na(CFMG_ERR_ARG, "cfmg_norm_noalloc: null pointer");
-  if (n < 0 || n > kMaxElems)
+  if (n < 0) return fail_na(CFMG_ERR_ARG, "cfmg_norm_noalloc: negative n = " + std::to_string(n));
+  if (n > kMaxElems)
     return fail_na(CFMG_ERR_ARG, "cfmg_norm_noalloc: n = " + std::to_string(n) + " exceeds the static scratch limit of " +
                                      std::to_string(kMaxElems) + " elements");
   double* partials = nullptr;

@@ -266,7 +266,9 @@ CFMG_API int cfmg_profile_read(cfmg_handle* h, long long* launches, double* tota
  * Its scratch is a static device array of 4096 doubles (32 KB) held on every
  * GPU that loads the library; n is limited to CFMG_NOALLOC_MAX_ELEMS and
  * larger n is rejected with CFMG_ERR_ARG. The first call on a device looks
- * up that array's device address; make it before any stream capture.
+ * up that array's device address; make it before any stream capture. The
+ * address is kept per device and CUDA context: a device reset drops it, and
+ * the next call looks it up again (so it, too, belongs before a capture).
  * Calls that overlap on the GPU race on the shared scratch. No cudaMalloc,
  * cudaFree or allocating library routine is called. Errors:
  * cfmg_last_error(NULL). */

@@ -55,3 +55,10 @@ def test_norm_noalloc_rejects_oversize():
                              ctypes.c_void_p(16), None)
     assert rc == cfmg._lib.ERR_ARG
     assert b"exceeds the static scratch limit" in L.cfmg_last_error(None)
+
+
+def test_norm_noalloc_rejects_negative_n():
+    L = cfmg._lib.load()
+    rc = L.cfmg_norm_noalloc(ctypes.c_void_p(16), ctypes.c_void_p(16), ctypes.c_longlong(-1), ctypes.c_void_p(16), None)
+    assert rc == cfmg._lib.ERR_ARG
+    assert b"negative n" in L.cfmg_last_error(None)
