@@ -7,7 +7,8 @@ import os
 import sys
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-for p in (ROOT, os.path.join(ROOT, "cfmultigrid.jl_gb300"), os.path.join(ROOT, "oracle"), os.path.dirname(__file__)):
+for p in (ROOT, os.path.join(ROOT, "cfmultigrid.jl_gb300"), os.path.join(ROOT, "oracle"), os.path.dirname(__file__),
+          os.path.join(os.path.dirname(__file__), "golden")):
     if p not in sys.path:
         sys.path.insert(0, p)
 

@@ -1,10 +1,12 @@
 """Writes oracle_solves.json: the CPU oracle's solves of the scenarios of
 ``fixtures.golden_scenarios()`` (the reference suite's known-answer cases,
-the rectangular pair and the iteration-count cases with exactly computed
-right-hand sides).
+the rectangular pair, the iteration-count cases with exactly computed
+right-hand sides, and the plain-method configuration 1 with its seeded
+N(0,1) right-hand side).
 
 Per scenario: the iteration count, the final residual ratio, the residual
-history of every iteration, and SHA-256 digests of the final level-1 x and r
+history of every iteration, and SHA-256 digests of the right-hand side and
+of the final level-1 x and r
 (``fixtures.field_digest``). The oracle's pointwise arithmetic and its
 sequential norms are plain IEEE FP64 operations on exactly representable
 inputs, so the values do not depend on the host.
@@ -28,10 +30,11 @@ import oracle as O  # noqa: E402
 
 def solve(sc):
     og = O.OracleGmg(sc.param)
-    F.prepare(F.OracleAdapter(og), sc)
+    b = F.prepare(F.OracleAdapter(og), sc)
     res, nite, hist = og.solve()
     x = og.x
     return {
+        "b_sha256": F.field_digest(b),
         "param": sc.param,
         "nite": int(nite),
         "res": float(res),

@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 import fixtures as F
+import oracle as O
 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -113,3 +114,63 @@ def test_batch_vertex_9point_matches_single_solves():
         assert np.linalg.norm(a - c) <= 1e-6 * np.linalg.norm(c), i
     res2, nite2, _ = batch.solve(from_zero=False)
     assert np.all(nite2 == 0) and np.all(res2 <= 1e-10), (nite2, res2)
+
+
+def _oracle_solve(p, n, nlev, msk, noise, maxite):
+    """The oracle's FP64 solve of one batch instance (same mask, coarse
+    hierarchy and right-hand side), to the same 1e-10 in ||r||/||b||, i.e.
+    1e-20 in the reference's squared ratio (src/gmg_solver.jl:29-39)."""
+    og = O.OracleGmg(dict(nx=n, ny=n, nz=1, case="twod", location=p.location, operator=p.operator, cycle=p.cycle,
+                          npre=p.npre, npost=p.npost, omega=p.omega, ndeepest=p.ndeepest, nlevels=nlev,
+                          tol=p.tol * p.tol, maxite=maxite))
+    og.field(1, "msk")[...] = msk
+    og.setup_operators()
+    for lev in range(1, og.nlevels + 1):
+        for f in ("x", "y", "r", "b"):
+            og.field(lev, f)[...] = 0.0
+    m = og.field(1, "msk").astype(np.float64)
+    b = np.asfortranarray(noise * m)
+    F.subtract_mean(b, m)
+    og.field(1, "b")[...] = b
+    res, nite, _ = og.solve()
+    return og, res ** 0.5, nite
+
+
+@pytest.mark.parametrize("cycle", ["v", "f"])
+def test_batch_against_oracle(cycle):
+    """A config-4-style batch (16 instances, sizes log-uniform in 64..320
+    rounded to 32, disk and smoothed-noise coastline masks, N(0,1) right-hand
+    sides, mixed precision, 1e-10) against the oracle's FP64 solve of each
+    instance: the batched x has a true residual (recomputed by the oracle
+    in FP64) at the tolerance, the iteration count is the oracle's within
+    one, and the solution is the oracle's to 1e-6 after wet-mean removal."""
+    probs = W.config4(ninst=16, seed=5, lo=64, hi=320)
+    kinds = {"disk" if q[2][q[0] // 2 + 3, 3, 0] == 0 and q[2][q[0] // 2 + 3, q[0] // 2 + 3, 0] else "noise"
+             for q in probs}
+    maxite = 150
+    p = _param(cycle=cycle, maxite=maxite)
+    batch = cfmg.Batch(p, [q[0] for q in probs], [q[0] for q in probs], [q[1] for q in probs])
+    for i, (n, nlev, msk, noise) in enumerate(probs):
+        _setup(batch.instance(i), msk, noise)
+    res, nite, _ = batch.solve()
+    converged = 0
+    for i, (n, nlev, msk, noise) in enumerate(probs):
+        og, ores, onite = _oracle_solve(p, n, nlev, msk, noise, maxite)
+        g = batch.instance(i)
+        assert np.array_equal(og.field(1, "msk"), g.download(1, "msk")), i
+        if ores > 1e-10:  # the oracle does not converge within maxite: neither may the batch
+            assert res[i] > 1e-10 and nite[i] == maxite, (i, res[i], nite[i])
+            continue
+        converged += 1
+        assert abs(int(nite[i]) - onite) <= 1, (i, nite[i], onite)
+        x = g.data[1].x
+        ox = og.x.copy(order="F")
+        # the batched solution's true residual, in the oracle's FP64 arithmetic
+        og.field(1, "x")[...] = x
+        true = og.normresidual(og.norm(1, "b")) ** 0.5
+        assert true <= 1e-10 * (1 + 1e-3), (i, true, res[i])
+        w = og.field(1, "msk").astype(bool)
+        a, c = x[w] - x[w].mean(), ox[w] - ox[w].mean()
+        assert np.linalg.norm(a - c) <= 1e-6 * np.linalg.norm(c), (i, np.linalg.norm(a - c) / np.linalg.norm(c))
+    assert converged >= 12, converged
+    assert len(kinds) == 2

@@ -177,7 +177,7 @@ def _solve_pair(sc, **gpu_kw):
     F.prepare(F.OracleAdapter(og), sc)
     r0 = og.solve()
     mg = cfmg.get_gmg(gpu_param(sc.param, **gpu_kw))
-    F.prepare(GpuAdapter(mg), sc)
+    mg.b_in = F.prepare(GpuAdapter(mg), sc)
     r1 = cfmg.solve(mg, history=True)
     return og, mg, r0, r1
 
@@ -205,6 +205,7 @@ def _check_solve(sc, og, mg, r0, r1):
     np.testing.assert_allclose(h1, h0, rtol=HIST_RTOL_SEQ, atol=0)
     g = GOLDEN.get(sc.name)
     if g is not None:  # the committed oracle solve
+        assert F.field_digest(mg.b_in) == g["b_sha256"]
         assert n1 == g["nite"]
         assert F.field_digest(mg.data[1].x) == g["x_sha256"]
         assert F.field_digest(mg.download(1, "r")) == g["r_sha256"]
@@ -224,3 +225,24 @@ def test_iteration_only_solve(sc):
     og, mg, r0, r1 = _solve_pair(sc)
     assert r1[1] == sc.expect_ite
     _check_solve(sc, og, mg, r0, r1)
+
+
+@pytest.mark.parametrize("host_loop", [0, 1])
+def test_config1_plain_method_exact(host_loop):
+    """Configuration 1 exactly as stated (256^2 cell-centred 5-point, disk
+    0.45 N, seed-0 N(0,1) right-hand side, V-cycle 2/2, 6 levels, omega 0.8,
+    1e-10 relative residual) in the FP64 drop-in: the oracle's iteration
+    count, x and r bit for bit, and the residual history within 1e-12
+    relative (68,644 cells: the sequential sum's own error is far below it),
+    also against the committed oracle solve. host_loop 1: one graph launch
+    per iteration instead of the device-side loop."""
+    sc = F.CONFIG1
+    og, mg, r0, r1 = _solve_pair(sc)
+    if host_loop:
+        mg.set_option("host_loop", 1)
+        cfmg.set_to_zero(mg, 1, "x")
+        r1 = cfmg.solve(mg, history=True)
+    _check_solve(sc, og, mg, r0, r1)
+    np.testing.assert_allclose(r1[2], r0[2], rtol=HIST_RTOL, atol=0)
+    np.testing.assert_allclose(r1[2], GOLDEN[sc.name]["hist"], rtol=HIST_RTOL, atol=0)
+    assert r1[0] <= sc.param["tol"]

@@ -4,6 +4,7 @@ Each case replays one Julia test (file:line in tests/fixtures.py) on the
 oracle and checks (res, ite) with the reference's own tolerance. This pins
 the oracle before any GPU result is compared with it.
 """
+import numpy as np
 import pytest
 
 import fixtures as F
@@ -15,7 +16,7 @@ GOLDEN = F.load_golden()
 
 def _solve(sc):
     og = O.OracleGmg(sc.param)
-    F.prepare(F.OracleAdapter(og), sc)
+    og.b_in = F.prepare(F.OracleAdapter(og), sc)
     return og, og.solve()
 
 
@@ -24,6 +25,7 @@ def _check_golden(sc, og, res, nite, hist):
     g = GOLDEN.get(sc.name)
     if g is None:
         return
+    assert F.field_digest(og.b_in) == g["b_sha256"]
     assert nite == g["nite"] and res == g["res"]
     assert [float(h) for h in hist] == g["hist"]
     assert F.field_digest(og.x) == g["x_sha256"]
@@ -92,3 +94,42 @@ def test_field_digest_sees_one_ulp_and_ignores_zero_sign():
     z[2, 3, 1] = -0.0
     assert F.field_digest(z) == d
     assert F.field_digest(np.ascontiguousarray(x)) == d
+
+
+def test_config1_plain_method():
+    """Configuration 1 as stated (256^2 cell-centred 5-point, disk 0.45 N,
+    seed-0 N(0,1) right-hand side, V-cycle 2/2, 6 levels, omega 0.8, 1e-10):
+    the oracle reaches the tolerance with a contraction that is steady from
+    cycle to cycle, and reproduces its committed solve bit for bit."""
+    sc = F.CONFIG1
+    og, (res, nite, hist) = _solve(sc)
+    assert res <= sc.param["tol"] and nite < sc.param["maxite"]
+    assert og.nlevels == 6 and og.dims(6)[:2] == (8, 8)
+    factors = [(hist[k + 1] / hist[k]) ** 0.5 for k in range(2, nite)]
+    assert max(factors) < 0.35, factors  # about 0.30 per V-cycle
+    _check_golden(sc, og, res, nite, hist)
+
+
+@pytest.mark.slow
+def test_config2_level_count_divergence():
+    """Why configuration 2 is benchmarked with 5 levels and not its stated 10:
+    on the configuration-2 coastline, the reference algorithm's F-cycle
+    (coarse masks by thresholded coverage, src/gmg_setup.jl:322-366)
+    contracts the residual with 5 levels and amplifies it with 6 or more.
+    The oracle re-runs 4 F-cycles at 4096^2 for 5, 6 and 10 levels and
+    reproduces the committed study (tests/golden/make_level_study.py)."""
+    import json
+
+    import make_level_study as S
+    import workloads as W
+
+    study = json.load(open(S.PATH))
+    _, vmsk, noise = W.config2(4096)
+    for nl, lo, hi in ((5, 0.0, 0.3), (6, 1.1, 1.3), (10, 150.0, 300.0)):
+        hist, f = S.factors(4096, nl, 4, vmsk, noise)
+        assert lo < f[-1] < hi, (nl, f)
+        ref = study["by_levels"][str(nl)]["hist"][: len(hist)]
+        np.testing.assert_allclose(hist, ref, rtol=1e-12, atol=0)
+    fac = {int(k): v["factors"][-1] for k, v in study["by_levels"].items()}
+    assert all(fac[k] < 1.0 for k in fac if k <= 5) and all(fac[k] > 1.0 for k in fac if k >= 6), fac
+    assert W.CONFIG2_LEVELS == max(k for k in fac if fac[k] < 1.0)

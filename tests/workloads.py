@@ -19,6 +19,35 @@ import numpy as np
 import fixtures as F
 
 
+def gaussian_smooth(a, sigma: float, truncate: float = 4.0):
+    """scipy.ndimage.gaussian_filter(a, sigma, mode='reflect', truncate) of
+    a 2D array, by FFT convolution along each axis: the same sampled and
+    normalised kernel and the same half-sample symmetric edges, equal to the
+    direct filter to rounding (about 1e-15 relative), at O(n^2 log n)
+    instead of O(n^2 sigma) for the wide kernels of large grids."""
+    from scipy.signal import fftconvolve
+
+    r = int(truncate * float(sigma) + 0.5)
+    t = np.arange(-r, r + 1, dtype=np.float64)
+    k = np.exp(-0.5 * (t / sigma) ** 2)
+    k /= k.sum()
+    out = np.asarray(a, dtype=np.float64)
+    for ax in range(out.ndim):
+        n = out.shape[ax]
+        if r >= n:  # the symmetric padding below must not wrap more than once
+            from scipy.ndimage import gaussian_filter1d
+
+            out = gaussian_filter1d(out, sigma, axis=ax, mode="reflect", truncate=truncate)
+            continue
+        pad = [(0, 0)] * out.ndim
+        pad[ax] = (r, r)
+        ext = np.pad(out, pad, mode="symmetric")
+        shape = [1] * out.ndim
+        shape[ax] = 2 * r + 1
+        out = fftconvolve(ext, k.reshape(shape), mode="valid", axes=ax)
+    return out
+
+
 def coastline_cells(n: int, seed: int, sigma: float, land: float):
     from scipy.ndimage import gaussian_filter
 
@@ -81,29 +110,39 @@ def config4(ninst: int = 2048, seed: int = 3, lo: int = 64, hi: int = 1024, nh: 
     and its cell-centred (Neumann) cycles stall near 0.95 per cycle (CPU
     oracle); an isolated wet pocket also makes a global-mean-free RHS
     inconsistent."""
-    from scipy.ndimage import gaussian_filter, label
+    from concurrent.futures import ThreadPoolExecutor
+    import os
+
+    from scipy.ndimage import label
 
     rng = np.random.default_rng(seed)
-    out = []
+    draws = []  # the random stream, in the order it is drawn
     for _ in range(ninst):
         n = int(32 * round(np.exp(rng.uniform(np.log(lo), np.log(hi))) / 32))
         n = max(32, n)
+        noise = rng.standard_normal((n, n)) if rng.uniform() >= 0.5 else None
+        rhs = np.asfortranarray(rng.standard_normal((n + 2 * nh, n + 2 * nh, 1)))
+        draws.append((n, noise, rhs))
+
+    def build(d):
+        n, noise, rhs = d
         nlev = int(np.floor(np.log2(n / 8))) + 1
         t = n + 2 * nh
-        if rng.uniform() < 0.5:
+        if noise is None:
             msk = F.get_circular_domain((t, t, 1), nh=nh, radius=0.45)
         else:
-            noise = rng.standard_normal((n, n))
-            sm = gaussian_filter(noise, n / 8.0, mode="reflect", truncate=4.0)
+            sm = gaussian_smooth(noise, n / 8.0)
             msk = np.zeros((t, t, 1), dtype=np.uint8, order="F")
             msk[nh:nh + n, nh:nh + n, 0] = sm > np.quantile(sm, 0.30)
             lab, nl = label(msk[:, :, 0] > 0)
             if nl > 1:
                 keep = 1 + int(np.argmax(np.bincount(lab.ravel())[1:]))
                 msk = np.asfortranarray((lab == keep).astype(np.uint8)[:, :, None])
-        rhs = np.asfortranarray(rng.standard_normal((t, t, 1)))
-        out.append((n, nlev, msk, rhs))
-    return out
+        return (n, nlev, msk, rhs)
+
+    # the FFTs and the labelling release the GIL
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        return list(ex.map(build, draws))
 
 
 def config5(ninst: int = 16, n: int = 2048, seed: int = 4, nh: int = 3):
