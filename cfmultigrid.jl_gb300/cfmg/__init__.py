@@ -220,13 +220,19 @@ class Gmg:
         return p.value
 
     def bind_level(self, lev: int, diag=None, idiag=None, Rcoef=None, Pcoef=None, msk=None) -> None:
-        """Bind coefficients computed by the caller's own setup."""
+        """Bind coefficients computed by the caller's own setup. Every array
+        must hold the level's tx*ty*tz values (the C ABI takes bare pointers,
+        so the size is checked here)."""
         keep = []
+        g = self.levels[lev]
 
         def ptr(a, dtype):
             if a is None:
                 return None
             a = np.asfortranarray(np.asarray(a, dtype=dtype))
+            if a.size != g.tx * g.ty * g.tz:
+                raise CfmgError(_lib.ERR_ARG, f"bind_level: {a.size} values for a level of "
+                                              f"{g.tx}x{g.ty}x{g.tz} = {g.tx * g.ty * g.tz} cells")
             keep.append(a)
             return a.ctypes.data_as(ctypes.c_void_p)
 

@@ -68,6 +68,10 @@ struct cfmg_handle {
   bool int_ok = false;
   bool int_on = true;
   bool host_loop = false;  // CFMG_OPT_HOST_LOOP
+  // call order: the operators' coefficients exist once cfmg_setup_operators,
+  // cfmg_bind_level or an upload of a coefficient field ran; cfmg_adjoint
+  // needs a forward cfmg_solve before it
+  bool coef_set = false, solved = false;
   bool record = false;  // emit() records every Op (whole-solve programs) instead of running it
   bool record_tb = false;  // while recording: temporally blocked smoothing is recorded as OPK_TB Ops
 };
@@ -768,6 +772,18 @@ int normresidual_dev(cfmg_handle* h, int kind) {
   return norm_dev(h, 1, h->lv[0].r, h->dscal + S_NORMB, kind);
 }
 
+// The reference builds its coefficients inside get_gmg (src/gmg_setup.jl:
+// 26-35), so none of its operators can run before them; here the handle
+// and its coefficients are separate steps, and running an operator or a
+// solve before the second is a call out of order.
+int need_setup(cfmg_handle* h) {
+  if (!h) return CFMG_ERR_ARG;
+  if (!h->coef_set)
+    return fail(h, CFMG_ERR_STATE,
+                "operators not set up: call cfmg_setup_operators, cfmg_bind_level or upload the coefficients first");
+  return CFMG_OK;
+}
+
 int check_lev(cfmg_handle* h, int lev, int lo_off = 0) {
   if (!h) return CFMG_ERR_ARG;
   if (lev < 1 || lev > L(h) - lo_off)
@@ -1193,7 +1209,9 @@ __global__ void k_loop_test(cudaGraphConditionalHandle hc, double* ds, double* h
   const double res = ds[S_RES];
   const int nite = (int)ds[S_NITE];
   hist[nite] = res;
-  const bool more = res > tol && nite < maxite;
+  // a NaN or Inf in b or in the residual ends the loop (reported as
+  // CFMG_ERR_NONFINITE): an infinite |b| would otherwise give res = 0
+  const bool more = isfinite(ds[S_NORMB]) && isfinite(res) && res > tol && nite < maxite;
   if (more) ds[S_NITE] = (double)(nite + 1);
   cudaGraphSetConditional(hc, more ? 1u : 0u);
 }
@@ -1480,6 +1498,20 @@ static int create_handle(const cfmg_desc* d, cudaStream_t shared, cfmg_handle** 
       if (vc) { l.cE32 = (float*)take(n * 4); l.cN32 = (float*)take(n * 4); }
     }
   }
+  // the fixed-point residual pass reads kResidIntReach elements beside level
+  // 1's x (values it never uses): the arena holds the device scalars in front
+  // of it and level 1's y behind it
+  static_assert(S_COUNT * sizeof(double) <= 256, "the device scalars fill one 256-byte slot");
+  {
+    const char* base = (const char*)h->arena;
+    const char* x0 = (const char*)h->lv[0].x;
+    const char* x1 = (const char*)(h->lv[0].x + h->lv[0].len);
+    if (x0 - base < kResidIntReach * (long)sizeof(double) ||
+        base + total - x1 < kResidIntReach * (long)sizeof(double)) {
+      cfmg_destroy(h);
+      return fail(nullptr, CFMG_ERR_STATE, "arena layout leaves no room beside level 1's x");
+    }
+  }
   if ((!shared && cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess) ||
       cudaHostAlloc((void**)&h->hscal, S_COUNT * sizeof(double), cudaHostAllocDefault) != cudaSuccess) {
     cudaGetLastError();
@@ -1597,6 +1629,8 @@ int cfmg_upload(cfmg_handle* h, int lev, int field, const void* src) {
   if (!p || !src) return fail(h, CFMG_ERR_ARG, "unknown field or null source");
   CUDA_OK(h, cudaMemcpyAsync(p, src, l.len * elt, cudaMemcpyDefault, h->stream));
   TRY(refresh_derived(h, lev, field));
+  if (field >= CFMG_DIAG && field != CFMG_MSK && field != CFMG_KAPPA) h->coef_set = true;
+  h->solved = false;
   return sync(h);
 }
 
@@ -1623,6 +1657,8 @@ int cfmg_bind_level(cfmg_handle* h, int lev, const double* diag, const double* i
   TRY(refresh_derived(h, lev, CFMG_IDIAG));
   if (msk) TRY(refresh_derived(h, lev, CFMG_MSK));
   h->mixed_dirty = true;
+  h->coef_set = true;
+  h->solved = false;
   return sync(h);
 }
 
@@ -1637,11 +1673,15 @@ int cfmg_set_default_msk(cfmg_handle* h) {
 int cfmg_setup_operators(cfmg_handle* h) {
   if (!h) return CFMG_ERR_ARG;
   TRY(setup_operators(h));
-  return sync(h);
+  TRY(sync(h));
+  h->coef_set = true;
+  h->solved = false;
+  return CFMG_OK;
 }
 
 int cfmg_smooth(cfmg_handle* h, int lev, int nite) {
   TRY(check_lev(h, lev));
+  TRY(need_setup(h));
   if (nite < 0) return fail(h, CFMG_ERR_ARG, "nite must be >= 0");
   TRY(smooth_t<double>(h, lev, nite));
   return flush(h);
@@ -1649,12 +1689,14 @@ int cfmg_smooth(cfmg_handle* h, int lev, int nite) {
 
 int cfmg_residual(cfmg_handle* h, int lev) {
   TRY(check_lev(h, lev));
+  TRY(need_setup(h));
   TRY(residual_t<double>(h, lev));
   return flush(h);
 }
 
 int cfmg_restrict(cfmg_handle* h, int lev, int field) {
   TRY(check_lev(h, lev, 1));
+  TRY(need_setup(h));
   if (field != CFMG_X && field != CFMG_R && field != CFMG_B && field != CFMG_Y)
     return fail(h, CFMG_ERR_ARG, "restriction field must be x, r, b or y");
   TRY(restrict_t<double>(h, lev, field));
@@ -1663,6 +1705,7 @@ int cfmg_restrict(cfmg_handle* h, int lev, int field) {
 
 int cfmg_prolong(cfmg_handle* h, int lev) {
   TRY(check_lev(h, lev, 1));
+  TRY(need_setup(h));
   TRY(prolong_t<double>(h, lev));
   return flush(h);
 }
@@ -1708,6 +1751,7 @@ int cfmg_norm(cfmg_handle* h, int lev, int field, double* out) {
 
 int cfmg_normresidual(cfmg_handle* h, double normb, double* out) {
   if (!h || !out) return CFMG_ERR_ARG;
+  TRY(need_setup(h));
   if (!(normb > 0.0)) {
     *out = 0.0;
     return CFMG_OK;
@@ -1721,11 +1765,22 @@ int cfmg_normresidual(cfmg_handle* h, double normb, double* out) {
 
 int cfmg_cycle(cfmg_handle* h, int kind) {
   if (!h) return CFMG_ERR_ARG;
+  TRY(need_setup(h));
   return cycle_t<double>(h, kind);
+}
+
+// A NaN or Inf in b, or a residual that is not finite, ends the solve and
+// makes it return CFMG_ERR_NONFINITE, with res and nite filled in.
+int nonfinite_check(cfmg_handle* h, double normb, double res) {
+  if (std::isfinite(normb) && std::isfinite(res)) return CFMG_OK;
+  return fail(h, CFMG_ERR_NONFINITE,
+              std::string("non-finite ") + (std::isfinite(normb) ? "residual norm" : "norm of b") +
+                  " (NaN or Inf in b, x or the coefficients)");
 }
 
 int cfmg_solve(cfmg_handle* h, double* res_out, int* nite_out, double* history) {
   if (!h || !res_out || !nite_out) return CFMG_ERR_ARG;
+  TRY(need_setup(h));
   const cfmg_desc& d = h->d;
   int prec = d.precision;
   if (prec == CFMG_MIXED && L(h) == 1) prec = CFMG_FP64;  // no coarse level to correct with
@@ -1769,15 +1824,17 @@ int cfmg_solve(cfmg_handle* h, double* res_out, int* nite_out, double* history) 
       CUDA_OK(h, cudaMemcpy(history, h->dhist, sizeof(double) * (size_t)(nite + 1), cudaMemcpyDeviceToHost));
     *res_out = h->hscal[S_RES];
     *nite_out = nite;
-    return CFMG_OK;
+    h->solved = true;
+    return nonfinite_check(h, h->hscal[S_NORMB], h->hscal[S_RES]);
   }
-  CUDA_OK(h, cudaMemcpyAsync(h->hscal, h->dscal, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_OK(h, cudaMemcpyAsync(h->hscal, h->dscal, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   TRY(sync(h));
   double res = h->hscal[S_RES];
+  const double normb = h->hscal[S_NORMB];
   if (history) history[0] = res;
   int nite = 0;
   cudaGraphExec_t ge = nullptr;
-  while ((res > d.tol) && (nite < d.maxite)) {  // src/gmg_solver.jl:29-39
+  while (std::isfinite(normb) && std::isfinite(res) && (res > d.tol) && (nite < d.maxite)) {  // src/gmg_solver.jl:29-39
     nite += 1;
     if (h->prof_cls >= 0) {
       TRY(iteration(h, prec, d.cycle, d.norm_kind));  // eager, so launches can be bracketed
@@ -1792,11 +1849,14 @@ int cfmg_solve(cfmg_handle* h, double* res_out, int* nite_out, double* history) 
   }
   *res_out = res;
   *nite_out = nite;
-  return CFMG_OK;
+  h->solved = true;
+  return nonfinite_check(h, normb, res);
 }
 
 int cfmg_adjoint(cfmg_handle* h, const double* g, double* grad_b, double* grad_kappa, double* res, int* nite) {
   if (!h || !g || !grad_b || !res || !nite) return CFMG_ERR_ARG;
+  TRY(need_setup(h));
+  if (!h->solved) return fail(h, CFMG_ERR_STATE, "cfmg_adjoint needs a forward cfmg_solve on this handle first");
   if (grad_kappa && h->d.op != CFMG_VARCOEF)
     return fail(h, CFMG_ERR_ARG, "grad_kappa needs the variable-coefficient operator");
   TRY(sync(h));
@@ -2338,6 +2398,10 @@ int cfmg_batch_set_option(cfmg_batch* b, int option, long long value) {
 
 int cfmg_batch_solve(cfmg_batch* b, int zero_x, double* res, int* nite, double* t_done_ms) {
   if (!b) return CFMG_ERR_ARG;
+  for (size_t i = 0; i < b->inst.size(); ++i)
+    if (!b->inst[i]->coef_set)
+      return bfail(b, CFMG_ERR_STATE, "instance " + std::to_string(i) + ": operators not set up (run "
+                                      "cfmg_setup_operators or cfmg_bind_level on it first)");
   for (cfmg_handle* h : b->inst)
     if (h->mixed_dirty) b->built = false;  // coefficients changed since the programs were made
   if (!b->built) {
@@ -2377,12 +2441,18 @@ int cfmg_batch_solve(cfmg_batch* b, int zero_x, double* res, int* nite, double* 
   const int kres = b->lockstep ? (int)BS_RES : (int)SS_RES, knite = b->lockstep ? (int)BS_NITE : (int)SS_NITE;
   double t0 = 1e300;
   for (int i = 0; i < ninst; ++i) t0 = std::min(t0, b->hsc[(size_t)i * b->nsc + kt0]);
+  int bad = -1;
   for (int i = 0; i < ninst; ++i) {
     const double* c = &b->hsc[(size_t)i * b->nsc];
     if (res) res[i] = c[kres];
     if (nite) nite[i] = (int)c[knite];
     if (t_done_ms) t_done_ms[i] = (c[kt1] - t0) * 1e-6;
+    if (bad < 0 && !std::isfinite(c[kres])) bad = i;
   }
+  for (cfmg_handle* h : b->inst) h->solved = true;
+  if (bad >= 0)
+    return bfail(b, CFMG_ERR_NONFINITE, "instance " + std::to_string(bad) +
+                                            ": non-finite residual norm (NaN or Inf in b, x or the coefficients)");
   return CFMG_OK;
 }
 

@@ -297,7 +297,13 @@ void launch_update_scaled(double* x, const float* e, const double* iscale, long 
 void launch_resid_int(int kind, const double* x, const double* b, const int8_t* dq, const Geom& g, const Box& bx,
                       long long lo, long long n, const double* ds, float* b32, float* r32, bool neumann,
                       double* partials, cudaStream_t s);
-// 2D single-layer form (each x converted once); false: use launch_resid_int
+// 2D single-layer form (each x converted once); false: use launch_resid_int.
+// Its warps read x up to kResidIntReach elements before x[0] and after
+// x[len-1] (lanes 0 and 31 beside a strip, the last strip past the row end)
+// and never use those values: x must lie inside an allocation with at least
+// that many elements on either side, as level 1's x does in a handle's arena
+// (checked by cfmg_create).
+constexpr int kResidIntReach = 32;
 bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t* dq, const Geom& g, const Box& bx,
                         const double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s);
 void launch_rhs32_shift(const uint8_t* m, const double* mean_scale, float* b32, float* r32, long long n,

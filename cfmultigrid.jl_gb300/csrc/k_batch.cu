@@ -396,6 +396,9 @@ __global__ void __launch_bounds__(kBThreads) k_bfinal(const BInst* __restrict__ 
     } else {
       res = normb > 0.0 ? sqrt(sum / normb) : 0.0;
     }
+    // a NaN or Inf |b| stops the instance with a NaN residual (reported as
+    // non-finite), where the ratio alone would read as converged
+    if (!isfinite(normb)) res = __longlong_as_double(0x7ff8000000000000LL);
     const int nite = (int)sc[BS_NITE];
     sc[BS_RES] = res;
     sc[BS_HIST + nite] = res;

@@ -100,7 +100,9 @@ __device__ void run_program(const Op* __restrict__ prog, int nops, long long t0,
         if (cluster_rank() == 0 && threadIdx.x == 0) {
           const double nb = sc[op.s2];
           const double q = nb > 0.0 ? sc[op.s1] / nb : 0.0;
-          sc[op.s0] = op.norm_kind == CFMG_NORM_L2 ? sqrt(q) : q;
+          // a NaN or Inf |b| gives a NaN ratio (reported as non-finite), not 0
+          sc[op.s0] = !isfinite(nb) ? __longlong_as_double(0x7ff8000000000000LL)
+                                    : (op.norm_kind == CFMG_NORM_L2 ? sqrt(q) : q);
         }
         break;
       case OPK_SCALE:

@@ -272,6 +272,7 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int(const double* __restri
 // space read up to 31 elements before its start and after its end, into the
 // device scalars before it and into y after it; those values are not used.
 constexpr int kIntCols = 30;  // output columns per warp strip
+static_assert(kIntCols + 1 < kResidIntReach, "a warp reaches kIntCols + 1 columns beyond its strip's first");
 constexpr int kIntUnroll = 6;  // rows per loop body; rows per task is a multiple
 
 struct StripSpace {
