@@ -8,7 +8,11 @@ at the first iteration count. The choice is cached in a JSON file keyed by
 the problem signature, so later runs skip the trials.
 
 A candidate is (cycle, npre, npost, omega). Every candidate must reach the
-tolerance on every sample instance, or it is discarded.
+tolerance on every sample instance, or it is discarded; when none does, the
+caller's own schedule is kept and the report says so.
+
+The cache lives outside the package: $CFMG_TUNE_CACHE if set, else
+$XDG_CACHE_HOME/cfmg/tuned.json (default ~/.cache/cfmg/tuned.json).
 """
 from __future__ import annotations
 
@@ -28,7 +32,11 @@ CANDIDATES = [
     ("f", 1, 1, 0.9),
 ]
 
-_CACHE = os.environ.get("CFMG_TUNE_CACHE", os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuned.json"))
+def _cache_path() -> str:
+    if os.environ.get("CFMG_TUNE_CACHE"):
+        return os.environ["CFMG_TUNE_CACHE"]
+    base = os.environ.get("XDG_CACHE_HOME") or os.path.join(os.path.expanduser("~"), ".cache")
+    return os.path.join(base, "cfmg", "tuned.json")
 
 
 def _signature(param, sizes) -> str:
@@ -39,7 +47,7 @@ def _signature(param, sizes) -> str:
 
 def _load():
     try:
-        with open(_CACHE) as f:
+        with open(_cache_path()) as f:
             return json.load(f)
     except (OSError, ValueError):
         return {}
@@ -47,7 +55,8 @@ def _load():
 
 def _store(d):
     try:
-        with open(_CACHE, "w") as f:
+        os.makedirs(os.path.dirname(_cache_path()), exist_ok=True)
+        with open(_cache_path(), "w") as f:
             json.dump(d, f, indent=1, sort_keys=True)
     except OSError:
         pass
@@ -77,7 +86,10 @@ def tune(param, sizes: Sequence[int], make_sample: Callable[[object, Sequence[in
         trials.append({"cycle": cyc, "npre": npre, "npost": npost, "omega": omega, "seconds": dt, "ok": ok,
                        "max_cycles": int(nite.max())})
         batch.close()
-    good = [t for t in trials if t["ok"]] or trials
+    good = [t for t in trials if t["ok"]]
+    if not good:  # no candidate converged on the sample: keep the caller's schedule, do not cache
+        return param, {"cached": False, "best": None, "trials": trials,
+                       "note": "no candidate reached the tolerance on every sample instance"}
     best = min(good, key=lambda t: t["seconds"])
     if use_cache:
         cache[sig] = best
