@@ -352,13 +352,24 @@ def cycle(mg: Gmg, kind: Optional[str] = None) -> None:
     mg._check(mg._L.cfmg_cycle(mg._h, CYCLES[kind or mg.param.cycle]))
 
 
-def solve(mg: Gmg, history: bool = False):
+def solve(mg: Gmg, history: bool = False, tol: Optional[float] = None, maxite: Optional[int] = None,
+          residual_norm: Optional[str] = None):
     """solve!(mg) (src/gmg_solver.jl:9-42): returns (res, nite), plus the
-    per-cycle residual history when ``history`` is true."""
+    per-cycle residual history when ``history`` is true. ``tol``, ``maxite``
+    and ``residual_norm`` override the Param's for this and later solves
+    (cfmg_solve_tol)."""
     res = ctypes.c_double()
     nite = ctypes.c_int()
-    hist = (ctypes.c_double * (mg.param.maxite + 1))()
-    mg._check(mg._L.cfmg_solve(mg._h, ctypes.byref(res), ctypes.byref(nite), hist))
+    if tol is not None or maxite is not None or residual_norm is not None:
+        mg.param = dataclasses.replace(mg.param, tol=mg.param.tol if tol is None else float(tol),
+                                       maxite=mg.param.maxite if maxite is None else int(maxite),
+                                       residual_norm=residual_norm or mg.param.residual_norm)
+        hist = (ctypes.c_double * (mg.param.maxite + 1))()
+        mg._check(mg._L.cfmg_solve_tol(mg._h, mg.param.tol, mg.param.maxite, NORMS[mg.param.residual_norm],
+                                       ctypes.byref(res), ctypes.byref(nite), hist))
+    else:
+        hist = (ctypes.c_double * (mg.param.maxite + 1))()
+        mg._check(mg._L.cfmg_solve(mg._h, ctypes.byref(res), ctypes.byref(nite), hist))
     if mg.param.verbose:
         print(" ----------------\n  ite     res    \n ----------------")
         for k in range(nite.value + 1):

@@ -33,7 +33,7 @@ EXPORTS = (
     "cfmg_set_default_msk", "cfmg_setup_operators", "cfmg_smooth", "cfmg_residual", "cfmg_restrict",
     "cfmg_prolong", "cfmg_zero", "cfmg_fill", "cfmg_norm", "cfmg_normresidual", "cfmg_cycle", "cfmg_solve",
     "cfmg_launch_count", "cfmg_profile", "cfmg_profile_read", "cfmg_set_option", "cfmg_norm_noalloc",
-    "cfmg_adjoint", "cfmg_batch_create", "cfmg_batch_destroy", "cfmg_batch_instance", "cfmg_batch_solve",
+    "cfmg_adjoint", "cfmg_solve_tol", "cfmg_adjoint_solve", "cfmg_batch_create", "cfmg_batch_destroy", "cfmg_batch_instance", "cfmg_batch_solve",
     "cfmg_batch_last_error", "cfmg_batch_set_option",
 )
 OPTIONS = {"engine_cells": 0, "temporal_blocking": 1, "coarsest_fp64": 2, "int_residual": 3, "host_loop": 4,
@@ -101,6 +101,8 @@ def load() -> ctypes.CDLL:
         "cfmg_set_option": [vp, i, ctypes.c_longlong],
         "cfmg_norm_noalloc": [vp, vp, ctypes.c_longlong, vp, vp],
         "cfmg_adjoint": [vp, vp, vp, vp, pd, pi],
+        "cfmg_solve_tol": [vp, d, i, i, pd, pi, pd],
+        "cfmg_adjoint_solve": [vp, vp, vp, vp],
         "cfmg_batch_create": [ctypes.POINTER(Desc), i, vp, vp, vp, ctypes.POINTER(vp)],
         "cfmg_batch_destroy": [vp],
         "cfmg_batch_instance": [vp, i, ctypes.POINTER(vp)],

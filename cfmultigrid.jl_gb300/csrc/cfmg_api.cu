@@ -1853,6 +1853,34 @@ int cfmg_solve(cfmg_handle* h, double* res_out, int* nite_out, double* history) 
   return nonfinite_check(h, normb, res);
 }
 
+int cfmg_solve_tol(cfmg_handle* h, double tol, int maxite, int norm_kind, double* res_out, int* nite_out,
+                   double* history) {
+  if (!h || !res_out || !nite_out) return CFMG_ERR_ARG;
+  if (maxite < 0) return fail(h, CFMG_ERR_ARG, "maxite must be >= 0");
+  if (norm_kind != CFMG_NORM_REF_SQUARED && norm_kind != CFMG_NORM_L2) return fail(h, CFMG_ERR_ARG, "unknown norm kind");
+  if (!(tol >= 0.0)) return fail(h, CFMG_ERR_ARG, "tol must be >= 0");
+  if (tol != h->d.tol || maxite != h->d.maxite || norm_kind != h->d.norm_kind) {
+    // the captured graphs hold the stopping rule, the norm kind and the
+    // history's length: rebuild them for the new values
+    TRY(sync(h));
+    drop_graphs(h);
+    if (maxite > h->d.maxite && h->dhist) {
+      cudaFree(h->dhist);
+      h->dhist = nullptr;
+    }
+    h->d.tol = tol;
+    h->d.maxite = maxite;
+    h->d.norm_kind = norm_kind;
+  }
+  return cfmg_solve(h, res_out, nite_out, history);
+}
+
+int cfmg_adjoint_solve(cfmg_handle* h, const double* cot, double* grad_b, double* grad_kappa) {
+  double res = 0.0;
+  int nite = 0;
+  return cfmg_adjoint(h, cot, grad_b, grad_kappa, &res, &nite);
+}
+
 int cfmg_adjoint(cfmg_handle* h, const double* g, double* grad_b, double* grad_kappa, double* res, int* nite) {
   if (!h || !g || !grad_b || !res || !nite) return CFMG_ERR_ARG;
   TRY(need_setup(h));

@@ -197,6 +197,15 @@ CFMG_API int cfmg_cycle(cfmg_handle* h, int kind);
  * The loop, its stopping test and the history run on the device in one
  * graph launch (CFMG_OPT_HOST_LOOP = 1: one launch per iteration). */
 CFMG_API int cfmg_solve(cfmg_handle* h, double* res, int* nite, double* history);
+/* solve! with the stopping rule given per call, as a caller that keeps
+ * Param.tol / Param.maxite on its side binds it: tol, maxite and norm_kind
+ * replace the descriptor's (the captured graphs are rebuilt when they
+ * change), then as cfmg_solve. Returns (res, nite) like solve!
+ * (src/gmg_solver.jl:9-42); exhausting maxite is not an error. Errors:
+ * CFMG_ERR_STATE before setup, CFMG_ERR_NONFINITE when b or the residual
+ * norm is NaN/Inf (res and nite are still written). */
+CFMG_API int cfmg_solve_tol(cfmg_handle* h, double tol, int maxite, int norm_kind, double* res, int* nite,
+                            double* history);
 
 /* Adjoint solve: the backward pass of solve! (no counterpart in the
  * reference; a Julia host exposes it as the pullback of a ChainRulesCore
@@ -211,6 +220,9 @@ CFMG_API int cfmg_solve(cfmg_handle* h, double* res, int* nite, double* history)
  * allocates three level-1 FP64 scratch arrays. */
 CFMG_API int cfmg_adjoint(cfmg_handle* h, const double* g, double* grad_b, double* grad_kappa, double* res,
                           int* nite);
+/* The same backward pass without the adjoint solve's (res, nite): the
+ * pullback's signature, cot = dL/dx in, dL/db and dL/dkappa out. */
+CFMG_API int cfmg_adjoint_solve(cfmg_handle* h, const double* cot, double* grad_b, double* grad_kappa);
 
 /* Batched solves (no counterpart in the reference, which solves one
  * problem at a time). ninst independent 2D closed-topology problems share

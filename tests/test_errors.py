@@ -234,3 +234,40 @@ def test_batch_errors():
                             None)
     assert rc == _lib.ERR_NONFINITE and b"instance 1" in L.cfmg_batch_last_error(batch._b)
     assert res[0] <= 1e-10 and res[2] <= 1e-10 and not np.isfinite(res[1]) and nite[1] == 0
+
+
+@gpu
+def test_solve_tol_sets_the_rule_per_call():
+    """cfmg_solve_tol(h, tol, maxite, norm_kind, ...): the stopping rule per
+    call (the graphs are rebuilt when it changes, the history buffer grows
+    with maxite); each solve matches the oracle's solve! with that rule."""
+    import oracle as O
+
+    mg = cfmg.get_gmg(_small(tol=1e-20, maxite=30))
+    b = _rhs(mg)
+    mg.data[1].b = b
+    base = dict(nx=64, ny=64, nz=1, case="twod", cycle="v", npre=2, npost=2, omega=0.8)
+    for tol, maxite, kind in ((1e-20, 30, "ref_squared"), (1e-8, 30, "ref_squared"), (1e-24, 60, "ref_squared"),
+                              (1e-6, 4, "ref_squared"), (1e-10, 30, "l2")):
+        cfmg.set_to_zero(mg, 1, "x")
+        res, nite, hist = cfmg.solve(mg, history=True, tol=tol, maxite=maxite, residual_norm=kind)
+        og = O.OracleGmg(dict(base, tol=tol * tol if kind == "l2" else tol, maxite=maxite))
+        og.field(1, "b")[...] = b
+        r0, n0, h0 = og.solve()
+        assert nite == n0 and len(hist) == n0 + 1, (tol, maxite, kind, nite, n0)
+        np.testing.assert_allclose(hist ** 2 if kind == "l2" else hist, h0, rtol=1e-11)
+        assert np.array_equal(mg.data[1].x, og.x)
+
+
+@gpu
+def test_adjoint_solve_matches_adjoint():
+    mg = cfmg.get_gmg(_small(tol=1e-20, maxite=30))
+    mg.data[1].b = _rhs(mg)
+    cfmg.solve(mg)
+    g = np.asfortranarray(_rhs(mg, 3))
+    gb, _ = cfmg.adjoint(mg, g)
+    gb2 = np.empty_like(gb)
+    L = mg._L
+    assert L.cfmg_adjoint_solve(mg.handle, g.ctypes.data_as(ctypes.c_void_p), gb2.ctypes.data_as(ctypes.c_void_p),
+                                None) == 0
+    assert np.array_equal(gb, gb2)
