@@ -72,6 +72,7 @@ struct cfmg_handle {
   // cfmg_bind_level or an upload of a coefficient field ran; cfmg_adjoint
   // needs a forward cfmg_solve before it
   bool coef_set = false, solved = false;
+  bool dep_launch = true;  // CFMG_OPT_DEPENDENT_LAUNCH
   bool record = false;  // emit() records every Op (whole-solve programs) instead of running it
   bool record_tb = false;  // while recording: temporally blocked smoothing is recorded as OPK_TB Ops
 };
@@ -133,6 +134,8 @@ std::mutex g_err_mu;
 std::string g_create_err;
 
 }  // namespace
+
+thread_local bool cfmg::tl_dep_launch = true;
 
 void cfmg::set_global_error(const std::string& msg) {
   std::lock_guard<std::mutex> lk(g_err_mu);
@@ -205,6 +208,7 @@ struct Launch {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   Launch(cfmg_handle* hh, int cls, int lev, int prec, int nkernels = 1) : h(hh) {
     h->launches += nkernels;
+    tl_dep_launch = h->dep_launch;
     if (h->prof_cls == cls && h->prof_lev == lev && h->prof_prec == prec && !h->capturing) {
       for (cudaEvent_t* e : {&e0, &e1}) {
         if (h->ev_pool.empty()) {
@@ -922,6 +926,7 @@ int prepare_mixed(cfmg_handle* h) {
 // correction equation on level 1, with the wet mean removed for the
 // cell-centred (Neumann) operator.
 __global__ void k_mean_partial(const double* r, const uint8_t* m, long long n, double* partials) {
+  dep_wait();
   // Neumaier-compensated per-thread sums, fixed-order tree across the block
   double s = 0.0, c = 0.0;
   for (long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x; I < n; I += (long long)gridDim.x * blockDim.x) {
@@ -943,6 +948,7 @@ __global__ void k_mean_partial(const double* r, const uint8_t* m, long long n, d
 }
 
 __global__ void k_scale_from_norm(double* dscal, const double* partials, int nparts, bool remove_mean) {
+  dep_wait();
   // dscal[S_NORM] = sum msk r^2 (raw or 1 if 0), dscal[S_NWET] = number of wet cells
   __shared__ double sh[kNormParts];
   double v = 0.0;
@@ -964,6 +970,7 @@ __global__ void k_scale_from_norm(double* dscal, const double* partials, int npa
 }
 
 __global__ void k_rhs32(const double* r, const uint8_t* m, const double* dscal, float* b32, float* r32, long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= n) return;
   double v = m[I] ? (r[I] - dscal[S_MEAN]) * dscal[S_SCALE] : 0.0;
@@ -974,6 +981,7 @@ __global__ void k_rhs32(const double* r, const uint8_t* m, const double* dscal, 
 
 // x += e / scale (the FP64 solution update)
 __global__ void k_update(double* x, const float* e, const double* dscal, long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= n) return;
   x[I] = __fma_rn((double)e[I], dscal[S_ISCALE], x[I]);
@@ -983,6 +991,7 @@ __global__ void k_update(double* x, const float* e, const double* dscal, long lo
 // wet-mean removal: x -= (sum msk x)/(sum msk) on wet cells, the sum in
 // Neumaier-compensated FP64 (k_mean_partial above) with a fixed-order final
 __global__ void k_mean_final(const double* partials, int nparts, double* dscal) {
+  dep_wait();
   __shared__ double sh[kNormParts];
   sh[threadIdx.x] = (int)threadIdx.x < nparts ? partials[threadIdx.x] : 0.0;
   __syncthreads();
@@ -993,6 +1002,7 @@ __global__ void k_mean_final(const double* partials, int nparts, double* dscal) 
   if (threadIdx.x == 0) dscal[S_MEAN] = dscal[S_NWET] > 0 ? sh[0] / dscal[S_NWET] : 0.0;
 }
 __global__ void k_sub_mean(double* x, const uint8_t* m, const double* dscal, long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= n) return;
   x[I] = m[I] ? x[I] - dscal[S_MEAN] : 0.0;
@@ -1003,6 +1013,7 @@ __global__ void k_sub_mean(double* x, const uint8_t* m, const double* dscal, lon
 // enters A as c_f (x_nb - x_k) in both rows, so dL/dc_f = (lam_i-lam_j)(x_i-x_j).
 __global__ void k_kappa_grad(const double* lam, const double* x, const uint8_t* m, double* gk, long long n1,
                              long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= n) return;
   double s = 0.0;
@@ -1031,9 +1042,9 @@ int count_wet(cfmg_handle* h) {
 int remove_wet_mean(cfmg_handle* h, double* x) {
   const Level& l1 = h->lv[0];
   const long long n = (long long)l1.len;
-  k_mean_partial<<<kNormParts, 256, 0, h->stream>>>(x, l1.msk, n, h->partials);
-  k_mean_final<<<1, kNormParts, 0, h->stream>>>(h->partials, kNormParts, h->dscal);
-  k_sub_mean<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(x, l1.msk, h->dscal, n);
+  launch_dep(k_mean_partial, kNormParts, 256, 0, h->stream, x, l1.msk, n, h->partials);
+  launch_dep(k_mean_final, 1, kNormParts, 0, h->stream, h->partials, kNormParts, h->dscal);
+  launch_dep(k_sub_mean, (unsigned)((n + 255) / 256), 256, 0, h->stream, x, l1.msk, h->dscal, n);
   h->launches += 3;
   LAUNCH_OK(h);
   return CFMG_OK;
@@ -1097,6 +1108,7 @@ int fused_residual(cfmg_handle* h) {
 }
 
 __global__ void init_scale(double* ds) {
+  dep_wait();
   const double nw = ds[S_NWET] > 0 ? ds[S_NWET] : 1.0;
   const double rms = sqrt(ds[S_NORMB] / nw);
   int e = 0;
@@ -1134,16 +1146,16 @@ int mixed_iteration(cfmg_handle* h, int kind) {
   TRY(flush(h));
   {
     Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED, remove_mean ? 3 : 2);
-    if (remove_mean) k_mean_partial<<<kNormParts, 256, 0, h->stream>>>(l1.r, l1.msk, n, h->partials);
-    k_scale_from_norm<<<1, kNormParts, 0, h->stream>>>(h->dscal, h->partials, kNormParts, remove_mean);
-    k_rhs32<<<nb, 256, 0, h->stream>>>(l1.r, l1.msk, h->dscal, l1.b32, l1.r32, n);
+    if (remove_mean) launch_dep(k_mean_partial, kNormParts, 256, 0, h->stream, l1.r, l1.msk, n, h->partials);
+    launch_dep(k_scale_from_norm, 1, kNormParts, 0, h->stream, h->dscal, h->partials, kNormParts, remove_mean);
+    launch_dep(k_rhs32, nb, 256, 0, h->stream, l1.r, l1.msk, h->dscal, l1.b32, l1.r32, n);
   }
   if (!lazy) TRY(zero_t<float>(h, 1, CFMG_X));
   LAUNCH_OK(h);
   TRY(cycle_t<float>(h, kind, lazy));
   {
     Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED);
-    k_update<<<nb, 256, 0, h->stream>>>(l1.x, view<float>(l1).x, h->dscal, n);
+    launch_dep(k_update, nb, 256, 0, h->stream, l1.x, view<float>(l1).x, h->dscal, n);
   }
   LAUNCH_OK(h);
   return CFMG_OK;
@@ -1796,7 +1808,7 @@ int cfmg_solve(cfmg_handle* h, double* res_out, int* nite_out, double* history) 
   }
   LAUNCH_OK(h);
   if (prec == CFMG_MIXED && fused_ok(h)) {
-    init_scale<<<1, 1, 0, h->stream>>>(h->dscal);  // the first right-hand side is scaled from |b|
+    launch_dep(init_scale, 1, 1, 0, h->stream, h->dscal);  // the first right-hand side is scaled from |b|
     if (int_path(h)) {
       // fixed-point range of the first pass: max |x|, max |b|; and max |x|
       // outside the update box U, which no update changes: each iteration's
@@ -1915,7 +1927,7 @@ int cfmg_adjoint(cfmg_handle* h, const double* g, double* grad_b, double* grad_k
   CUDA_OK(h, cudaMemcpyAsync(grad_b, l1.x, bytes, cudaMemcpyDefault, s));
   if (grad_kappa) {
     const long long n = (long long)l1.len;
-    k_kappa_grad<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(l1.x, h->adj_x, l1.msk, h->adj_gk, l1.tx, n);
+    launch_dep(k_kappa_grad, (unsigned)((n + 255) / 256), 256, 0, s, l1.x, h->adj_x, l1.msk, h->adj_gk, l1.tx, n);
     h->launches += 1;
     LAUNCH_OK(h);
     CUDA_OK(h, cudaMemcpyAsync(grad_kappa, h->adj_gk, bytes, cudaMemcpyDefault, s));
@@ -1942,6 +1954,7 @@ int bfail(cfmg_batch* b, int code, const std::string& msg) {
   } while (0)
 
 __global__ void k_batch_init(double* sc, const double* nwet, int ninst, int nsc, double zero_x) {
+  dep_wait();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ninst * nsc) return;
   const int k = i % nsc;
@@ -1995,7 +2008,7 @@ int batch_build(cfmg_batch* b) {
   for (int z = 0; z < 2; ++z) {
     cudaGraph_t g = nullptr;
     BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
-    k_batch_init<<<(tot + 255) / 256, 256, 0, b->stream>>>(b->sc, b->nwet, ninst, b->nsc, (double)z);
+    launch_dep(k_batch_init, (tot + 255) / 256, 256, 0, b->stream, b->sc, b->nwet, ninst, b->nsc, (double)z);
     cudaMemsetAsync(b->counter, 0, sizeof(int) * (size_t)(1 + b->nclusters), b->stream);
     launch_batch(b->ptrs, b->nops, ninst, b->counter, b->red, b->nclusters, b->stream);
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
@@ -2524,6 +2537,11 @@ int cfmg_set_option(cfmg_handle* h, int option, long long value) {
   if (option == CFMG_OPT_FUSED_UPDATE) {
     h->upd_on = value != 0;
     drop_graphs(h);
+    return CFMG_OK;
+  }
+  if (option == CFMG_OPT_DEPENDENT_LAUNCH) {
+    h->dep_launch = value != 0;
+    drop_graphs(h);  // captured graphs embed the launch attributes
     return CFMG_OK;
   }
   if (option == CFMG_OPT_ENGINE_CELLS) {

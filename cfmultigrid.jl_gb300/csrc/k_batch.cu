@@ -90,6 +90,7 @@ __device__ __forceinline__ double bmax(double v, double* sh) {
 // engine, 4 (FP32) or 2 (FP64) items per thread in flight.
 __global__ void __launch_bounds__(kBThreads, 2) k_bstage(const Op* __restrict__ ops, const int4* __restrict__ tab,
                                                          long long nchunks, int win, const int* __restrict__ active) {
+  dep_wait();
   __shared__ Op op;
   __shared__ int list[kBThreads];
   __shared__ int wsum[kBThreads / 32 + 1];
@@ -120,6 +121,7 @@ static_assert(sizeof(Op) / sizeof(int) <= kBThreads, "one thread per word of an 
 // One block per instance.
 __global__ void __launch_bounds__(kBThreads) k_binit(const BInst* __restrict__ bi, int zero_x, int* active,
                                                      int* nactive) {
+  dep_wait();
   __shared__ double sh[kBThreads / 32];
   const BInst& B = bi[blockIdx.x];
   double* sc = B.sc;
@@ -162,6 +164,7 @@ template <int KIND, bool NEUMANN>
 __global__ void __launch_bounds__(kBThreads) k_bres(const BInst* __restrict__ bi, const int4* __restrict__ tab,
                                                     long long nchunks, int win, const int* __restrict__ active,
                                                     double* __restrict__ partials) {
+  dep_wait();
   constexpr int U = kBChunk / kBThreads;
   __shared__ int list[kBThreads];
   __shared__ int wsum[kBThreads / 32 + 1];
@@ -246,6 +249,7 @@ template <int KIND, bool NEUMANN>
 __global__ void __launch_bounds__(kBThreads) k_bres_int(const BInst* __restrict__ bi, const int4* __restrict__ ttab,
                                                         long long ntasks, const int* __restrict__ active,
                                                         double* __restrict__ partials) {
+  dep_wait();
   constexpr int q = (KIND == OPK_RESID9) ? 2 : 0;
   const int lane = threadIdx.x & 31;
   const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -332,6 +336,7 @@ __global__ void __launch_bounds__(kBThreads) k_bres_int(const BInst* __restrict_
 // cell-centred, integer form: b32 = r32 = msk ? b32 - mean * CUR : 0
 __global__ void __launch_bounds__(kBThreads) k_brhs_shift(const BInst* __restrict__ bi, const int4* __restrict__ tab,
                                                           long long nchunks, int win, const int* __restrict__ active) {
+  dep_wait();
   constexpr int U = kBChunk / kBThreads;
   __shared__ int list[kBThreads];
   __shared__ int wsum[kBThreads / 32 + 1];
@@ -374,6 +379,7 @@ __global__ void __launch_bounds__(kBThreads) k_bfinal(const BInst* __restrict__ 
                                                       const long long* __restrict__ cstart,
                                                       const double* __restrict__ partials, int* active,
                                                       int* nactive) {
+  dep_wait();
   __shared__ double sh[kBThreads / 32];
   const int i = blockIdx.x;
   if (!active[i]) return;
@@ -426,6 +432,7 @@ __global__ void __launch_bounds__(kBThreads) k_bfinal(const BInst* __restrict__ 
 // cell-centred: b32 = r32 = msk ? (r - mean) * CUR : 0 over the whole array
 __global__ void __launch_bounds__(kBThreads) k_brhs(const BInst* __restrict__ bi, const int4* __restrict__ tab,
                                                     long long nchunks, int win, const int* __restrict__ active) {
+  dep_wait();
   constexpr int U = kBChunk / kBThreads;
   __shared__ int list[kBThreads];
   __shared__ int wsum[kBThreads / 32 + 1];
@@ -459,6 +466,7 @@ __global__ void __launch_bounds__(kBThreads) k_brhs(const BInst* __restrict__ bi
 // x += e32 * ICUR over the whole array
 __global__ void __launch_bounds__(kBThreads) k_bupdate(const BInst* __restrict__ bi, const int4* __restrict__ tab,
                                                        long long nchunks, int win, const int* __restrict__ active) {
+  dep_wait();
   constexpr int U = kBChunk / kBThreads;
   __shared__ int list[kBThreads];
   __shared__ int wsum[kBThreads / 32 + 1];
@@ -538,6 +546,7 @@ __device__ void bsmall_run(const BSmall& s, T* X, T* Y, T* B, T* W) {
 }
 
 __global__ void __launch_bounds__(kBThreads) k_bsmall(const BSmall* __restrict__ sm, const int* __restrict__ active) {
+  dep_wait();
   extern __shared__ double dsm[];
   const BSmall& s = sm[blockIdx.x];
   if (!active[s.inst]) return;
@@ -551,6 +560,7 @@ __global__ void __launch_bounds__(kBThreads) k_bsmall(const BSmall* __restrict__
 
 // the `while` condition: another iteration while any instance continues
 __global__ void k_bcond(cudaGraphConditionalHandle hc, int* nactive) {
+  dep_wait();
   const int n = *nactive;
   *nactive = 0;
   cudaGraphSetConditional(hc, n > 0 ? 1u : 0u);
@@ -579,11 +589,11 @@ void launch_bstage(const Op* ops, const int4* tab, long long nchunks, const int*
   if (nchunks <= 0) return;
   int win;
   const unsigned g = (unsigned)grid_for(nchunks, 2, &win);
-  k_bstage<<<g, kBThreads, 0, s>>>(ops, tab, nchunks, win, active);
+  launch_dep(k_bstage, g, kBThreads, 0, s, ops, tab, nchunks, win, active);
 }
 
 void launch_binit(const BInst* bi, int ninst, int zero_x, int* active, int* nactive, cudaStream_t s) {
-  k_binit<<<ninst, kBThreads, 0, s>>>(bi, zero_x, active, nactive);
+  launch_dep(k_binit, ninst, kBThreads, 0, s, bi, zero_x, active, nactive);
 }
 
 void launch_bres(int kind, bool neumann, const BInst* bi, const int4* tab, long long nchunks, const int* active,
@@ -591,29 +601,29 @@ void launch_bres(int kind, bool neumann, const BInst* bi, const int4* tab, long 
   int win;
   const unsigned g = (unsigned)grid_for(nchunks, 6, &win);
   if (kind == OPK_RESID9) {
-    if (neumann) k_bres<OPK_RESID9, true><<<g, kBThreads, 0, s>>>(bi, tab, nchunks, win, active, partials);
-    else k_bres<OPK_RESID9, false><<<g, kBThreads, 0, s>>>(bi, tab, nchunks, win, active, partials);
+    if (neumann) launch_dep(k_bres<OPK_RESID9, true>, g, kBThreads, 0, s, bi, tab, nchunks, win, active, partials);
+    else launch_dep(k_bres<OPK_RESID9, false>, g, kBThreads, 0, s, bi, tab, nchunks, win, active, partials);
   } else {
-    if (neumann) k_bres<OPK_RESID5, true><<<g, kBThreads, 0, s>>>(bi, tab, nchunks, win, active, partials);
-    else k_bres<OPK_RESID5, false><<<g, kBThreads, 0, s>>>(bi, tab, nchunks, win, active, partials);
+    if (neumann) launch_dep(k_bres<OPK_RESID5, true>, g, kBThreads, 0, s, bi, tab, nchunks, win, active, partials);
+    else launch_dep(k_bres<OPK_RESID5, false>, g, kBThreads, 0, s, bi, tab, nchunks, win, active, partials);
   }
 }
 
 void launch_bfinal(const BInst* bi, const long long* cstart, int ninst, const double* partials, int* active,
                    int* nactive, cudaStream_t s) {
-  k_bfinal<<<ninst, kBThreads, 0, s>>>(bi, cstart, partials, active, nactive);
+  launch_dep(k_bfinal, ninst, kBThreads, 0, s, bi, cstart, partials, active, nactive);
 }
 
 void launch_brhs(const BInst* bi, const int4* tab, long long nchunks, const int* active, cudaStream_t s) {
   int win;
   const unsigned g = (unsigned)grid_for(nchunks, 6, &win);
-  k_brhs<<<g, kBThreads, 0, s>>>(bi, tab, nchunks, win, active);
+  launch_dep(k_brhs, g, kBThreads, 0, s, bi, tab, nchunks, win, active);
 }
 
 void launch_bupdate(const BInst* bi, const int4* tab, long long nchunks, const int* active, cudaStream_t s) {
   int win;
   const unsigned g = (unsigned)grid_for(nchunks, 6, &win);
-  k_bupdate<<<g, kBThreads, 0, s>>>(bi, tab, nchunks, win, active);
+  launch_dep(k_bupdate, g, kBThreads, 0, s, bi, tab, nchunks, win, active);
 }
 
 void launch_bres_int(int kind, bool neumann, const BInst* bi, const int4* ttab, long long ntasks, const int* active,
@@ -623,18 +633,18 @@ void launch_bres_int(int kind, bool neumann, const BInst* bi, const int4* ttab, 
   const long long want = (ntasks + kBThreads / 32 - 1) / (kBThreads / 32);  // one warp per task
   const unsigned grid = (unsigned)std::max(1LL, std::min(want, (long long)g_nsm * 8));
   if (kind == OPK_RESID9) {
-    if (neumann) k_bres_int<OPK_RESID9, true><<<grid, kBThreads, 0, s>>>(bi, ttab, ntasks, active, partials);
-    else k_bres_int<OPK_RESID9, false><<<grid, kBThreads, 0, s>>>(bi, ttab, ntasks, active, partials);
+    if (neumann) launch_dep(k_bres_int<OPK_RESID9, true>, grid, kBThreads, 0, s, bi, ttab, ntasks, active, partials);
+    else launch_dep(k_bres_int<OPK_RESID9, false>, grid, kBThreads, 0, s, bi, ttab, ntasks, active, partials);
   } else {
-    if (neumann) k_bres_int<OPK_RESID5, true><<<grid, kBThreads, 0, s>>>(bi, ttab, ntasks, active, partials);
-    else k_bres_int<OPK_RESID5, false><<<grid, kBThreads, 0, s>>>(bi, ttab, ntasks, active, partials);
+    if (neumann) launch_dep(k_bres_int<OPK_RESID5, true>, grid, kBThreads, 0, s, bi, ttab, ntasks, active, partials);
+    else launch_dep(k_bres_int<OPK_RESID5, false>, grid, kBThreads, 0, s, bi, ttab, ntasks, active, partials);
   }
 }
 
 void launch_brhs_shift(const BInst* bi, const int4* tab, long long nchunks, const int* active, cudaStream_t s) {
   int win;
   const unsigned g = (unsigned)grid_for(nchunks, 6, &win);
-  k_brhs_shift<<<g, kBThreads, 0, s>>>(bi, tab, nchunks, win, active);
+  launch_dep(k_brhs_shift, g, kBThreads, 0, s, bi, tab, nchunks, win, active);
 }
 
 void launch_bsmall(const BSmall* sm, int n, int smem, const int* active, cudaStream_t st) {
@@ -644,11 +654,11 @@ void launch_bsmall(const BSmall* sm, int n, int smem, const int* active, cudaStr
     cudaFuncSetAttribute(k_bsmall, cudaFuncAttributeMaxDynamicSharedMemorySize, kBSmallBytes);
     attr = true;
   }
-  k_bsmall<<<n, kBThreads, smem, st>>>(sm, active);
+  launch_dep(k_bsmall, n, kBThreads, smem, st, sm, active);
 }
 
 void launch_bcond(cudaGraphConditionalHandle hc, int* nactive, cudaStream_t s) {
-  k_bcond<<<1, 1, 0, s>>>(hc, nactive);
+  launch_dep(k_bcond, 1, 1, 0, s, hc, nactive);
 }
 
 }  // namespace cfmg

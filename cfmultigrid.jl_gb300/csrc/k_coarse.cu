@@ -163,6 +163,7 @@ __device__ void run_program(const Op* __restrict__ prog, int nops, long long t0,
 }
 
 __global__ void __launch_bounds__(kEngineThreads) k_program(const Op* __restrict__ prog, int nops, double* red) {
+  dep_wait();
   __shared__ Op op;
   __shared__ double sh[32];
   const long long t0 = (long long)cluster_rank() * blockDim.x + threadIdx.x;
@@ -234,13 +235,16 @@ void launch_program(const Op* prog, int nops, double* red, cudaStream_t s) {
   cfg.blockDim = dim3(kEngineThreads, 1, 1);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
+  cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = kEngineCtas;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
+  // a programmatic dependent of the kernel before it (k_program opens with dep_wait)
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = tl_dep_launch ? 2 : 1;
   cudaLaunchKernelEx(&cfg, k_program, prog, nops, red);
 }
 

@@ -31,6 +31,7 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_fused(double* __restrict__
                                                             long long lo, long long n, const double* __restrict__ ds,
                                                             float* __restrict__ b32, float* __restrict__ r32,
                                                             double* __restrict__ partials) {
+  dep_wait();
   const double scale = ds[0];
   double s2 = 0.0, s1 = 0.0, c1 = 0.0;
   const long long ni = bx.i1 - bx.i0 + 1, nj = bx.j1 - bx.j0 + 1;
@@ -92,6 +93,7 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_fused(double* __restrict__
 // 2^-round(log2(rms)) goes to S_NEXT (powers of two, exact both ways).
 __global__ void __launch_bounds__(kMxParts) k_fused_final(const double* __restrict__ partials, double* ds,
                                                           const double* normb, const double* nwet, int norm_kind) {
+  dep_wait();
   __shared__ double a[kMxParts], c[kMxParts];
   a[threadIdx.x] = partials[threadIdx.x];
   c[threadIdx.x] = partials[kMxParts + threadIdx.x];
@@ -134,6 +136,7 @@ __global__ void __launch_bounds__(kMxParts) k_fused_final(const double* __restri
 __global__ void k_rhs32_mean(const double* __restrict__ r, const uint8_t* __restrict__ m,
                              const double* __restrict__ ms, float* __restrict__ b32, float* __restrict__ r32,
                              long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= n) return;
   const float f = m[I] ? (float)((r[I] - ms[0]) * ms[S_CUR - S_MEAN2]) : 0.f;
@@ -144,6 +147,7 @@ __global__ void k_rhs32_mean(const double* __restrict__ r, const uint8_t* __rest
 // x += e * iscale
 __global__ void k_update_scaled(double* __restrict__ x, const float* __restrict__ e, const double* __restrict__ is,
                                 long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I < n) x[I] = __fma_rn((double)e[I], is[0], x[I]);
 }
@@ -202,6 +206,7 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int(const double* __restri
                                                           long long n, const double* __restrict__ ds,
                                                           float* __restrict__ b32, float* __restrict__ r32,
                                                           double* __restrict__ partials) {
+  dep_wait();
   constexpr int q = (KIND == OPK_RESID9) ? 2 : 0;  // Q = 2^q
   const int k = fix_exponent(ds);
   const float fm = (float)ldexp(ds[S_NEXT], -(k + q));  // power of two: R -> r * scale
@@ -292,6 +297,7 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __rest
                                                             const int8_t* __restrict__ dq, StripSpace sp,
                                                             const double* __restrict__ ds, float* __restrict__ b32,
                                                             float* __restrict__ r32, double* __restrict__ partials) {
+  dep_wait();
   constexpr int q = (KIND == OPK_RESID9) ? 2 : 0;  // Q = 2^q
   const int k = fix_exponent(ds);
   const double scale = ds[S_NEXT];
@@ -465,9 +471,9 @@ bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t
     rows = rows < kIntUnroll ? kIntUnroll : (rows > 96 ? 96 : rows);                                        \
     sp.rows = (int)((rows + kIntUnroll - 1) / kIntUnroll * kIntUnroll);                                     \
     if (neumann)                                                                                            \
-      k_resid_int2d<K, true><<<grid, kMxThreads, 0, s>>>(x, b, dq, sp, ds, b32, r32, partials);             \
+      launch_dep(k_resid_int2d<K, true>, grid, kMxThreads, 0, s, x, b, dq, sp, ds, b32, r32, partials);             \
     else                                                                                                    \
-      k_resid_int2d<K, false><<<grid, kMxThreads, 0, s>>>(x, b, dq, sp, ds, b32, r32, partials);            \
+      launch_dep(k_resid_int2d<K, false>, grid, kMxThreads, 0, s, x, b, dq, sp, ds, b32, r32, partials);            \
     return true;                                                                                            \
   }
   CFMG_INT2(OPK_RESID5)
@@ -481,6 +487,7 @@ bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t
 // ms = ds + S_MEAN2 (the FP32 shift sits in S_SHIFT, made once by k_fused_final)
 __global__ void k_rhs32_shift(const uint8_t* __restrict__ m, const double* __restrict__ ms, float* __restrict__ b32,
                               float* __restrict__ r32, long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= n) return;
   const float sh = *reinterpret_cast<const float*>(ms + (S_SHIFT - S_MEAN2));  // (float)(mean * scale)
@@ -493,6 +500,7 @@ __global__ void k_rhs32_shift(const uint8_t* __restrict__ m, const double* __res
 // integer in 0..127 or a mask value is not 0/1
 __global__ void k_make_dq(const double* __restrict__ diag, const uint8_t* __restrict__ m, double Q, int8_t* dq,
                           long long n, int* ok) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= n) return;
   int8_t v = -128;
@@ -512,6 +520,7 @@ __global__ void k_make_dq(const double* __restrict__ diag, const uint8_t* __rest
 // tx, ty the array's row and plane extents) into ds[S_MAXO]; all start at 0
 __global__ void k_maxabs2(const double* __restrict__ x, const double* __restrict__ b, long long n, int tx, int ty,
                           int ui0, int ui1, int uj0, int uj1, double* ds) {
+  dep_wait();
   unsigned long long mx = 0, mb = 0, mo = 0;
   const long long nrows = n / tx;  // rows of all layers
   for (long long row = blockIdx.x; row < nrows; row += gridDim.x) {
@@ -549,6 +558,7 @@ __global__ void k_maxabs2(const double* __restrict__ x, const double* __restrict
 __global__ void __launch_bounds__(kMxThreads) k_update_scaled_max(double* __restrict__ x, const float* __restrict__ e,
                                                                   const double* __restrict__ ds, long long n,
                                                                   double* dsw) {
+  dep_wait();
   const double is = ds[S_ICUR];
   const int pe = pow2_exponent(is);  // iscale = 2^pe
   unsigned long long mx = 0;
@@ -590,9 +600,9 @@ void launch_resid_int(int kind, const double* x, const double* b, const int8_t* 
 #define CFMG_INT(K)                                                                                        \
   if (kind == K) {                                                                                         \
     if (neumann)                                                                                           \
-      k_resid_int<K, true><<<kMxParts, kMxThreads, 0, s>>>(x, b, dq, g, bx, lo, n, ds, b32, r32, partials); \
+      launch_dep(k_resid_int<K, true>, kMxParts, kMxThreads, 0, s, x, b, dq, g, bx, lo, n, ds, b32, r32, partials); \
     else                                                                                                   \
-      k_resid_int<K, false><<<kMxParts, kMxThreads, 0, s>>>(x, b, dq, g, bx, lo, n, ds, b32, r32, partials); \
+      launch_dep(k_resid_int<K, false>, kMxParts, kMxThreads, 0, s, x, b, dq, g, bx, lo, n, ds, b32, r32, partials); \
     return;                                                                                                \
   }
   CFMG_INT(OPK_RESID5)
@@ -603,17 +613,17 @@ void launch_resid_int(int kind, const double* x, const double* b, const int8_t* 
 
 void launch_rhs32_shift(const uint8_t* m, const double* mean_scale, float* b32, float* r32, long long n,
                         cudaStream_t s) {
-  k_rhs32_shift<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(m, mean_scale, b32, r32, n);
+  launch_dep(k_rhs32_shift, (unsigned)((n + 255) / 256), 256, 0, s, m, mean_scale, b32, r32, n);
 }
 
 void launch_make_dq(const double* diag, const uint8_t* m, double Q, int8_t* dq, long long n, int* ok,
                     cudaStream_t s) {
-  k_make_dq<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(diag, m, Q, dq, n, ok);
+  launch_dep(k_make_dq, (unsigned)((n + 255) / 256), 256, 0, s, diag, m, Q, dq, n, ok);
 }
 
 void launch_maxabs2(const double* x, const double* b, long long n, int tx, int ty, int ui0, int ui1, int uj0, int uj1,
                     double* ds, cudaStream_t s) {
-  k_maxabs2<<<1024, 256, 0, s>>>(x, b, n, tx, ty, ui0, ui1, uj0, uj1, ds);
+  launch_dep(k_maxabs2, 1024, 256, 0, s, x, b, n, tx, ty, ui0, ui1, uj0, uj1, ds);
 }
 
 void launch_update_scaled_max(double* x, const float* e, double* ds, long long n, cudaStream_t s) {
@@ -623,7 +633,7 @@ void launch_update_scaled_max(double* x, const float* e, double* ds, long long n
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   }
-  k_update_scaled_max<<<nsm * 4, kMxThreads, 0, s>>>(x, e, ds, n, ds);  // 4 blocks per SM: measured 4 % faster than 8
+  launch_dep(k_update_scaled_max, nsm * 4, kMxThreads, 0, s, x, e, ds, n, ds);  // 4 blocks per SM: measured 4 % faster than 8
 }
 
 void launch_resid_fused(int kind, double* r, const double* x, const double* b, const double* d, const uint8_t* m,
@@ -632,9 +642,9 @@ void launch_resid_fused(int kind, double* r, const double* x, const double* b, c
 #define CFMG_FUSED(K)                                                                                            \
   if (kind == K) {                                                                                               \
     if (neumann)                                                                                                 \
-      k_resid_fused<K, true><<<kMxParts, kMxThreads, 0, s>>>(r, x, b, d, m, g, bx, lo, n, scale, b32, r32, partials); \
+      launch_dep(k_resid_fused<K, true>, kMxParts, kMxThreads, 0, s, r, x, b, d, m, g, bx, lo, n, scale, b32, r32, partials); \
     else                                                                                                         \
-      k_resid_fused<K, false><<<kMxParts, kMxThreads, 0, s>>>(r, x, b, d, m, g, bx, lo, n, scale, b32, r32, partials); \
+      launch_dep(k_resid_fused<K, false>, kMxParts, kMxThreads, 0, s, r, x, b, d, m, g, bx, lo, n, scale, b32, r32, partials); \
     return;                                                                                                      \
   }
   CFMG_FUSED(OPK_RESID5)
@@ -646,16 +656,16 @@ void launch_resid_fused(int kind, double* r, const double* x, const double* b, c
 
 void launch_fused_final(const double* partials, double* ds, const double* normb, const double* nwet, int norm_kind,
                         cudaStream_t s) {
-  k_fused_final<<<1, kMxParts, 0, s>>>(partials, ds, normb, nwet, norm_kind);
+  launch_dep(k_fused_final, 1, kMxParts, 0, s, partials, ds, normb, nwet, norm_kind);
 }
 
 void launch_rhs32_mean(const double* r, const uint8_t* m, const double* mean_scale, float* b32, float* r32,
                        long long n, cudaStream_t s) {
-  k_rhs32_mean<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(r, m, mean_scale, b32, r32, n);
+  launch_dep(k_rhs32_mean, (unsigned)((n + 255) / 256), 256, 0, s, r, m, mean_scale, b32, r32, n);
 }
 
 void launch_update_scaled(double* x, const float* e, const double* iscale, long long n, cudaStream_t s) {
-  k_update_scaled<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, e, iscale, n);
+  launch_dep(k_update_scaled, (unsigned)((n + 255) / 256), 256, 0, s, x, e, iscale, n);
 }
 
 }  // namespace cfmg

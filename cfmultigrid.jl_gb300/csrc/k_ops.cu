@@ -27,6 +27,7 @@ template <class T>
 __global__ void __launch_bounds__(kThreads) k_sweep5_2d(const T* __restrict__ x, T* __restrict__ y,
                                                         const T* __restrict__ b, const T* __restrict__ w, T cff,
                                                         long long n1, long long lo, long long hi) {
+  dep_wait();
   long long I = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I < hi) d_sweep5(x, y, b, w, cff, n1, I);
 }
@@ -36,6 +37,7 @@ template <class T>
 __global__ void __launch_bounds__(kThreads) k_sweep7_3d(const T* __restrict__ x, T* __restrict__ y,
                                                         const T* __restrict__ b, const T* __restrict__ w, T cff,
                                                         long long n1, long long n2, long long lo, long long hi) {
+  dep_wait();
   long long I = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I < hi) d_sweep7(x, y, b, w, cff, n1, n2, I);
 }
@@ -64,6 +66,7 @@ template <class T>
 __global__ void __launch_bounds__(kThreads) k_sweep9_2d(const T* __restrict__ x, T* __restrict__ y,
                                                         const T* __restrict__ b, const T* __restrict__ w, T cff,
                                                         Geom g, Box bx) {
+  dep_wait();
   BoxIdx q = box_idx(bx);
   if (q.ok) d_sweep9(x, y, b, w, cff, g.n1, lin(g, q.i, q.j, q.k));
 }
@@ -72,6 +75,7 @@ template <class T>
 __global__ void __launch_bounds__(kThreads) k_sweep19_3d(const T* __restrict__ x, T* __restrict__ y,
                                                          const T* __restrict__ b, const T* __restrict__ w, T cff,
                                                          Geom g, Box bx) {
+  dep_wait();
   BoxIdx q = box_idx(bx);
   if (q.ok) d_sweep19(x, y, b, w, cff, g.n1, g.n2, lin(g, q.i, q.j, q.k));
 }
@@ -81,6 +85,7 @@ __global__ void __launch_bounds__(kThreads) k_sweep_vc_2d(const T* __restrict__ 
                                                           const T* __restrict__ b, const T* __restrict__ w,
                                                           const T* __restrict__ cE, const T* __restrict__ cN, T cff,
                                                           long long n1, long long lo, long long hi) {
+  dep_wait();
   long long I = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I < hi) d_sweepvc(x, y, b, w, cE, cN, cff, n1, I);
 }
@@ -92,6 +97,7 @@ __global__ void __launch_bounds__(kThreads) k_resid5_2d(T* __restrict__ r, const
                                                         const T* __restrict__ b, const T* __restrict__ d,
                                                         const uint8_t* __restrict__ m, long long n1, long long lo,
                                                         long long hi) {
+  dep_wait();
   long long I = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I < hi) d_resid5(r, x, b, d, m, n1, I);
 }
@@ -101,6 +107,7 @@ template <class T>
 __global__ void __launch_bounds__(kThreads) k_resid7_3d(T* __restrict__ r, const T* __restrict__ x,
                                                         const T* __restrict__ b, const T* __restrict__ d,
                                                         const uint8_t* __restrict__ m, Geom g, Box bx) {
+  dep_wait();
   BoxIdx q = box_idx(bx);
   if (q.ok) d_resid7(r, x, b, d, m, g.n1, g.n2, lin(g, q.i, q.j, q.k));
 }
@@ -110,6 +117,7 @@ template <class T>
 __global__ void __launch_bounds__(kThreads) k_resid9_2d(T* __restrict__ r, const T* __restrict__ x,
                                                         const T* __restrict__ b, const T* __restrict__ d,
                                                         const uint8_t* __restrict__ m, Geom g, Box bx) {
+  dep_wait();
   BoxIdx q = box_idx(bx);
   if (q.ok) d_resid9(r, x, b, d, m, g.n1, lin(g, q.i, q.j, q.k));
 }
@@ -119,6 +127,7 @@ template <class T>
 __global__ void __launch_bounds__(kThreads) k_resid19_3d(T* __restrict__ r, const T* __restrict__ x,
                                                          const T* __restrict__ b, const T* __restrict__ d,
                                                          const uint8_t* __restrict__ m, Geom g, Box bx) {
+  dep_wait();
   BoxIdx q = box_idx(bx);
   if (q.ok) d_resid19(r, x, b, d, m, g.n1, g.n2, lin(g, q.i, q.j, q.k));
 }
@@ -129,6 +138,7 @@ __global__ void __launch_bounds__(kThreads) k_resid_vc_2d(T* __restrict__ r, con
                                                           const T* __restrict__ cE, const T* __restrict__ cN,
                                                           const uint8_t* __restrict__ m, long long n1, long long lo,
                                                           long long hi) {
+  dep_wait();
   long long I = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I < hi) d_residvc(r, x, b, d, cE, cN, m, n1, I);
 }
@@ -139,6 +149,7 @@ __global__ void __launch_bounds__(kThreads) k_resid_vc_2d(T* __restrict__ r, con
 template <class T, int KIND>
 __global__ void __launch_bounds__(kThreads) k_restrict(const T* __restrict__ x, T* __restrict__ xc,
                                                        const T* __restrict__ coef, Geom gf, Geom gc, Box cb) {
+  dep_wait();
   BoxIdx q = box_idx(cb);
   if (q.ok) d_restrict<T, KIND>(x, xc, coef, gf, gc, q.i, q.j, q.k);
 }
@@ -151,6 +162,7 @@ template <class T, int KIND, bool ASSIGN>
 __global__ void __launch_bounds__(kThreads) k_prolong(T* __restrict__ xf, const T* __restrict__ x,
                                                       const T* __restrict__ coef, Geom gf, Geom gc, int np_i,
                                                       int np_j, int kf0, int kf1, int np_k) {
+  dep_wait();
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const int qj = blockIdx.y * blockDim.y + threadIdx.y;
   const int qk = blockIdx.z;
@@ -163,6 +175,7 @@ __global__ void __launch_bounds__(kThreads) k_prolong(T* __restrict__ xf, const 
 // before they write, as Julia's sliced assignment does.
 template <class T>
 __global__ void __launch_bounds__(kThreads) k_fill_xperio(T* __restrict__ x, int tx, int nh, long long nlines) {
+  dep_wait();
   long long L = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (L < nlines) d_fill_line(x + L * tx, tx, nh);
 }
@@ -174,6 +187,7 @@ __global__ void __launch_bounds__(kThreads) k_fill_xperio(T* __restrict__ x, int
 template <class T>
 __global__ void __launch_bounds__(kThreads) k_norm_partial(const T* __restrict__ x, const uint8_t* __restrict__ m,
                                                            long long n, double* __restrict__ partials) {
+  dep_wait();
   double s = 0.0;
   for (long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x; I < n; I += (long long)gridDim.x * blockDim.x) {
     uint8_t mm = m[I];
@@ -197,6 +211,7 @@ __global__ void __launch_bounds__(kThreads) k_norm_partial(const T* __restrict__
 
 __global__ void __launch_bounds__(kNormParts) k_norm_final(const double* __restrict__ partials, double* out,
                                                            const double* normb, int norm_kind) {
+  dep_wait();
   __shared__ double sh[kNormParts];
   sh[threadIdx.x] = partials[threadIdx.x];
   __syncthreads();
@@ -222,63 +237,63 @@ template <class T>
 void launch_sweep5_2d(const T* x, T* y, const T* b, const T* w, T cff, const Geom& g, cudaStream_t s) {
   long long lo = g.n1, hi = g.len - g.n1;
   if (hi <= lo) return;
-  k_sweep5_2d<T><<<nblocks(hi - lo), kThreads, 0, s>>>(x, y, b, w, cff, g.n1, lo, hi);
+  launch_dep(k_sweep5_2d<T>, nblocks(hi - lo), kThreads, 0, s, x, y, b, w, cff, g.n1, lo, hi);
 }
 template <class T>
 void launch_sweep7_3d(const T* x, T* y, const T* b, const T* w, T cff, const Geom& g, cudaStream_t s) {
   long long lo = g.n2, hi = g.len - g.n2;
   if (hi <= lo) return;
-  k_sweep7_3d<T><<<nblocks(hi - lo), kThreads, 0, s>>>(x, y, b, w, cff, g.n1, g.n2, lo, hi);
+  launch_dep(k_sweep7_3d<T>, nblocks(hi - lo), kThreads, 0, s, x, y, b, w, cff, g.n1, g.n2, lo, hi);
 }
 template <class T>
 void launch_sweep9_2d(const T* x, T* y, const T* b, const T* w, T cff, const Geom& g, const Box& bx,
                       cudaStream_t s) {
   if (box_empty(bx)) return;
-  k_sweep9_2d<T><<<box_grid(bx, kBoxBlk), kBoxBlk, 0, s>>>(x, y, b, w, cff, g, bx);
+  launch_dep(k_sweep9_2d<T>, box_grid(bx, kBoxBlk), kBoxBlk, 0, s, x, y, b, w, cff, g, bx);
 }
 template <class T>
 void launch_sweep19_3d(const T* x, T* y, const T* b, const T* w, T cff, const Geom& g, const Box& bx,
                        cudaStream_t s) {
   if (box_empty(bx)) return;
-  k_sweep19_3d<T><<<box_grid(bx, kBoxBlk), kBoxBlk, 0, s>>>(x, y, b, w, cff, g, bx);
+  launch_dep(k_sweep19_3d<T>, box_grid(bx, kBoxBlk), kBoxBlk, 0, s, x, y, b, w, cff, g, bx);
 }
 template <class T>
 void launch_sweep_vc_2d(const T* x, T* y, const T* b, const T* w, const T* cE, const T* cN, T cff, const Geom& g,
                         cudaStream_t s) {
   long long lo = g.n1, hi = g.len - g.n1;
   if (hi <= lo) return;
-  k_sweep_vc_2d<T><<<nblocks(hi - lo), kThreads, 0, s>>>(x, y, b, w, cE, cN, cff, g.n1, lo, hi);
+  launch_dep(k_sweep_vc_2d<T>, nblocks(hi - lo), kThreads, 0, s, x, y, b, w, cE, cN, cff, g.n1, lo, hi);
 }
 template <class T>
 void launch_resid5_2d(T* r, const T* x, const T* b, const T* d, const uint8_t* m, const Geom& g, cudaStream_t s) {
   long long lo = g.n1, hi = g.len - g.n1;
   if (hi <= lo) return;
-  k_resid5_2d<T><<<nblocks(hi - lo), kThreads, 0, s>>>(r, x, b, d, m, g.n1, lo, hi);
+  launch_dep(k_resid5_2d<T>, nblocks(hi - lo), kThreads, 0, s, r, x, b, d, m, g.n1, lo, hi);
 }
 template <class T>
 void launch_resid7_3d(T* r, const T* x, const T* b, const T* d, const uint8_t* m, const Geom& g, const Box& bx,
                       cudaStream_t s) {
   if (box_empty(bx)) return;
-  k_resid7_3d<T><<<box_grid(bx, kBoxBlk), kBoxBlk, 0, s>>>(r, x, b, d, m, g, bx);
+  launch_dep(k_resid7_3d<T>, box_grid(bx, kBoxBlk), kBoxBlk, 0, s, r, x, b, d, m, g, bx);
 }
 template <class T>
 void launch_resid9_2d(T* r, const T* x, const T* b, const T* d, const uint8_t* m, const Geom& g, const Box& bx,
                       cudaStream_t s) {
   if (box_empty(bx)) return;
-  k_resid9_2d<T><<<box_grid(bx, kBoxBlk), kBoxBlk, 0, s>>>(r, x, b, d, m, g, bx);
+  launch_dep(k_resid9_2d<T>, box_grid(bx, kBoxBlk), kBoxBlk, 0, s, r, x, b, d, m, g, bx);
 }
 template <class T>
 void launch_resid19_3d(T* r, const T* x, const T* b, const T* d, const uint8_t* m, const Geom& g, const Box& bx,
                        cudaStream_t s) {
   if (box_empty(bx)) return;
-  k_resid19_3d<T><<<box_grid(bx, kBoxBlk), kBoxBlk, 0, s>>>(r, x, b, d, m, g, bx);
+  launch_dep(k_resid19_3d<T>, box_grid(bx, kBoxBlk), kBoxBlk, 0, s, r, x, b, d, m, g, bx);
 }
 template <class T>
 void launch_resid_vc_2d(T* r, const T* x, const T* b, const T* d, const T* cE, const T* cN, const uint8_t* m,
                         const Geom& g, cudaStream_t s) {
   long long lo = g.n1, hi = g.len - g.n1;
   if (hi <= lo) return;
-  k_resid_vc_2d<T><<<nblocks(hi - lo), kThreads, 0, s>>>(r, x, b, d, cE, cN, m, g.n1, lo, hi);
+  launch_dep(k_resid_vc_2d<T>, nblocks(hi - lo), kThreads, 0, s, r, x, b, d, cE, cN, m, g.n1, lo, hi);
 }
 template <class T>
 void launch_restrict(int kind, const T* xf, T* bc, const T* Rcoef, const Geom& gf, const Geom& gc, const Box& cb,
@@ -286,10 +301,10 @@ void launch_restrict(int kind, const T* xf, T* bc, const T* Rcoef, const Geom& g
   if (box_empty(cb)) return;
   dim3 grid = box_grid(cb, kBoxBlk);
   switch (kind) {
-    case 0: k_restrict<T, 0><<<grid, kBoxBlk, 0, s>>>(xf, bc, Rcoef, gf, gc, cb); break;
-    case 1: k_restrict<T, 1><<<grid, kBoxBlk, 0, s>>>(xf, bc, Rcoef, gf, gc, cb); break;
-    case 2: k_restrict<T, 2><<<grid, kBoxBlk, 0, s>>>(xf, bc, Rcoef, gf, gc, cb); break;
-    default: k_restrict<T, 3><<<grid, kBoxBlk, 0, s>>>(xf, bc, Rcoef, gf, gc, cb); break;
+    case 0: launch_dep(k_restrict<T, 0>, grid, kBoxBlk, 0, s, xf, bc, Rcoef, gf, gc, cb); break;
+    case 1: launch_dep(k_restrict<T, 1>, grid, kBoxBlk, 0, s, xf, bc, Rcoef, gf, gc, cb); break;
+    case 2: launch_dep(k_restrict<T, 2>, grid, kBoxBlk, 0, s, xf, bc, Rcoef, gf, gc, cb); break;
+    default: launch_dep(k_restrict<T, 3>, grid, kBoxBlk, 0, s, xf, bc, Rcoef, gf, gc, cb); break;
   }
 }
 template <class T>
@@ -305,9 +320,9 @@ void launch_prolong(int kind, T* xf, const T* xc, const T* Pcoef, const Geom& gf
 #define CFMG_PRO(K)                                                                                       \
   case K:                                                                                                 \
     if (assign)                                                                                           \
-      k_prolong<T, K, true><<<grid, blk, 0, s>>>(xf, xc, Pcoef, gf, gc, np_i, np_j, kf0, kf1, np_k);      \
+      launch_dep(k_prolong<T, K, true>, grid, blk, 0, s, xf, xc, Pcoef, gf, gc, np_i, np_j, kf0, kf1, np_k);      \
     else                                                                                                  \
-      k_prolong<T, K, false><<<grid, blk, 0, s>>>(xf, xc, Pcoef, gf, gc, np_i, np_j, kf0, kf1, np_k);     \
+      launch_dep(k_prolong<T, K, false>, grid, blk, 0, s, xf, xc, Pcoef, gf, gc, np_i, np_j, kf0, kf1, np_k);     \
     break;
   switch (kind) {
     CFMG_PRO(0)
@@ -321,13 +336,13 @@ void launch_prolong(int kind, T* xf, const T* xc, const T* Pcoef, const Geom& gf
 template <class T>
 void launch_fill_xperio(T* x, const Geom& g, cudaStream_t s) {
   long long nlines = (long long)g.ty * g.tz;
-  k_fill_xperio<T><<<nblocks(nlines), kThreads, 0, s>>>(x, g.tx, g.nh, nlines);
+  launch_dep(k_fill_xperio<T>, nblocks(nlines), kThreads, 0, s, x, g.tx, g.nh, nlines);
 }
 template <class T>
 void launch_norm(const T* x, const uint8_t* m, size_t n, double* partials, double* out, const double* normb,
                  int norm_kind, cudaStream_t s) {
-  k_norm_partial<T><<<kNormParts, kThreads, 0, s>>>(x, m, (long long)n, partials);
-  k_norm_final<<<1, kNormParts, 0, s>>>(partials, out, normb, norm_kind);
+  launch_dep(k_norm_partial<T>, kNormParts, kThreads, 0, s, x, m, (long long)n, partials);
+  launch_dep(k_norm_final, 1, kNormParts, 0, s, partials, out, normb, norm_kind);
 }
 
 #define CFMG_INST(T)                                                                                             \
@@ -363,10 +378,12 @@ template void launch_fill_xperio<uint8_t>(uint8_t*, const Geom&, cudaStream_t);
 namespace cfmg {
 
 __global__ void k_f32_to_f64(const float* a, double* out, long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I < n) out[I] = (double)a[I];
 }
 __global__ void k_f64_to_f32(const double* a, float* out, long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I < n) out[I] = (float)a[I];
 }
@@ -416,11 +433,11 @@ static void launch_op_t(const Op& op, cudaStream_t s) {
 
 void launch_op(const Op& op, cudaStream_t s) {
   if (op.kind == OPK_F32TO64) {
-    k_f32_to_f64<<<nblocks(op.n), kThreads, 0, s>>>((const float*)op.x, (double*)op.y, op.n);
+    launch_dep(k_f32_to_f64, nblocks(op.n), kThreads, 0, s, (const float*)op.x, (double*)op.y, op.n);
     return;
   }
   if (op.kind == OPK_F64TO32) {
-    k_f64_to_f32<<<nblocks(op.n), kThreads, 0, s>>>((const double*)op.x, (float*)op.y, op.n);
+    launch_dep(k_f64_to_f32, nblocks(op.n), kThreads, 0, s, (const double*)op.x, (float*)op.y, op.n);
     return;
   }
   if (op.prec == 0) launch_op_t<double>(op, s);

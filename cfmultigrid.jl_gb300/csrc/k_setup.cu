@@ -27,6 +27,7 @@ __device__ __forceinline__ uint8_t defmsk_raw(int i, int j, int k, int nx, int n
 // (the fill! at the end of get_default_msk!).
 __global__ void k_default_msk(int mode, uint8_t* msk, double* f, double coef, int nx, int ny, int nz, int nh,
                               int tx, int ty, long long len, bool vertices, bool threed, bool xperio) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= len) return;
   int i = (int)(I % tx) + 1;
@@ -46,37 +47,40 @@ __global__ void k_default_msk(int mode, uint8_t* msk, double* f, double coef, in
 
 void launch_default_msk(int mode, uint8_t* msk, double* f, double coef, const Level& l, bool vertices, bool threed,
                         bool xperio, cudaStream_t s) {
-  k_default_msk<<<nb(l.len), kT, 0, s>>>(mode, msk, f, coef, l.nx, l.ny, l.nz, l.nh, l.tx, l.ty, (long long)l.len,
-                                         vertices, threed, xperio);
+  launch_dep(k_default_msk, nb(l.len), kT, 0, s, mode, msk, f, coef, l.nx, l.ny, l.nz, l.nh, l.tx, l.ty, (long long)l.len, vertices, threed, xperio);
 }
 
 __global__ void k_fill_f64(double* a, double v, long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I < n) a[I] = v;
 }
 void launch_fill_f64(double* a, double v, size_t n, cudaStream_t s) {
-  k_fill_f64<<<nb(n), kT, 0, s>>>(a, v, (long long)n);
+  launch_dep(k_fill_f64, nb(n), kT, 0, s, a, v, (long long)n);
 }
 
 __global__ void k_u8_to_f64(const uint8_t* m, double* out, long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I < n) out[I] = (double)m[I];
 }
 void launch_u8_to_f64(const uint8_t* m, double* out, size_t n, cudaStream_t s) {
-  k_u8_to_f64<<<nb(n), kT, 0, s>>>(m, out, (long long)n);
+  launch_dep(k_u8_to_f64, nb(n), kT, 0, s, m, out, (long long)n);
 }
 
 // msk = b > threshold (compute_msk_dev, src/gmg_setup.jl:360-362)
 __global__ void k_threshold(const double* b, uint8_t* msk, double thr, long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I < n) msk[I] = (b[I] > thr) ? 1 : 0;
 }
 void launch_threshold(const double* b, uint8_t* msk, double thr, size_t n, cudaStream_t s) {
-  k_threshold<<<nb(n), kT, 0, s>>>(b, msk, thr, (long long)n);
+  launch_dep(k_threshold, nb(n), kT, 0, s, b, msk, thr, (long long)n);
 }
 
 // Rcoef = msk * f(b) (compute_Rcoef!, src/gmg_setup.jl:203-211)
 __global__ void k_rcoef(const uint8_t* msk, const double* b, double* R, bool vertices, double coef, long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= n) return;
   double bb = b[I];
@@ -85,22 +89,24 @@ __global__ void k_rcoef(const uint8_t* msk, const double* b, double* R, bool ver
 }
 void launch_rcoef(const uint8_t* msk, const double* b, double* R, bool vertices, double coef, size_t n,
                   cudaStream_t s) {
-  k_rcoef<<<nb(n), kT, 0, s>>>(msk, b, R, vertices, coef, (long long)n);
+  launch_dep(k_rcoef, nb(n), kT, 0, s, msk, b, R, vertices, coef, (long long)n);
 }
 
 // Pcoef = (x>0 ? 1/x : 0) * msk (compute_Pcoef!, src/gmg_setup.jl:232-236)
 __global__ void k_pcoef(const uint8_t* msk, const double* x, double* P, long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= n) return;
   double xv = x[I];
   P[I] = __dmul_rn((xv > 0) ? __ddiv_rn(1.0, xv) : 0.0, (double)msk[I]);
 }
 void launch_pcoef(const uint8_t* msk, const double* x, double* P, size_t n, cudaStream_t s) {
-  k_pcoef<<<nb(n), kT, 0, s>>>(msk, x, P, (long long)n);
+  launch_dep(k_pcoef, nb(n), kT, 0, s, msk, x, P, (long long)n);
 }
 
 // diag = -r*msk; idiag = diag>0 ? 1/diag : 0 (compute_diag!, src/gmg_setup.jl:258-261)
 __global__ void k_diag(const uint8_t* msk, const double* r, double* diag, double* idiag, long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= n) return;
   double d = __dmul_rn(-r[I], (double)msk[I]);
@@ -108,22 +114,24 @@ __global__ void k_diag(const uint8_t* msk, const double* r, double* diag, double
   idiag[I] = (d > 0.0) ? __ddiv_rn(1.0, d) : 0.0;
 }
 void launch_diag(const uint8_t* msk, const double* r, double* diag, double* idiag, size_t n, cudaStream_t s) {
-  k_diag<<<nb(n), kT, 0, s>>>(msk, r, diag, idiag, (long long)n);
+  launch_dep(k_diag, nb(n), kT, 0, s, msk, r, diag, idiag, (long long)n);
 }
 
 // widiag = omega*idiag: the product the reference forms inside every sweep
 // (src/laplacian.jl:69, `omega*idiag[I]`), computed once.
 __global__ void k_widiag(const double* idiag, double* w, double omega, long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I < n) w[I] = __dmul_rn(omega, idiag[I]);
 }
 void launch_widiag(const double* idiag, double* w, double omega, size_t n, cudaStream_t s) {
-  k_widiag<<<nb(n), kT, 0, s>>>(idiag, w, omega, (long long)n);
+  launch_dep(k_widiag, nb(n), kT, 0, s, idiag, w, omega, (long long)n);
 }
 
 // Coarse kappa of the variable-coefficient operator: mean of kappa over the
 // wet children (1 where none is wet); written on the coarse interior.
 __global__ void k_restrict_kappa(const double* kf, const uint8_t* mf, double* kc, Geom gf, Geom gc, Box cb) {
+  dep_wait();
   int ii = cb.i0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
   int jj = cb.j0 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
   int kk = cb.k0 + (int)blockIdx.z;
@@ -146,12 +154,13 @@ void launch_restrict_kappa(const double* kf, const uint8_t* mf, double* kc, cons
                            const Box& cb, cudaStream_t s) {
   dim3 blk(64, 4, 1);
   dim3 grid((unsigned)((cb.i1 - cb.i0 + 64) / 64), (unsigned)((cb.j1 - cb.j0 + 4) / 4), (unsigned)(cb.k1 - cb.k0 + 1));
-  k_restrict_kappa<<<grid, blk, 0, s>>>(kf, mf, kc, gf, gc, cb);
+  launch_dep(k_restrict_kappa, grid, blk, 0, s, kf, mf, kc, gf, gc, cb);
 }
 
 // Face coefficients: cE[I] between I and I+1, cN[I] between I and I+n1,
 // (kappa_I + kappa_J)/2 when both cells are wet, else 0.
 __global__ void k_face_coef(const double* kap, const uint8_t* m, double* cE, double* cN, long long n1, long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= n) return;
   double e = 0.0, nn = 0.0;
@@ -162,15 +171,16 @@ __global__ void k_face_coef(const double* kap, const uint8_t* m, double* cE, dou
 }
 void launch_face_coef(const double* kappa, const uint8_t* msk, double* cE, double* cN, const Geom& g,
                       cudaStream_t s) {
-  k_face_coef<<<nb((size_t)g.len), kT, 0, s>>>(kappa, msk, cE, cN, g.n1, g.len);
+  launch_dep(k_face_coef, nb((size_t)g.len), kT, 0, s, kappa, msk, cE, cN, g.n1, g.len);
 }
 
 __global__ void k_to_f32(const double* a, float* out, long long n) {
+  dep_wait();
   long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I < n) out[I] = (float)a[I];
 }
 void launch_to_f32(const double* a, float* out, size_t n, cudaStream_t s) {
-  k_to_f32<<<nb(n), kT, 0, s>>>(a, out, (long long)n);
+  launch_dep(k_to_f32, nb(n), kT, 0, s, a, out, (long long)n);
 }
 
 }  // namespace cfmg

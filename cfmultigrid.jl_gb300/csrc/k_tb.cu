@@ -310,6 +310,7 @@ __global__ void __launch_bounds__(kT3Tx * kT3Ty, 1) k_smooth_tb3(const float* __
                                                                  const float* __restrict__ b,
                                                                  const float* __restrict__ w, float cff, int tx,
                                                                  int ty, int ui0, int ui1, int uj0, int uj1) {
+  dep_wait();
   extern __shared__ float smem[];
   tb3_tile<ST, NITE>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1, (int)blockIdx.x, (int)blockIdx.y,
                      (int)blockIdx.z, smem);
@@ -440,6 +441,7 @@ __global__ void __launch_bounds__(kT5Tx * TY, MINB) k_smooth_tb5(const float* __
                                                                  const float* __restrict__ w, float cff, int tx,
                                                                  int ty, int ui0, int ui1, int uj0, int uj1,
                                                                  TbEpi ep) {
+  dep_wait();
   extern __shared__ float smem[];
   // with the epilogue the core is 2 cells narrower: r is needed one cell
   // beyond it, and x one cell beyond that
@@ -702,6 +704,7 @@ __global__ void __launch_bounds__(kTbW * kTbTy, 1) k_smooth_tb(const float* __re
                                                                const float* __restrict__ b,
                                                                const float* __restrict__ w, float cff, int tx,
                                                                int ty, int ui0, int ui1, int uj0, int uj1) {
+  dep_wait();
   extern __shared__ float smem[];
   tb_tile<ST, NITE>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z,
                     smem);
@@ -715,6 +718,7 @@ __global__ void __launch_bounds__(kTbW * kTbTy, 1) k_smooth_tb(const float* __re
 template <int ST, int NITE>
 __global__ void __launch_bounds__(kTbW * kTbTy, 1) k_btb(const Op* __restrict__ ops, const int4* __restrict__ tab,
                                                          long long ntiles, int win, const int* __restrict__ active) {
+  dep_wait();
   extern __shared__ float smem[];
   __shared__ int list[kTbW * kTbTy];
   __shared__ int wsum[kTbW * kTbTy / 32 + 1];
@@ -769,7 +773,7 @@ static void launch_tb3_n(const float* x, float* xo, const float* b, const float*
     attr = true;
   }
   dim3 grid((unsigned)((ui1 - ui0 + CW) / CW), (unsigned)((uj1 - uj0 + CH) / CH), (unsigned)nz);
-  k_smooth_tb3<ST, NITE><<<grid, dim3(kT3Tx, kT3Ty, 1), smem, s>>>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1);
+  launch_dep(k_smooth_tb3<ST, NITE>, grid, dim3(kT3Tx, kT3Ty, 1), smem, s, x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1);
 }
 
 template <int ST, int NITE, int TY, int ROWS, int MINB, bool EPI, bool PER = false, bool UPD = false>
@@ -786,8 +790,7 @@ static void launch_tb5_n(const float* x, float* xo, const float* b, const float*
     attr = true;
   }
   dim3 grid((unsigned)((ui1 - ui0 + CW) / CW), (unsigned)((uj1 - uj0 + CH) / CH), (unsigned)nz);
-  k_smooth_tb5<ST, NITE, TY, ROWS, MINB, EPI, PER, UPD>
-      <<<grid, dim3(kT5Tx, TY, 1), smem, s>>>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1, ep);
+  launch_dep(k_smooth_tb5<ST, NITE, TY, ROWS, MINB, EPI, PER, UPD>, grid, dim3(kT5Tx, TY, 1), smem, s, x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1, ep);
 }
 
 template <int ST, int NITE>
@@ -812,7 +815,7 @@ static void launch_tb_n(int version, const float* x, float* xo, const float* b, 
     attr = true;
   }
   dim3 grid((unsigned)((ui1 - ui0 + CW) / CW), (unsigned)((uj1 - uj0 + CH) / CH), (unsigned)nz);
-  k_smooth_tb<ST, NITE><<<grid, dim3(kTbW, kTbTy, 1), smem, s>>>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1);
+  launch_dep(k_smooth_tb<ST, NITE>, grid, dim3(kTbW, kTbTy, 1), smem, s, x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1);
 }
 
 // nite pairs of sweeps in one pass (nite in 1..kTbMaxPairs); returns false when the
@@ -900,7 +903,7 @@ static void launch_btb_n(const Op* ops, const int4* tab, long long ntiles, const
   if (win > kTbW * kTbTy) win = kTbW * kTbTy;
   const long long windows = (ntiles + win - 1) / win;
   const long long grid = windows < nsm ? windows : nsm;
-  k_btb<ST, NITE><<<(unsigned)grid, dim3(kTbW, kTbTy, 1), smem, s>>>(ops, tab, ntiles, (int)win, active);
+  launch_dep(k_btb<ST, NITE>, (unsigned)grid, dim3(kTbW, kTbTy, 1), smem, s, ops, tab, ntiles, (int)win, active);
 }
 
 bool launch_btb(int stencil, int nite, const Op* ops, const int4* tab, long long ntiles, const int* active,

@@ -33,6 +33,7 @@ __global__ void __launch_bounds__(kT3dThreads, 1) k_smooth_tb3d(const float* __r
                                                                 const float* __restrict__ w, float cff, int tx, int ty,
                                                                 int tz, int ui0, int ui1, int uj0, int uj1, int uk0,
                                                                 int uk1, int kchunk) {
+  dep_wait();
   constexpr int H = S;
   constexpr int CW = kT3dW - 2 * H, CH = kT3dH - 2 * H;
   extern __shared__ float smem[];
@@ -146,8 +147,7 @@ static void launch_tb3d_s(const float* x, float* xo, const float* b, const float
   const int kchunk = (nk + nchunk - 1) / nchunk;
   nchunk = (nk + kchunk - 1) / kchunk;
   dim3 grid((unsigned)ntx, (unsigned)nty, (unsigned)nchunk);
-  k_smooth_tb3d<S><<<grid, kT3dThreads, smem, st>>>(x, xo, b, w, cff, tx, ty, tz, ui0, ui1, uj0, uj1, uk0, uk1,
-                                                     kchunk);
+  launch_dep(k_smooth_tb3d<S>, grid, kT3dThreads, smem, st, x, xo, b, w, cff, tx, ty, tz, ui0, ui1, uj0, uj1, uk0, uk1, kchunk);
 }
 
 // nite pairs (1 or 2) of 7-point sweeps over the box U in one pass, x -> xo

@@ -122,6 +122,11 @@ extern "C" {
                                    the FP64 solution update x += e * iscale (and collects max |x|)
                                    instead of storing the FP32 correction; 0 a separate kernel. Both give
                                    the same bits. */
+#define CFMG_OPT_DEPENDENT_LAUNCH 7 /* 1 (default): the kernels of a cycle are launched as programmatic
+                                       dependents of the kernel before them, so that a launch overlaps the
+                                       completion of the previous kernel (each kernel waits for its
+                                       predecessor's results before it reads or writes); 0 plain stream
+                                       order. Both give the same bits. */
 
 typedef struct cfmg_desc {
   int kase;     /* CFMG_TWOD / CFMG_THREED            (Param.case) */

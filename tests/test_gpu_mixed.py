@@ -313,3 +313,36 @@ def test_fused_update_replaces_the_update_kernel():
     assert c0 - c1 == n0, (c0, c1, n0)
     assert np.array_equal(h1, h0)
     assert np.array_equal(x1, x0)
+
+
+@pytest.mark.parametrize("name", ["config2_512_vertices_lap9_f", "config1_256_centers_v"])
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_dependent_launch_is_bit_identical(name, precision):
+    """Kernels launched as programmatic dependents of their predecessor
+    (the default) give the plain stream order's history and solution bit
+    for bit, in the graph-launched loop and in the host loop."""
+    base, mkind = CASES[name]
+    out = []
+    for dep, host in ((1, 0), (0, 0), (1, 1)):
+        mg = cfmg.get_gmg(cfmg.Param(**base, tol=1e-10, maxite=40, residual_norm="l2", precision=precision,
+                                     verbose=False))
+        mg.set_option("dependent_launch", dep)
+        mg.set_option("host_loop", host)
+        custom = _mask(base, mg.shape(1), mkind)
+        if custom is not None:
+            mg.oper[1].msk = custom
+            cfmg.setup_operators(mg)
+            for lev in range(1, mg.nlevels + 1):
+                for f in ("x", "y", "r", "b"):
+                    cfmg.set_to_zero(mg, lev, f)
+        msk = mg.download(1, "msk").astype(np.float64)
+        b = np.asfortranarray(np.random.default_rng(21).standard_normal(mg.shape(1))) * msk
+        F.subtract_mean(b, msk)
+        mg.data[1].b = b
+        res, n, hist = cfmg.solve(mg, history=True)
+        out.append((res, n, hist, mg.data[1].x))
+    for o in out[1:]:
+        assert o[1] == out[0][1] and o[0] == out[0][0]
+        assert np.array_equal(o[2], out[0][2])
+        assert np.array_equal(o[3], out[0][3])
+
