@@ -73,6 +73,10 @@ struct cfmg_handle {
   // needs a forward cfmg_solve before it
   bool coef_set = false, solved = false;
   bool dep_launch = true;  // CFMG_OPT_DEPENDENT_LAUNCH
+  // FP32 omega*idiag as one-byte codes (CFMG_OPT_CODED_WIDIAG): wq_on the
+  // option, wq_ok when every level's codes reproduce the floats (prepare_wq)
+  bool wq_on = true, wq_ok = false;
+  float* wtab = nullptr;  // 256 entries
   bool record = false;  // emit() records every Op (whole-solve programs) instead of running it
   bool record_tb = false;  // while recording: temporally blocked smoothing is recorded as OPK_TB Ops
 };
@@ -363,6 +367,10 @@ int sweep(cfmg_handle* h, int lev, int kind, const T* x, T* y, const Box* bx) {
   View<T> v = view<T>(l);
   Op op = mkop(kind, pc<T>(), lev, CFMG_K_SWEEP, l);
   op.x = x; op.y = y; op.b = v.b; op.w = v.widiag; op.cE = v.cE; op.cN = v.cN;
+  if (sizeof(T) == 4 && h->wq_on && h->wq_ok && !h->record) {  // standalone launches only; the engine reads w
+    op.wq = l.wq;
+    op.wtab = h->wtab;
+  }
   op.cff = 1.0 - h->d.omega;
   if (bx) {
     op.box = *bx;
@@ -896,6 +904,31 @@ int prepare_int(cfmg_handle* h) {
   return CFMG_OK;
 }
 
+// The FP32 omega*idiag of each level as one-byte codes into the handle's
+// table, for the standalone FP32 7-point sweeps of 3D levels (bandwidth-
+// bound: 13 instead of 16 bytes per cell, 249 -> 243 us per 512x512x256
+// sweep). The 2D blocked passes keep the floats: they are issue-bound, and
+// the table lookups made configuration 2 slower (14.0 against 13.6 ms).
+// wq_ok only when every cell of every level reproduces its float exactly,
+// so the coded and the streamed forms give the same bits.
+int prepare_wq(cfmg_handle* h) {
+  h->wq_ok = false;
+  if (h->d.op != CFMG_LAPLACIAN && h->d.op != CFMG_LAPLACIAN9) return CFMG_OK;
+  if (!h->wtab) return CFMG_OK;  // not a mixed-precision handle
+  const double Q = h->d.op == CFMG_LAPLACIAN9 ? 4.0 : 1.0;
+  int* ok = (int*)h->partials;  // scratch
+  const int one = 1;
+  CUDA_OK(h, cudaMemcpyAsync(ok, &one, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  launch_wq_table(h->wtab, h->d.omega, Q, h->stream);
+  for (Level& l : h->lv) launch_make_wq(l.diag, l.widiag32, h->wtab, Q, l.wq, (long long)l.len, ok, h->stream);
+  int hok = 0;
+  CUDA_OK(h, cudaMemcpyAsync(&hok, ok, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_OK(h, cudaStreamSynchronize(h->stream));
+  LAUNCH_OK(h);
+  h->wq_ok = hok != 0;
+  return CFMG_OK;
+}
+
 int prepare_mixed(cfmg_handle* h) {
   if (!h->mixed_dirty) return CFMG_OK;
   for (Level& l : h->lv) {
@@ -908,6 +941,7 @@ int prepare_mixed(cfmg_handle* h) {
       launch_to_f32(l.cN, l.cN32, l.len, h->stream);
     }
   }
+  TRY(prepare_wq(h));
   // number of wet cells of level 1 (for the residual scaling)
   const Level& l1 = h->lv[0];
   launch_fill_f64(l1.y, 1.0, l1.len, h->stream);
@@ -1470,6 +1504,8 @@ static int create_handle(const cfmg_desc* d, cudaStream_t shared, cfmg_handle** 
   // arena: all level arrays, 256-byte aligned
   const bool mixed = d->precision == CFMG_MIXED;
   const bool vc = d->op == CFMG_VARCOEF;
+  // coded omega*idiag: the 3D 7-point operator's standalone FP32 sweeps
+  const bool coded = mixed && d->kase == CFMG_THREED && d->op == CFMG_LAPLACIAN;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   size_t total = al(kPartials * sizeof(double)) + al(S_COUNT * sizeof(double)) + al((size_t)pool_ops * sizeof(Op));
   for (const Level& l : h->lv) {
@@ -1479,7 +1515,9 @@ static int create_handle(const cfmg_desc* d, cudaStream_t shared, cfmg_handle** 
     total += (vc ? 3 : 0) * al(n * 8);        // kappa cE cN
     total += (mixed ? 8 : 0) * al(n * 4);     // x32 y32 r32 b32 widiag32 diag32 Rcoef32 Pcoef32
     total += (mixed && vc ? 2 : 0) * al(n * 4);
+    total += coded ? al(n) : 0;               // wq
   }
+  total += coded ? al(256 * sizeof(float)) : 0;  // wtab
   if (cudaMalloc(&h->arena, total) != cudaSuccess) {
     cudaGetLastError();
     delete h;
@@ -1509,7 +1547,9 @@ static int create_handle(const cfmg_desc* d, cudaStream_t shared, cfmg_handle** 
       l.Rcoef32 = (float*)take(n * 4); l.Pcoef32 = (float*)take(n * 4);
       if (vc) { l.cE32 = (float*)take(n * 4); l.cN32 = (float*)take(n * 4); }
     }
+    if (coded) l.wq = (uint8_t*)take(n);
   }
+  if (coded) h->wtab = (float*)take(256 * sizeof(float));
   // the fixed-point residual pass reads kResidIntReach elements beside level
   // 1's x (values it never uses): the arena holds the device scalars in front
   // of it and level 1's y behind it
@@ -2536,6 +2576,11 @@ int cfmg_set_option(cfmg_handle* h, int option, long long value) {
   }
   if (option == CFMG_OPT_FUSED_UPDATE) {
     h->upd_on = value != 0;
+    drop_graphs(h);
+    return CFMG_OK;
+  }
+  if (option == CFMG_OPT_CODED_WIDIAG) {
+    h->wq_on = value != 0;
     drop_graphs(h);
     return CFMG_OK;
   }

@@ -61,6 +61,9 @@ struct Level {
   uint8_t* msk;
   // mixed precision copies (used by CFMG_MIXED)
   float *x32, *y32, *r32, *b32, *widiag32, *diag32, *Rcoef32, *Pcoef32, *cE32, *cN32;
+  // 3D 7-point mixed form: the FP32 omega*idiag as a one-byte code c = diag
+  // (0: omega*idiag = 0) into the handle's table wtab (prepare_wq, cfmg_api.cu)
+  uint8_t* wq;
   int xswap;  // 1: the FP32 x currently lives in y32 (after a temporally blocked smoothing)
   int ic0, ic1, jc0, jc1, kc0, kc1;  // interior box (1-based inclusive)
 };
@@ -90,6 +93,9 @@ template <class T>
 void launch_sweep5_2d(const T* x, T* y, const T* b, const T* widiag, T cff, const Geom& g, cudaStream_t s);
 template <class T>
 void launch_sweep7_3d(const T* x, T* y, const T* b, const T* widiag, T cff, const Geom& g, cudaStream_t s);
+// the same FP32 7-point sweep with omega*idiag read as wtab[wq[I]]
+void launch_sweep7_3d_q(const float* x, float* y, const float* b, const uint8_t* wq, const float* wtab, float cff,
+                        const Geom& g, cudaStream_t s);
 template <class T>
 void launch_sweep9_2d(const T* x, T* y, const T* b, const T* widiag, T cff, const Geom& g, const Box& bx,
                       cudaStream_t s);
@@ -188,6 +194,9 @@ struct Op {
   int s0, s1, s2, maxite, norm_kind;
   int inst;  // batched solver: the instance the Op belongs to
   int assign;  // standalone prolongation onto a fine x known to be +0: written, not read
+  // standalone FP32 sweeps: omega*idiag read as wtab[wq[I]] instead of w[I] (same bits)
+  const uint8_t* wq;
+  const float* wtab;
 };
 // scalar block of a whole-solve program
 enum SolveSlot { SS_NORMB = 0, SS_NR, SS_RES, SS_NITE, SS_NWET, SS_MEAN, SS_SCALE, SS_ISCALE, SS_T0, SS_T1,
@@ -370,5 +379,11 @@ void launch_restrict_kappa(const double* kf, const uint8_t* mf, double* kc, cons
 void launch_face_coef(const double* kappa, const uint8_t* msk, double* cE, double* cN, const Geom& g,
                       cudaStream_t s);
 void launch_to_f32(const double* a, float* out, size_t n, cudaStream_t s);
+// the omega*idiag code table: tab[c] = (float)(omega * (1 / (c / Q))) for c = 1..255, tab[0] = 0,
+// with the FP64 operations of k_diag and k_widiag; then the codes of one level (ok cleared when
+// a cell's diag is not c/Q or its FP32 omega*idiag differs from tab[c] in any bit)
+void launch_wq_table(float* tab, double omega, double Q, cudaStream_t s);
+void launch_make_wq(const double* diag, const float* w32, const float* tab, double Q, uint8_t* wq, long long n,
+                    int* ok, cudaStream_t s);
 
 }  // namespace cfmg

@@ -245,6 +245,45 @@ void launch_sweep7_3d(const T* x, T* y, const T* b, const T* w, T cff, const Geo
   if (hi <= lo) return;
   launch_dep(k_sweep7_3d<T>, nblocks(hi - lo), kThreads, 0, s, x, y, b, w, cff, g.n1, g.n2, lo, hi);
 }
+// The FP32 7-point sweep of a 3D level (the linear range n2 .. len-n2 of
+// sloop3d_v1!, src/laplacian.jl:11-20: every (i, j) of the planes k = 2 ..
+// tz-1), register-blocked along k: a thread owns one (i, j) column and a
+// run of kKRun planes, carries x at k-1, k and k+1 in registers from one
+// plane to the next, and takes the four in-plane neighbours from L1 (the
+// block covers 32 x 8 columns). omega*idiag is read as a one-byte code into
+// a 256-entry table (L1-resident): 13 instead of 16 bytes of traffic per
+// cell. The per-cell arithmetic and its order are k_sweep7_3d<float>'s
+// (faces6, then cff*x - w*(b - faces)), so the bits are the same.
+constexpr int kKRun = 8;
+__global__ void __launch_bounds__(256) k_sweep7_3d_q(const float* __restrict__ x, float* __restrict__ y,
+                                                     const float* __restrict__ b, const uint8_t* __restrict__ wq,
+                                                     const float* __restrict__ wtab, float cff, int tx, int ty,
+                                                     int tz) {
+  dep_wait();
+  const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+  const int k0 = 1 + blockIdx.z * kKRun;  // 0-based planes k0 .. k1-1 of 1 .. tz-2
+  if (i >= tx || j >= ty || k0 > tz - 2) return;
+  const int k1 = min(k0 + kKRun, tz - 1);
+  typedef Ar<float> A;
+  const long long n1 = tx, n2 = (long long)tx * ty;
+  long long I = (long long)i + n1 * j + n2 * k0;
+  float xm = x[I - n2], xc = x[I];
+  for (int k = k0; k < k1; ++k, I += n2) {
+    const float xp = x[I + n2];
+    const float f = A::add(A::add(A::add(A::add(A::add(x[I - 1], x[I + 1]), x[I - n1]), x[I + n1]), xm), xp);
+    const float w = __ldg(wtab + wq[I]);
+    y[I] = A::sub(A::mul(cff, xc), A::mul(w, A::sub(b[I], f)));
+    xm = xc;
+    xc = xp;
+  }
+}
+void launch_sweep7_3d_q(const float* x, float* y, const float* b, const uint8_t* wq, const float* wtab, float cff,
+                        const Geom& g, cudaStream_t s) {
+  if (g.tz < 3) return;
+  const dim3 grid((unsigned)((g.tx + 31) / 32), (unsigned)((g.ty + 7) / 8), (unsigned)((g.tz - 2 + kKRun - 1) / kKRun));
+  launch_dep(k_sweep7_3d_q, grid, dim3(32, 8, 1), 0, s, x, y, b, wq, wtab, cff, g.tx, g.ty, g.tz);
+}
+
 template <class T>
 void launch_sweep9_2d(const T* x, T* y, const T* b, const T* w, T cff, const Geom& g, const Box& bx,
                       cudaStream_t s) {
@@ -399,7 +438,12 @@ static void launch_op_t(const Op& op, cudaStream_t s) {
   const T cff = (T)op.cff;
   switch (op.kind) {
     case OPK_SWEEP5: launch_sweep5_2d<T>(x, y, b, w, cff, op.g, s); break;
-    case OPK_SWEEP7: launch_sweep7_3d<T>(x, y, b, w, cff, op.g, s); break;
+    case OPK_SWEEP7:
+      if (sizeof(T) == 4 && op.wq)
+        launch_sweep7_3d_q((const float*)x, (float*)y, (const float*)b, op.wq, op.wtab, (float)cff, op.g, s);
+      else
+        launch_sweep7_3d<T>(x, y, b, w, cff, op.g, s);
+      break;
     case OPK_SWEEP9: launch_sweep9_2d<T>(x, y, b, w, cff, op.g, op.box, s); break;
     case OPK_SWEEP19: launch_sweep19_3d<T>(x, y, b, w, cff, op.g, op.box, s); break;
     case OPK_SWEEPVC: launch_sweep_vc_2d<T>(x, y, b, w, (const T*)op.cE, (const T*)op.cN, cff, op.g, s); break;

@@ -183,4 +183,41 @@ void launch_to_f32(const double* a, float* out, size_t n, cudaStream_t s) {
   launch_dep(k_to_f32, nb(n), kT, 0, s, a, out, (long long)n);
 }
 
+// The FP32 omega*idiag of every cell of the 5-, 7-, 9- and 19-point
+// operators is a function of diag alone (k_diag, k_widiag), and diag is a
+// multiple of 1/Q (Q = 1 for the 5- and 7-point operators, whose weights are
+// 1; Q = 4 for the weights 1/2 and 1/4), so a one-byte code c = Q*diag and a
+// table of 256 floats reproduce it: the table entries are computed with the
+// same FP64 operations on the same exact diag = c/Q.
+__global__ void k_wq_table(float* tab, double omega, double Q) {
+  dep_wait();
+  const int c = threadIdx.x;
+  const double d = (double)c / Q;  // exact: c < 256 and Q a power of two
+  const double id = (d > 0.0) ? __ddiv_rn(1.0, d) : 0.0;
+  tab[c] = (float)__dmul_rn(omega, id);
+}
+void launch_wq_table(float* tab, double omega, double Q, cudaStream_t s) {
+  launch_dep(k_wq_table, 1, 256, 0, s, tab, omega, Q);
+}
+
+__global__ void k_make_wq(const double* __restrict__ diag, const float* __restrict__ w32, const float* __restrict__ tab,
+                          double Q, uint8_t* wq, long long n, int* ok) {
+  dep_wait();
+  const long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= n) return;
+  const double d = diag[I];
+  unsigned c = 0;
+  if (d > 0.0) {
+    const double qd = d * Q;
+    if (qd >= 1.0 && qd <= 255.0 && qd == floor(qd)) c = (unsigned)qd;
+    else atomicAnd(ok, 0);
+  }
+  if (__float_as_uint(tab[c]) != __float_as_uint(w32[I])) atomicAnd(ok, 0);
+  wq[I] = (uint8_t)c;
+}
+void launch_make_wq(const double* diag, const float* w32, const float* tab, double Q, uint8_t* wq, long long n,
+                    int* ok, cudaStream_t s) {
+  launch_dep(k_make_wq, nb(n), kT, 0, s, diag, w32, tab, Q, wq, n, ok);
+}
+
 }  // namespace cfmg

@@ -127,6 +127,10 @@ extern "C" {
                                        completion of the previous kernel (each kernel waits for its
                                        predecessor's results before it reads or writes); 0 plain stream
                                        order. Both give the same bits. */
+#define CFMG_OPT_CODED_WIDIAG 8 /* mixed form, 3D 7-point operator: 1 (default) the standalone FP32 sweeps
+                                   read omega*idiag as a one-byte code diag into a 256-entry table (when
+                                   every cell's code reproduces its float exactly) instead of a 4-byte
+                                   float per cell; 0 the floats. Both give the same bits. */
 
 typedef struct cfmg_desc {
   int kase;     /* CFMG_TWOD / CFMG_THREED            (Param.case) */

@@ -346,3 +346,32 @@ def test_dependent_launch_is_bit_identical(name, precision):
         assert np.array_equal(o[2], out[0][2])
         assert np.array_equal(o[3], out[0][3])
 
+
+
+@pytest.mark.parametrize("name", ["3d_48_centers_v", "3d_32_vertices_v"])
+def test_coded_widiag_is_bit_identical(name):
+    """The 3D 7-point FP32 sweeps reading omega*idiag as a one-byte code into
+    a table (the default where every cell's code reproduces its float) give
+    the streamed floats' history and solution bit for bit."""
+    base, mkind = CASES[name]
+    out = []
+    for coded in (1, 0):
+        mg = cfmg.get_gmg(cfmg.Param(**base, tol=1e-10, maxite=40, residual_norm="l2", precision="mixed",
+                                     verbose=False))
+        mg.set_option("engine_cells", 2000)  # fine levels as standalone kernels
+        mg.set_option("coded_widiag", coded)
+        custom = _mask(base, mg.shape(1), mkind)
+        if custom is not None:
+            mg.oper[1].msk = custom
+            cfmg.setup_operators(mg)
+            for lev in range(1, mg.nlevels + 1):
+                for f in ("x", "y", "r", "b"):
+                    cfmg.set_to_zero(mg, lev, f)
+        msk = mg.download(1, "msk").astype(np.float64)
+        b = np.asfortranarray(np.random.default_rng(23).standard_normal(mg.shape(1))) * msk
+        F.subtract_mean(b, msk)
+        mg.data[1].b = b
+        res, n, hist = cfmg.solve(mg, history=True)
+        out.append((res, n, hist, mg.data[1].x))
+    assert out[0][1] == out[1][1] and out[0][0] == out[1][0]
+    assert np.array_equal(out[0][2], out[1][2]) and np.array_equal(out[0][3], out[1][3])
