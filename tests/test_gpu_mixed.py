@@ -30,6 +30,9 @@ CASES = {
                                    operator="laplacian9", cycle="v", npre=2, npost=2, omega=0.8), None),
     "2d_xperio_vertices_v": (dict(nx=64, ny=64, nz=1, case="twod", location="vertices", topology="xperio",
                                   cycle="v", npre=2, npost=2, omega=0.9, ndeepest=60), None),
+    # ragged 3D: plane and column counts that are no multiple of the sweeps' blocks
+    "3d_40x36x26_centers_f": (dict(nx=40, ny=36, nz=26, case="threed", cycle="f", npre=2, npost=2, omega=0.8,
+                                   nlevels=3), None),
 }
 
 
@@ -348,7 +351,7 @@ def test_dependent_launch_is_bit_identical(name, precision):
 
 
 
-@pytest.mark.parametrize("name", ["3d_48_centers_v", "3d_32_vertices_v"])
+@pytest.mark.parametrize("name", ["3d_48_centers_v", "3d_32_vertices_v", "3d_40x36x26_centers_f"])
 def test_coded_widiag_is_bit_identical(name):
     """The 3D 7-point FP32 sweeps reading omega*idiag as a one-byte code into
     a table (the default where every cell's code reproduces its float) give
@@ -373,5 +376,6 @@ def test_coded_widiag_is_bit_identical(name):
         mg.data[1].b = b
         res, n, hist = cfmg.solve(mg, history=True)
         out.append((res, n, hist, mg.data[1].x))
+    assert out[0][0] <= 1e-10
     assert out[0][1] == out[1][1] and out[0][0] == out[1][0]
     assert np.array_equal(out[0][2], out[1][2]) and np.array_equal(out[0][3], out[1][3])
