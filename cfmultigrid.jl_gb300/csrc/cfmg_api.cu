@@ -67,6 +67,10 @@ struct cfmg_handle {
   int8_t* dq = nullptr;
   bool int_ok = false;
   bool int_on = true;
+  // 3D 7-point: dq with rows padded to 16 bytes for the TMA-staged pass
+  // (k_resid3d.cu, CFMG_OPT_STAGED_RESIDUAL); r3_ran once that pass ran
+  int8_t* dqp = nullptr;
+  bool r3_on = true, r3_ran = false;
   bool host_loop = false;  // CFMG_OPT_HOST_LOOP
   // call order: the operators' coefficients exist once cfmg_setup_operators,
   // cfmg_bind_level or an upload of a coefficient field ran; cfmg_adjoint
@@ -897,6 +901,11 @@ int prepare_int(cfmg_handle* h) {
   const int one = 1;
   CUDA_OK(h, cudaMemcpyAsync(ok, &one, sizeof(int), cudaMemcpyHostToDevice, h->stream));
   launch_make_dq(l1.diag, l1.msk, kind == OPK_RESID9 ? 4.0 : 1.0, h->dq, (long long)l1.len, ok, h->stream);
+  if (kind == OPK_RESID7) {
+    const int txp = dq_pitch(l1.tx);
+    if (!h->dqp) CUDA_OK(h, cudaMalloc((void**)&h->dqp, (size_t)txp * l1.ty * l1.tz));
+    launch_pad_dq(h->dq, h->dqp, l1.tx, txp, (long long)l1.ty * l1.tz, h->stream);
+  }
   int hok = 0;
   CUDA_OK(h, cudaMemcpyAsync(&hok, ok, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   CUDA_OK(h, cudaStreamSynchronize(h->stream));
@@ -1111,8 +1120,12 @@ int fused_residual(cfmg_handle* h) {
       // the F-cycle restricts level 1's r first: it must hold the right-hand side too
       Launch k(h, CFMG_K_RESIDUAL, 1, CFMG_FP64, 2);
       float* r32 = h->d.cycle == CFMG_CYCLE_F ? l1.r32 : nullptr;
-      if (!launch_resid_int2d(kind, l1.x, l1.b, h->dq, g, bx, h->dscal, l1.b32, r32, neumann, h->partials,
-                              h->stream))
+      const bool r3 = kind == OPK_RESID7 && h->r3_on &&
+                      launch_resid_int3d(l1.x, l1.b, h->dqp, g, bx, h->dscal, l1.b32, r32, neumann, h->partials,
+                                         h->stream);
+      h->r3_ran |= r3;
+      if (!r3 && !launch_resid_int2d(kind, l1.x, l1.b, h->dq, g, bx, h->dscal, l1.b32, r32, neumann, h->partials,
+                                     h->stream))
         launch_resid_int(kind, l1.x, l1.b, h->dq, g, bx, lo, n, h->dscal, l1.b32, r32, neumann, h->partials,
                          h->stream);
       launch_fused_final(h->partials, h->dscal, h->dscal + S_NORMB, neumann ? h->dscal + S_NWET : nullptr,
@@ -1598,6 +1611,7 @@ int cfmg_destroy(cfmg_handle* h) {
   for (double* p : {h->adj_x, h->adj_b, h->adj_gk})
     if (p) cudaFree(p);
   if (h->dq) cudaFree(h->dq);
+  if (h->dqp) cudaFree(h->dqp);
   if (h->dhist) cudaFree(h->dhist);
   if (h->arena) cudaFree(h->arena);
   if (h->hscal) cudaFreeHost(h->hscal);
@@ -1823,7 +1837,20 @@ int cfmg_cycle(cfmg_handle* h, int kind) {
 
 // A NaN or Inf in b, or a residual that is not finite, ends the solve and
 // makes it return CFMG_ERR_NONFINITE, with res and nite filled in.
+// A bounded wait of the staged 3D residual pass (k_resid3d.cu) ran out: the
+// pass set S_FAULT and NaN partial sums, which stopped the loop.
+int fault_check(cfmg_handle* h) {
+  if (!h->r3_ran) return CFMG_OK;
+  double f = 0.0;
+  CUDA_OK(h, cudaMemcpyAsync(&f, h->dscal + S_FAULT, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  if (f == 0.0) return CFMG_OK;
+  CUDA_OK(h, cudaMemsetAsync(h->dscal + S_FAULT, 0, sizeof(double), h->stream));
+  return fail(h, CFMG_ERR_CUDA, "a wait for a TMA copy in the staged 3D residual pass ran out (1 s)");
+}
+
 int nonfinite_check(cfmg_handle* h, double normb, double res) {
+  TRY(fault_check(h));
   if (std::isfinite(normb) && std::isfinite(res)) return CFMG_OK;
   return fail(h, CFMG_ERR_NONFINITE,
               std::string("non-finite ") + (std::isfinite(normb) ? "residual norm" : "norm of b") +
@@ -2576,6 +2603,11 @@ int cfmg_set_option(cfmg_handle* h, int option, long long value) {
   }
   if (option == CFMG_OPT_FUSED_UPDATE) {
     h->upd_on = value != 0;
+    drop_graphs(h);
+    return CFMG_OK;
+  }
+  if (option == CFMG_OPT_STAGED_RESIDUAL) {
+    h->r3_on = value != 0;
     drop_graphs(h);
     return CFMG_OK;
   }

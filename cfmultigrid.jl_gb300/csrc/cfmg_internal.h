@@ -145,6 +145,11 @@ constexpr int kNormParts = 1024;
 // the handle's partial-sum scratch: two sums per block for the fused
 // residual pass of the mixed loop (k_mixed.cu), one for the norms
 constexpr int kPartials = 2 * kNormParts;
+// the fused residual passes of the mixed loop (k_mixed.cu, k_resid3d.cu):
+// threads per block, and at most kMxParts blocks with two partial sums each
+constexpr int kMxThreads = 256;
+constexpr int kMxParts = 1024;
+static_assert(2 * kMxParts <= kPartials, "the fused pass writes 2*kMxParts partial sums");
 
 // ---- operator descriptors and the coarse-level program engine (k_coarse.cu)
 // One Op describes one launch-worth of work on one level: its kind, the
@@ -327,7 +332,9 @@ void launch_bcond(cudaGraphConditionalHandle hc, int* nactive, cudaStream_t s);
 // device scalars of a handle (dscal[])
 enum Scal { S_NORM = 0, S_RES = 1, S_NORMB = 2, S_NWET = 3, S_SCALE = 4, S_MEAN = 5, S_TMP0 = 6, S_ISCALE = 7,
             S_NEXT = 8, S_CUR = 9, S_ICUR = 10, S_MEAN2 = 11, S_MAXX = 12, S_MAXB = 13, S_NITE = 14,
-            S_SHIFT = 15, S_MAXO = 16, S_COUNT = 17 };
+            S_SHIFT = 15, S_MAXO = 16,
+            // 1 after a bounded wait in a kernel ran out (k_resid3d.cu); the solve reports it
+            S_FAULT = 17, S_COUNT = 18 };
 
 // fused FP64 steps of the mixed loop (k_mixed.cu)
 void launch_resid_fused(int kind, double* r, const double* x, const double* b, const double* d, const uint8_t* m,
@@ -351,6 +358,13 @@ void launch_resid_int(int kind, const double* x, const double* b, const int8_t* 
 constexpr int kResidIntReach = 32;
 bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t* dq, const Geom& g, const Box& bx,
                         const double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s);
+// 3D 7-point form with TMA-staged planes (k_resid3d.cu). dqp: dq with rows
+// padded to txp = dq_pitch(tx) bytes (launch_pad_dq). false: not applicable
+// (odd tx, misaligned arrays, no tensor-map encoder): use launch_resid_int2d.
+int dq_pitch(int tx);
+void launch_pad_dq(const int8_t* dq, int8_t* dqp, int tx, int txp, long long rows, cudaStream_t s);
+bool launch_resid_int3d(const double* x, const double* b, const int8_t* dqp, const Geom& g, const Box& bx,
+                        double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s);
 void launch_rhs32_shift(const uint8_t* m, const double* mean_scale, float* b32, float* r32, long long n,
                         cudaStream_t s);
 void launch_make_dq(const double* diag, const uint8_t* m, double Q, int8_t* dq, long long n, int* ok, cudaStream_t s);

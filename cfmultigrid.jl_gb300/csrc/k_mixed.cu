@@ -16,9 +16,6 @@
 
 namespace cfmg {
 
-constexpr int kMxThreads = 256;
-constexpr int kMxParts = 1024;  // blocks of the fused pass; two sums each
-static_assert(2 * kMxParts <= kPartials, "the fused pass writes 2*kMxParts partial sums");
 
 // per-block partial sums -> 2 * kMxParts doubles: [sum r^2 | sum r]. With
 // NEUMANN the FP64 r is kept for the mean-removing pass and sum r is
@@ -168,13 +165,6 @@ __global__ void k_update_scaled(double* __restrict__ x, const float* __restrict_
 // in 128-bit integers per thread.
 //
 // dq[I] = Q*diag[I] (an integer in 0..127) on wet cells, -128 on dry ones.
-
-__device__ __forceinline__ int fix_exponent(const double* ds) {
-  const double mx = fmax(ds[S_MAXX], ds[S_MAXB]);
-  int e = 0;
-  if (mx > 0 && isfinite(mx)) frexp(mx, &e);  // mx < 2^e
-  return 58 - e;
-}
 
 template <int KIND>
 __device__ __forceinline__ long long fix_resid(const double* __restrict__ x, const double* __restrict__ b, int dq,

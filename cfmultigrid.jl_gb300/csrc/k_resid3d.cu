@@ -1,0 +1,396 @@
+// Fixed-point level-1 residual of the 3D 7-point operator (rloop3d! over
+// the interior box, src/laplacian.jl:44-64, in the integer form of the mixed
+// loop's fused pass) with TMA-staged planes.
+//
+// The strip form (k_resid_int2d, k_mixed.cu) walks the rows of a plane and
+// loads the x of the planes below and above each row separately: every x is
+// read three times and converted three times, and its warps, waiting on
+// those loads with few bytes in flight, ran at 2.3 TB/s. Here a block owns a
+// 32 x 8 column tile of the interior box and marches along k through a run
+// of kt planes. One thread issues each plane's loads as TMA copies
+// (cp.async.bulk.tensor) into a ring of kR3Stages shared-memory stages that
+// complete on mbarriers: x with a one-cell halo in i and j (a 36 x 10 box of
+// doubles starting on an even column), b (34 x 8 doubles) and dq (48 x 8
+// bytes from a copy whose rows are padded to a multiple of 16 bytes). The
+// threads convert each x of a plane once (their own cell, and one halo cell
+// for 84 of them) into a ring of three converted planes; the residual at
+// plane k takes its four in-plane neighbours from converted plane k and its
+// k -/+ 1 neighbours from the thread's registers. The loads of the next
+// kR3Stages - 1 planes are in flight while a plane is computed, without
+// registers held for them, and every x comes from DRAM about once.
+//
+// Per cell the arithmetic is the strip form's: the same exact integer R, the
+// same FP32 right-hand side f = R * 2^-(k+q) * scale, sum f^2 in double-float
+// per thread and the exact sum R in 128 bits. Only the order in which the
+// per-thread sums are combined differs.
+//
+// Every wait on an mbarrier is bounded (one second of %globaltimer). A block
+// whose wait runs out waits (bounded again) for its copies in flight, writes
+// NaN into its partial sums, so that the solve loop stops on a non-finite
+// residual, and 1 into ds[S_FAULT], which the solve reports.
+#include <cuda.h>
+
+#include <mutex>
+
+#include "cfmg_internal.h"
+#include "ops_dev.cuh"
+
+namespace cfmg {
+namespace {
+
+constexpr int kR3TI = 32, kR3TJ = 8;          // column tile: 32 cells in i, 8 in j (one per thread)
+constexpr int kR3Stages = 4;                  // planes in the TMA ring
+constexpr int kR3XW = 36, kR3XH = 10;         // x box (halo of one cell, even first column)
+constexpr int kR3BW = 34;                     // b box (even first column)
+constexpr int kR3DW = 48;                     // dq box (first column a multiple of 16)
+constexpr int kR3PW = 34, kR3PH = 10;         // converted plane: tile + halo
+constexpr int kR3Halo = 2 * kR3PW + 2 * kR3TJ;  // 84 halo cells
+constexpr int kR3XBytes = kR3XW * kR3XH * 8;  // 2880
+constexpr int kR3BBytes = kR3BW * kR3TJ * 8;  // 2176
+constexpr int kR3DBytes = kR3DW * kR3TJ;      // 384
+constexpr int kR3XSlot = 2944;                // x box rounded up to 128 bytes
+constexpr int kR3StageBytes = kR3XSlot + kR3BBytes + kR3DBytes;  // 5504
+constexpr int kR3PBytes = kR3PW * kR3PH * 8;
+constexpr int kR3Smem = kR3Stages * kR3StageBytes + 3 * kR3PBytes + kR3Stages * 8;
+static_assert(kR3TI * kR3TJ == kMxThreads, "one thread per cell of the tile");
+static_assert(kR3Halo <= kMxThreads, "a halo cell per thread at most");
+static_assert(kR3XSlot >= kR3XBytes && kR3XSlot % 128 == 0 && kR3BBytes % 128 == 0 && kR3DBytes % 128 == 0,
+              "TMA destinations on 128-byte boundaries");
+
+struct R3Space {
+  int c0, r0, p0;    // 0-based column, row and plane of the box's first cell
+  int ni, nj, nk;    // box extent
+  int nti, ntj;      // column tiles in i and j
+  int kt, nkc;       // planes per task, runs of planes along k
+  long long n1, n2;  // strides of b32 and r32 (elements)
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool mbar_try(unsigned bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// false when the phase has not completed within one second
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+  if (mbar_try(bar, parity)) return true;
+  const unsigned long long t0 = globaltimer();
+  while (!mbar_try(bar, parity))
+    if (globaltimer() - t0 > 1000000000ULL) return false;
+  return true;
+}
+
+__device__ __forceinline__ void tma3(unsigned dst, const CUtensorMap* map, int c, int r, int p, unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];"
+      :
+      : "r"(dst), "l"(reinterpret_cast<unsigned long long>(map)), "r"(c), "r"(r), "r"(p), "r"(bar)
+      : "memory");
+}
+
+struct R3Task {
+  int c0t, r0t, ka, np;  // first column and row of the tile, first plane, planes streamed (kt + 2 at most)
+};
+__device__ __forceinline__ R3Task r3_task(const R3Space& sp, int T) {
+  R3Task t;
+  const int tI = T % sp.nti, rest = T / sp.nti;
+  const int tJ = rest % sp.ntj, kc = rest / sp.ntj;
+  t.c0t = sp.c0 + kR3TI * tI;
+  t.r0t = sp.r0 + kR3TJ * tJ;
+  t.ka = sp.p0 + kc * sp.kt;
+  const int kb = min(t.ka + sp.kt, sp.p0 + sp.nk);
+  t.np = kb - t.ka + 2;  // planes ka-1 .. kb
+  return t;
+}
+
+template <bool NEUMANN>
+__global__ void __launch_bounds__(kMxThreads) k_resid_int3d(const __grid_constant__ CUtensorMap mx,
+                                                            const __grid_constant__ CUtensorMap mb,
+                                                            const __grid_constant__ CUtensorMap md, R3Space sp,
+                                                            double* ds, float* __restrict__ b32,
+                                                            float* __restrict__ r32, double* __restrict__ partials) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  long long* pring = reinterpret_cast<long long*>(smem + kR3Stages * kR3StageBytes);
+  unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + kR3Stages * kR3StageBytes + 3 * kR3PBytes);
+  const int tid = threadIdx.x, ti = tid & 31, tj = tid >> 5;
+  if (tid == 0) {
+    for (int s = 0; s < kR3Stages; ++s)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bars + s)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<unsigned long long>(&mx)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<unsigned long long>(&mb)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<unsigned long long>(&md)) : "memory");
+  }
+  __syncthreads();
+  dep_wait();  // x and b are the predecessor's output
+  constexpr int q = 0;  // Q = 1 for the 7-point weights
+  const int k = fix_exponent(ds);
+  const double scale = ds[S_NEXT];
+  const float fm = (float)ldexp(scale, -(k + q));  // power of two: R -> r * scale
+  const int ntasks = sp.nti * sp.ntj * sp.nkc;
+
+  // issue cursor (thread 0): the block's sequence of (task, plane) in order
+  int iT = blockIdx.x, iq = 0;
+  unsigned long long in = 0;
+  R3Task it = r3_task(sp, iT);
+  auto issue_next = [&]() {
+    if (iT >= ntasks) return;
+    const int s = (int)(in % kR3Stages);
+    const unsigned bar = smem_u32(bars + s);
+    unsigned char* st = smem + s * kR3StageBytes;
+    const bool full = iq >= 1 && iq <= it.np - 2;  // b and dq for planes ka .. kb-1 only
+    const unsigned bytes = kR3XBytes + (full ? kR3BBytes + kR3DBytes : 0);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    const int p = it.ka - 1 + iq;
+    tma3(smem_u32(st), &mx, (it.c0t - 1) & ~1, it.r0t - 1, p, bar);
+    if (full) {
+      tma3(smem_u32(st + kR3XSlot), &mb, it.c0t & ~1, it.r0t, p, bar);
+      tma3(smem_u32(st + kR3XSlot + kR3BBytes), &md, it.c0t & ~15, it.r0t, p, bar);
+    }
+    ++in;
+    if (++iq == it.np) {
+      iT += gridDim.x;
+      iq = 0;
+      if (iT < ntasks) it = r3_task(sp, iT);
+    }
+  };
+  if (tid == 0)
+    for (int s = 0; s < kR3Stages; ++s) issue_next();
+
+  // this thread's halo cell (tid < 84): its place in the converted plane
+  int hp = -1, hx = 0;  // index in the converted plane, and in the x box without the column offset
+  if (tid < kR3Halo) {
+    int hr, hc;
+    if (tid < kR3PW) {
+      hr = 0;
+      hc = tid;
+    } else if (tid < 2 * kR3PW) {
+      hr = kR3PH - 1;
+      hc = tid - kR3PW;
+    } else {
+      const int h = tid - 2 * kR3PW;
+      hr = 1 + (h >> 1);
+      hc = (h & 1) ? kR3PW - 1 : 0;
+    }
+    hp = hr * kR3PW + hc;
+    hx = hr * kR3XW + hc;
+  }
+  const int op = (tj + 1) * kR3PW + ti + 1;  // own cell in the converted plane
+  float hi = 0.f, lo = 0.f;                  // double-float sum of f^2
+  __int128 s1 = 0;
+  unsigned long long n = 0;  // planes consumed
+  bool fault = false;
+  for (int T = blockIdx.x; T < ntasks && !fault; T += gridDim.x) {
+    const R3Task t = r3_task(sp, T);
+    const int ox = (t.c0t - 1) - ((t.c0t - 1) & ~1), ob = t.c0t - (t.c0t & ~1), od = t.c0t - (t.c0t & ~15);
+    const int col = t.c0t + ti, row = t.r0t + tj;
+    const bool own = col < sp.c0 + sp.ni && row < sp.r0 + sp.nj;
+    long long Cm = 0, Cc = 0, Bp = 0;
+    int dp = -1;
+    for (int qq = 0; qq < t.np; ++qq, ++n) {
+      const int s = (int)(n % kR3Stages);
+      const bool ok = mbar_wait(smem_u32(bars + s), (unsigned)((n / kR3Stages) & 1));
+      const unsigned char* st = smem + s * kR3StageBytes;
+      const double* xs = reinterpret_cast<const double*>(st);
+      long long* P = pring + (qq % 3) * (kR3PW * kR3PH);
+      const long long Cn = to_fix(xs[(tj + 1) * kR3XW + ti + 1 + ox], k);
+      P[op] = Cn;
+      if (hp >= 0) P[hp] = to_fix(xs[hx + ox], k);
+      long long Bn = 0;
+      int dn = -1;
+      if (qq >= 1 && qq <= t.np - 2) {
+        Bn = to_fix(reinterpret_cast<const double*>(st + kR3XSlot)[tj * kR3BW + ti + ob], k);
+        dn = (int)reinterpret_cast<const signed char*>(st + kR3XSlot + kR3BBytes)[tj * kR3DW + ti + od];
+      }
+      // the plane is converted and its stage free again; one thread refills it
+      if (__syncthreads_or(!ok)) {
+        fault = true;
+        break;
+      }
+      if (tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue_next();
+      }
+      if (qq >= 2) {  // plane m = ka + qq - 2 from converted plane m and own C(m-1), C(m), C(m+1)
+        const long long* Pc = pring + ((qq - 1) % 3) * (kR3PW * kR3PH);
+        long long R = (long long)dp * Cc + Bp -
+                      (Pc[op - 1] + Pc[op + 1] + Pc[op - kR3PW] + Pc[op + kR3PW] + Cm + Cn);
+        R = (own && dp >= 0) ? R : 0LL;  // dry cells and cells outside the box
+        const float f = __fmul_rn(__ll2float_rn(R), fm);
+        if (own) {
+          const long long I = (long long)col + sp.n1 * row + sp.n2 * (t.ka + qq - 2);
+          b32[I] = f;
+          if (!NEUMANN && r32) r32[I] = f;
+        }
+        if (NEUMANN) s1 += (__int128)R;
+        // p + e = f^2 exactly; (hi, lo) += p + e by TwoSum (explicit _rn operations)
+        const float pp = __fmul_rn(f, f), e = __fmaf_rn(f, f, -pp);
+        const float sn = __fadd_rn(hi, pp), bp = __fsub_rn(sn, hi);
+        lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(__fsub_rn(hi, __fsub_rn(sn, bp)), __fsub_rn(pp, bp)), e));
+        hi = sn;
+      }
+      Cm = Cc;
+      Cc = Cn;
+      Bp = Bn;
+      dp = dn;
+    }
+    __syncthreads();  // the converted-plane ring is reused by the next task
+  }
+  if (fault) {  // block-uniform (__syncthreads_or): drain the copies in flight, then report
+    if (tid == 0) {
+      for (unsigned long long m = n; m < in; ++m)
+        if (!mbar_wait(smem_u32(bars + (m % kR3Stages)), (unsigned)((m / kR3Stages) & 1))) break;
+      ds[S_FAULT] = 1.0;
+      partials[blockIdx.x] = __longlong_as_double(0x7ff8000000000000LL);
+      partials[kMxParts + blockIdx.x] = __longlong_as_double(0x7ff8000000000000LL);
+      for (int i = gridDim.x + blockIdx.x; i < kMxParts; i += gridDim.x) partials[i] = partials[kMxParts + i] = 0.0;
+    }
+    return;
+  }
+  // sum f^2 -> sum r^2 = sum f^2 / scale^2 (exact power of two)
+  const double s2d = ((double)hi + (double)lo) / (scale * scale);
+  const double s1d = NEUMANN ? ldexp(__dadd_rn(__dmul_rn((double)(long long)(s1 >> 64), 18446744073709551616.0),
+                                               (double)(unsigned long long)s1),
+                                     -(k + q))
+                             : 0.0;
+  __shared__ double sh2[kMxThreads / 32], sh1[kMxThreads / 32];
+  double a2 = s2d, a1 = s1d;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a2 += __shfl_down_sync(0xffffffffu, a2, o);
+    a1 += __shfl_down_sync(0xffffffffu, a1, o);
+  }
+  if (ti == 0) {
+    sh2[tj] = a2;
+    sh1[tj] = a1;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double u = 0.0, v = 0.0;
+    for (int w = 0; w < kMxThreads / 32; ++w) {
+      u += sh2[w];
+      v += sh1[w];
+    }
+    partials[blockIdx.x] = u;
+    partials[kMxParts + blockIdx.x] = v;
+    // the final pass reads kMxParts partials: the blocks clear the unused ones
+    for (int i = gridDim.x + blockIdx.x; i < kMxParts; i += gridDim.x) partials[i] = partials[kMxParts + i] = 0.0;
+  }
+}
+
+__global__ void k_pad_dq(const int8_t* __restrict__ dq, int8_t* __restrict__ dqp, int tx, int txp, long long rows) {
+  const long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= rows * txp) return;
+  const long long r = I / txp;
+  const int c = (int)(I - r * txp);
+  dqp[I] = c < tx ? dq[r * tx + c] : (int8_t)-128;
+}
+
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+PFN_encodeTiled g_encode = nullptr;
+std::once_flag g_encode_once;
+
+PFN_encodeTiled encoder() {
+  std::call_once(g_encode_once, [] {
+    cudaDriverEntryPointQueryResult qr;
+    void* f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &qr) ==
+            cudaSuccess &&
+        qr == cudaDriverEntryPointSuccess)
+      g_encode = (PFN_encodeTiled)f;
+    else
+      cudaGetLastError();
+  });
+  return g_encode;
+}
+
+// a 3D tiled map of a tx x ty x tz array (row pitch `pitch` elements), box w x h x 1, zero fill outside
+bool encode3(CUtensorMap* m, CUtensorMapDataType dt, int esize, const void* base, int tx, long long pitch, int ty,
+             int tz, int w, int h) {
+  PFN_encodeTiled enc = encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)tx, (cuuint64_t)ty, (cuuint64_t)tz};
+  const cuuint64_t strides[2] = {(cuuint64_t)(pitch * esize), (cuuint64_t)(pitch * esize * ty)};
+  const cuuint32_t box[3] = {(cuuint32_t)w, (cuuint32_t)h, 1};
+  const cuuint32_t es[3] = {1, 1, 1};
+  return enc(m, dt, 3, const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <bool NEUMANN>
+int r3_grid() {
+  static int blocks = 0;  // one wave: resident blocks per SM x SMs, at most kMxParts
+  if (!blocks) {
+    int dev = 0, nsm = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_resid_int3d<NEUMANN>, kMxThreads, kR3Smem);
+    blocks = nsm * (per > 0 ? per : 1);
+    if (blocks > kMxParts || blocks <= 0) blocks = kMxParts;
+  }
+  return blocks;
+}
+
+}  // namespace
+
+int dq_pitch(int tx) { return (tx + 15) & ~15; }
+
+void launch_pad_dq(const int8_t* dq, int8_t* dqp, int tx, int txp, long long rows, cudaStream_t s) {
+  const long long n = rows * txp;
+  k_pad_dq<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dq, dqp, tx, txp, rows);
+}
+
+bool launch_resid_int3d(const double* x, const double* b, const int8_t* dqp, const Geom& g, const Box& bx,
+                        double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s) {
+  // TMA: global addresses on 16 bytes, row and plane pitches multiples of 16 bytes
+  if (!dqp || g.tx % 2 != 0 || ((uintptr_t)x | (uintptr_t)b | (uintptr_t)dqp) % 16 != 0) return false;
+  R3Space sp;
+  sp.c0 = bx.i0 - 1;
+  sp.r0 = bx.j0 - 1;
+  sp.p0 = bx.k0 - 1;
+  sp.ni = bx.i1 - bx.i0 + 1;
+  sp.nj = bx.j1 - bx.j0 + 1;
+  sp.nk = bx.k1 - bx.k0 + 1;
+  // the boxes start at column c0t-1 >= 0, row r0t-1 >= 0 and plane ka-1 >= 0
+  if (sp.ni <= 0 || sp.nj <= 0 || sp.nk <= 0 || sp.c0 < 1 || sp.r0 < 1 || sp.p0 < 1) return false;
+  sp.nti = (sp.ni + kR3TI - 1) / kR3TI;
+  sp.ntj = (sp.nj + kR3TJ - 1) / kR3TJ;
+  sp.n1 = g.n1;
+  sp.n2 = g.n2;
+  CUtensorMap mx, mb, md;
+  const int txp = dq_pitch(g.tx);
+  if (!encode3(&mx, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, x, g.tx, g.tx, g.ty, g.tz, kR3XW, kR3XH) ||
+      !encode3(&mb, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, b, g.tx, g.tx, g.ty, g.tz, kR3BW, kR3TJ) ||
+      !encode3(&md, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, dqp, txp, txp, g.ty, g.tz, kR3DW, kR3TJ))
+    return false;
+  const int grid = neumann ? r3_grid<true>() : r3_grid<false>();
+  // about 8 tasks per block: runs of kt planes (each streams kt + 2)
+  const long long cols = (long long)sp.nti * sp.ntj;
+  long long kt = (sp.nk * cols + 8LL * grid - 1) / (8LL * grid);
+  kt = kt < 4 ? 4 : kt;
+  sp.kt = (int)(kt > sp.nk ? sp.nk : kt);
+  sp.nkc = (sp.nk + sp.kt - 1) / sp.kt;
+  if (neumann)
+    launch_dep(k_resid_int3d<true>, grid, kMxThreads, kR3Smem, s, mx, mb, md, sp, ds, b32, r32, partials);
+  else
+    launch_dep(k_resid_int3d<false>, grid, kMxThreads, kR3Smem, s, mx, mb, md, sp, ds, b32, r32, partials);
+  return true;
+}
+
+}  // namespace cfmg

@@ -382,6 +382,13 @@ __device__ __forceinline__ long long to_fix(double v, int k) {
   const long long r = ex ? (long long)(((M >> (t - 1)) + 1ULL) >> 1) : 0LL;
   return u < 0 ? -r : r;
 }
+// k = 58 - E for max(|x|, |b|) < 2^E (device scalars S_MAXX, S_MAXB)
+__device__ __forceinline__ int fix_exponent(const double* ds) {
+  const double mx = fmax(ds[S_MAXX], ds[S_MAXB]);
+  int e = 0;
+  if (mx > 0 && isfinite(mx)) frexp(mx, &e);  // mx < 2^e
+  return 58 - e;
+}
 
 // e * 2^p as a double, exactly, with integer operations on the bits of the
 // float (the FP64 pipe then only adds: x + e*2^p rounds once, as

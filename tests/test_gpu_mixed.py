@@ -33,6 +33,9 @@ CASES = {
     # ragged 3D: plane and column counts that are no multiple of the sweeps' blocks
     "3d_40x36x26_centers_f": (dict(nx=40, ny=36, nz=26, case="threed", cycle="f", npre=2, npost=2, omega=0.8,
                                    nlevels=3), None),
+    # odd row length (tx = 39): no TMA-staged residual pass
+    "3d_odd_33x30x20_centers_v": (dict(nx=33, ny=30, nz=20, case="threed", cycle="v", npre=2, npost=2,
+                                       omega=0.8, nlevels=3), None),
 }
 
 
@@ -206,6 +209,41 @@ def test_integer_residual_matches_fp64_residual(name):
     (r1, n1, h1, x1, w), (r0, n0, h0, x0, _) = out[1], out[0]
     assert r1 <= 1e-10 and r0 <= 1e-10 and n1 == n0, (r1, r0, n1, n0)
     np.testing.assert_allclose(h1, h0, rtol=1e-4)
+    singular = base.get("location", "centers") == "centers"
+    a = _wet_mean_removed(x1, w) if singular else x1 * w
+    c = _wet_mean_removed(x0, w) if singular else x0 * w
+    assert np.linalg.norm(a - c) <= 1e-8 * np.linalg.norm(c)
+
+
+@pytest.mark.parametrize("name", ["3d_48_centers_v", "3d_32_vertices_v", "3d_40x36x26_centers_f",
+                                  "3d_odd_33x30x20_centers_v"])
+def test_staged_residual_matches_strip_residual(name):
+    """The TMA-staged 3D residual pass (default) against the row-strip pass:
+    per cell the same exact integer residual and FP32 right-hand side; the
+    norm's per-thread partial sums are combined in another order, so the
+    initial residual agrees to 1e-13, and the histories (through the last
+    bit of the wet mean) to 1e-6, with the same iteration count and the
+    same solution to 1e-8. An odd row length keeps the strip pass: bit for
+    bit."""
+    base, mkind = CASES[name]
+    out = {}
+    for on in (1, 0):
+        mg = cfmg.get_gmg(cfmg.Param(**base, tol=1e-10, maxite=40, residual_norm="l2", precision="mixed",
+                                     verbose=False))
+        msk = mg.download(1, "msk")
+        b = np.asfortranarray(np.random.default_rng(27).standard_normal(mg.shape(1))) * msk
+        F.subtract_mean(b, msk.astype(np.float64))
+        mg.data[1].b = b
+        mg.set_option("staged_residual", on)
+        res, n, hist = cfmg.solve(mg, history=True)
+        out[on] = (res, n, hist, mg.data[1].x, msk.astype(bool), mg.shape(1)[0])
+    (r1, n1, h1, x1, w, tx), (r0, n0, h0, x0, _, _) = out[1], out[0]
+    assert r1 <= 1e-10 and r0 <= 1e-10 and n1 == n0, (r1, r0, n1, n0)
+    if tx % 2:
+        assert np.array_equal(h1, h0) and np.array_equal(x1, x0)
+        return
+    np.testing.assert_allclose(h1[0], h0[0], rtol=1e-13)
+    np.testing.assert_allclose(h1, h0, rtol=1e-6)
     singular = base.get("location", "centers") == "centers"
     a = _wet_mean_removed(x1, w) if singular else x1 * w
     c = _wet_mean_removed(x0, w) if singular else x0 * w
