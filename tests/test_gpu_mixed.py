@@ -389,11 +389,13 @@ def test_dependent_launch_is_bit_identical(name, precision):
 
 
 
-@pytest.mark.parametrize("name", ["3d_48_centers_v", "3d_32_vertices_v", "3d_40x36x26_centers_f"])
+@pytest.mark.parametrize("name", ["3d_48_centers_v", "3d_32_vertices_v", "3d_40x36x26_centers_f",
+                                  "3d_odd_33x30x20_centers_v"])
 def test_coded_widiag_is_bit_identical(name):
     """The 3D 7-point FP32 sweeps reading omega*idiag as a one-byte code into
     a table (the default where every cell's code reproduces its float) give
-    the streamed floats' history and solution bit for bit."""
+    the streamed floats' history and solution bit for bit: in the four-cell
+    form (even row length) and in the one-cell form (odd row length)."""
     base, mkind = CASES[name]
     out = []
     for coded in (1, 0):
