@@ -71,6 +71,9 @@ struct cfmg_handle {
   // (k_resid3d.cu, CFMG_OPT_STAGED_RESIDUAL); r3_ran once that pass ran
   int8_t* dqp = nullptr;
   bool r3_on = true, r3_ran = false;
+  // mixed V-cycle, 3D 7-point: level 1's FP32 x is not zeroed before the
+  // cycle; its first sweep reads it as +0 instead (x1_zero_ok)
+  bool x1_zero = false;
   bool host_loop = false;  // CFMG_OPT_HOST_LOOP
   // call order: the operators' coefficients exist once cfmg_setup_operators,
   // cfmg_bind_level or an upload of a coefficient field ran; cfmg_adjoint
@@ -365,8 +368,9 @@ constexpr int pc() {
 }
 
 // ------------------------------------------------------- per-level operators
+// x_zero (3D 7-point coded sweeps only, see x1_zero_ok): x holds +0 and is not read
 template <class T>
-int sweep(cfmg_handle* h, int lev, int kind, const T* x, T* y, const Box* bx) {
+int sweep(cfmg_handle* h, int lev, int kind, const T* x, T* y, const Box* bx, bool x_zero = false) {
   const Level& l = h->lv[lev - 1];
   View<T> v = view<T>(l);
   Op op = mkop(kind, pc<T>(), lev, CFMG_K_SWEEP, l);
@@ -374,6 +378,7 @@ int sweep(cfmg_handle* h, int lev, int kind, const T* x, T* y, const Box* bx) {
   if (sizeof(T) == 4 && h->wq_on && h->wq_ok && !h->record) {  // standalone launches only; the engine reads w
     op.wq = l.wq;
     op.wtab = h->wtab;
+    op.assign = x_zero ? 1 : 0;
   }
   op.cff = 1.0 - h->d.omega;
   if (bx) {
@@ -508,7 +513,10 @@ int smooth_t(cfmg_handle* h, int lev, int nite) {
       // smooth_laplacian2d! (src/laplacian.jl:95-112), smooth_laplacian!
       // (src/laplacian.jl:24-41), variable coefficient
       const int k = h->d.op == CFMG_VARCOEF ? OPK_SWEEPVC : (threed(h) ? OPK_SWEEP7 : OPK_SWEEP5);
-      TRY(sweep<T>(h, lev, k, v.x, v.y, nullptr));
+      // the mixed V-cycle's first level-1 sweep reads an x of +0 (x1_zero)
+      const bool xz = sizeof(T) == 4 && lev == 1 && kt == 0 && h->x1_zero;
+      h->x1_zero = h->x1_zero && !(sizeof(T) == 4 && lev == 1);
+      TRY(sweep<T>(h, lev, k, v.x, v.y, nullptr, xz));
       TRY(sweep<T>(h, lev, k, v.y, v.x, nullptr));
     }
     TRY(fill_if<T>(h, lev, v.x));
@@ -688,9 +696,43 @@ int smooth_tb_epi(cfmg_handle* h, int lev, int nite) {
   return CFMG_OK;
 }
 
+// 3D 7-point cell-centred FP32 level (standalone, coded diag): the residual
+// is formed at the children of the coarse interior cells and restricted in
+// one pass (k_resid_restrict7c), which needs every such child inside the
+// fine interior box
+bool resid_restrict3d_ok(const cfmg_handle* h, int lev) {
+  if (!h->fuse_on || h->record || !threed(h) || xperio(h) || lev >= L(h) || h->d.op != CFMG_LAPLACIAN ||
+      vertices(h) || !h->wq_on || !h->wq_ok)
+    return false;
+  const Level& f = h->lv[lev - 1];
+  if (h->engine_on && (long long)f.len <= engine_limit(h, CFMG_MIXED)) return false;
+  const Box fi = interior(f), ci = interior(h->lv[lev]);
+  auto c2f = [](int i, int nh) { return (i - nh - 1) * 2 + nh + 1; };
+  return c2f(ci.i0, f.nh) >= fi.i0 && c2f(ci.i1, f.nh) + 1 <= fi.i1 && c2f(ci.j0, f.nh) >= fi.j0 &&
+         c2f(ci.j1, f.nh) + 1 <= fi.j1 && c2f(ci.k0, f.nh) >= fi.k0 && c2f(ci.k1, f.nh) + 1 <= fi.k1;
+}
+
+int resid_restrict3d(cfmg_handle* h, int lev) {
+  const Level& f = h->lv[lev - 1];
+  const Level& c = h->lv[lev];
+  const View<float> vf = view<float>(f), vc = view<float>(c);
+  TRY(flush(h));
+  {
+    Launch k(h, CFMG_K_RESIDUAL, lev, CFMG_MIXED);
+    launch_resid_restrict7c(vf.x, vf.b, f.wq, f.msk, vc.Rcoef, vc.b, geom(f), geom(c), interior(c), h->stream);
+  }
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
 template <class T>
 int descend_t(cfmg_handle* h, int lev, int nite) {
   if (sizeof(T) == 4 && fused_descent_ok(h, lev)) return smooth_tb_epi(h, lev, nite);
+  if (sizeof(T) == 4 && resid_restrict3d_ok(h, lev)) {
+    TRY(smooth_t<T>(h, lev, nite));
+    TRY(resid_restrict3d(h, lev));
+    return zero_t<T>(h, lev + 1, CFMG_X);
+  }
   TRY(smooth_t<T>(h, lev, nite));
   TRY(residual_t<T>(h, lev));
   TRY(restrict_t<T>(h, lev, CFMG_R));
@@ -1163,20 +1205,38 @@ __global__ void init_scale(double* ds) {
   ds[S_NEXT] = ldexp(1.0, -e);
 }
 
+// The V-cycle's first read of level 1's FP32 x is its first pre-smoothing
+// sweep: in the 3D 7-point coded four-cell form that sweep takes x as +0
+// without reading it, so x is not zeroed. The cells the sweeps never write
+// (planes 1 and tz) hold +0 from the arena's clearing, like every cell
+// outside the wet interior of the mixed form's FP32 fields.
+bool x1_zero_ok(const cfmg_handle* h, int kind) {
+  if (kind != CFMG_CYCLE_V && kind != CFMG_CYCLE_VREC) return false;
+  if (!threed(h) || h->d.op != CFMG_LAPLACIAN || xperio(h) || h->d.npre < 1 || h->record || !h->wq_on ||
+      !h->wq_ok || tb_eligible<float>(h, 1) || L(h) < 2)
+    return false;
+  const Level& l = h->lv[0];
+  if (h->engine_on && (long long)l.len <= engine_limit(h, CFMG_MIXED)) return false;
+  const View<float> v = view<float>(l);
+  return l.xswap == 0 && sweep7_quad_ok(geom(l), v.x, v.y, v.b, l.wq);
+}
+
 int mixed_iteration(cfmg_handle* h, int kind) {
   for (Level& l : h->lv) l.xswap = 0;  // every FP32 x is zeroed before use in the cycle
   // the F-cycle's first write of level 1's x is its last prolongation: the
   // x buffer (+0 outside the wet interior in both buffers) is assigned
   // there, not zeroed first
   const bool lazy = kind == CFMG_CYCLE_F && !xperio(h);
+  h->x1_zero = !lazy && x1_zero_ok(h, kind);
   if (fused_ok(h)) {  // the right-hand side was made by the previous fused pass
     const Level& l1 = h->lv[0];
-    if (!lazy) TRY(zero_t<float>(h, 1, CFMG_X));
+    if (!lazy && !h->x1_zero) TRY(zero_t<float>(h, 1, CFMG_X));
     // the update with max |x| can run in the cycle's last level-1 pass
     h->upd_req = h->upd_on && int_path(h);
     h->upd_done = false;
     const int st = cycle_t<float>(h, kind, lazy);
     h->upd_req = false;
+    h->x1_zero = false;
     if (st != CFMG_OK) return st;
     if (!h->upd_done) {
       Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED);
@@ -1197,9 +1257,11 @@ int mixed_iteration(cfmg_handle* h, int kind) {
     launch_dep(k_scale_from_norm, 1, kNormParts, 0, h->stream, h->dscal, h->partials, kNormParts, remove_mean);
     launch_dep(k_rhs32, nb, 256, 0, h->stream, l1.r, l1.msk, h->dscal, l1.b32, l1.r32, n);
   }
-  if (!lazy) TRY(zero_t<float>(h, 1, CFMG_X));
+  if (!lazy && !h->x1_zero) TRY(zero_t<float>(h, 1, CFMG_X));
   LAUNCH_OK(h);
-  TRY(cycle_t<float>(h, kind, lazy));
+  const int st = cycle_t<float>(h, kind, lazy);
+  h->x1_zero = false;
+  TRY(st);
   {
     Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED);
     launch_dep(k_update, nb, 256, 0, h->stream, l1.x, view<float>(l1).x, h->dscal, n);

@@ -93,9 +93,16 @@ template <class T>
 void launch_sweep5_2d(const T* x, T* y, const T* b, const T* widiag, T cff, const Geom& g, cudaStream_t s);
 template <class T>
 void launch_sweep7_3d(const T* x, T* y, const T* b, const T* widiag, T cff, const Geom& g, cudaStream_t s);
-// the same FP32 7-point sweep with omega*idiag read as wtab[wq[I]]
+// the same FP32 7-point sweep with omega*idiag read as wtab[wq[I]]; x_zero:
+// x holds +0 in every cell and is not read (four-cell form only, see
+// sweep7_quad_ok)
 void launch_sweep7_3d_q(const float* x, float* y, const float* b, const uint8_t* wq, const float* wtab, float cff,
-                        const Geom& g, cudaStream_t s);
+                        const Geom& g, cudaStream_t s, bool x_zero = false);
+bool sweep7_quad_ok(const Geom& g, const void* x, const void* y, const void* b, const void* wq);
+// FP32 3D 7-point cell-centred residual at the children of the coarse box cb
+// restricted into the coarse b (k_ops.cu); dc: diag as one-byte codes
+void launch_resid_restrict7c(const float* x, const float* b, const uint8_t* dc, const uint8_t* m, const float* rcoef,
+                             float* bc, const Geom& gf, const Geom& gc, const Box& cb, cudaStream_t s);
 template <class T>
 void launch_sweep9_2d(const T* x, T* y, const T* b, const T* widiag, T cff, const Geom& g, const Box& bx,
                       cudaStream_t s);

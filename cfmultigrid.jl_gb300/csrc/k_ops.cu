@@ -169,6 +169,47 @@ __global__ void __launch_bounds__(kThreads) k_prolong(T* __restrict__ xf, const 
   if (p < np_i && qj < np_j && qk < np_k) d_prolong<T, KIND, ASSIGN>(xf, x, coef, gf, gc, p, qj, qk, kf0);
 }
 
+// ------------------------------------------ residual + restriction, 3D
+// rloop3d! (src/laplacian.jl:43-51) at the eight children of each coarse
+// interior cell and the cell-centred 3D restriction of those residuals
+// (rcloop3d!, src/RP_on_centers.jl:62-82) into the coarse b, in one pass of
+// the FP32 7-point level: the fine r is not stored and read back. diag is
+// read as its one-byte code (an integer diag for the 7-point weights, the
+// float exactly). Each child's residual and the sum of the eight are
+// computed as v_resid7 and v_restrict<KIND 1> do, so the coarse b is the
+// same bits. Every child must lie in the fine interior box (checked by the
+// caller).
+__global__ void __launch_bounds__(256) k_resid_restrict7c(const float* __restrict__ x, const float* __restrict__ b,
+                                                          const uint8_t* __restrict__ dc,
+                                                          const uint8_t* __restrict__ m,
+                                                          const float* __restrict__ rcoef, float* __restrict__ bc,
+                                                          Geom gf, Geom gc, Box cb) {
+  dep_wait();
+  const BoxIdx q = box_idx(cb);
+  if (!q.ok) return;
+  typedef Ar<float> A;
+  const int nh = gc.nh;
+  const long long n1 = gf.n1, n2 = gf.n2;
+  const long long F = lin(gf, c2f(q.i, nh), c2f(q.j, nh), c2f(q.k, nh));
+  auto r = [&](long long I) {
+    return mask_mul(m[I], A::sub(A::add(A::mul((float)dc[I], x[I]), b[I]), faces6(x, I, n1, n2)));
+  };
+  float s = A::add(r(F), r(F + 1));
+  s = A::add(s, r(F + n1));
+  s = A::add(s, r(F + 1 + n1));
+  s = A::add(s, r(F + n2));
+  s = A::add(s, r(F + 1 + n2));
+  s = A::add(s, r(F + n1 + n2));
+  s = A::add(s, r(F + 1 + n1 + n2));
+  const long long C = lin(gc, q.i, q.j, q.k);
+  bc[C] = A::mul(rcoef[C], s);
+}
+void launch_resid_restrict7c(const float* x, const float* b, const uint8_t* dc, const uint8_t* m, const float* rcoef,
+                             float* bc, const Geom& gf, const Geom& gc, const Box& cb, cudaStream_t s) {
+  if (box_empty(cb)) return;
+  launch_dep(k_resid_restrict7c, box_grid(cb, kBoxBlk), kBoxBlk, 0, s, x, b, dc, m, rcoef, bc, gf, gc, cb);
+}
+
 // ------------------------------------------------------------------- halo
 // fill! for :xperio (src/halo.jl:6-9). One thread per (j,k) line copies the
 // nh columns through registers, so the copies of each statement read
@@ -287,7 +328,11 @@ __global__ void __launch_bounds__(256) k_sweep7_3d_q(const float* __restrict__ x
 // the measured HBM copy bandwidth for its 13 bytes a cell (against four
 // times as many load instructions in the one-cell form, whose warps stalled
 // on the load queue). Each cell's arithmetic is the one-cell form's.
+// ZERO: x is known to hold +0 in every cell (the first sweep of a cycle's
+// level-1 pre-smoothing): it is not read, and the same formula on +0
+// operands gives the same bits.
 constexpr int kQRun = 4;
+template <bool ZERO>
 __global__ void __launch_bounds__(256) k_sweep7_3d_q4(const float* __restrict__ x, float* __restrict__ y,
                                                       const float* __restrict__ b, const uint8_t* __restrict__ wq,
                                                       const float* __restrict__ wtab, float cff, long long n1,
@@ -302,12 +347,16 @@ __global__ void __launch_bounds__(256) k_sweep7_3d_q4(const float* __restrict__ 
   const int k1 = min(k0 + kQRun, tz - 1);
   typedef Ar<float> A;
   long long I = 4 * t + n2 * k0;
-  float4 xm = *reinterpret_cast<const float4*>(x + I - n2), xc = *reinterpret_cast<const float4*>(x + I);
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  const float2 z2 = make_float2(0.f, 0.f);
+  auto ld4 = [&](long long J) { return ZERO ? z4 : *reinterpret_cast<const float4*>(x + J); };
+  auto ld2 = [&](long long J) { return ZERO ? z2 : *reinterpret_cast<const float2*>(x + J); };
+  float4 xm = ld4(I - n2), xc = ld4(I);
   for (int k = k0; k < k1; ++k, I += n2) {
-    const float4 xp = *reinterpret_cast<const float4*>(x + I + n2);
-    const float xw = x[I - 1], xe = x[I + 4];
-    const float2 s0 = *reinterpret_cast<const float2*>(x + I - n1), s1 = *reinterpret_cast<const float2*>(x + I - n1 + 2);
-    const float2 u0 = *reinterpret_cast<const float2*>(x + I + n1), u1 = *reinterpret_cast<const float2*>(x + I + n1 + 2);
+    const float4 xp = ld4(I + n2);
+    const float xw = ZERO ? 0.f : x[I - 1], xe = ZERO ? 0.f : x[I + 4];
+    const float2 s0 = ld2(I - n1), s1 = ld2(I - n1 + 2);
+    const float2 u0 = ld2(I + n1), u1 = ld2(I + n1 + 2);
     const float4 bb = *reinterpret_cast<const float4*>(b + I);
     const uchar4 q = *reinterpret_cast<const uchar4*>(wq + I);
     const float f0 = A::add(A::add(A::add(A::add(A::add(xw, xc.y), s0.x), u0.x), xm.x), xp.x);
@@ -325,16 +374,22 @@ __global__ void __launch_bounds__(256) k_sweep7_3d_q4(const float* __restrict__ 
     xc = xp;
   }
 }
+bool sweep7_quad_ok(const Geom& g, const void* x, const void* y, const void* b, const void* wq) {
+  return g.n2 % 4 == 0 && g.n1 % 2 == 0 && ((uintptr_t)x | (uintptr_t)y | (uintptr_t)b) % 16 == 0 &&
+         (uintptr_t)wq % 4 == 0;
+}
 void launch_sweep7_3d_q(const float* x, float* y, const float* b, const uint8_t* wq, const float* wtab, float cff,
-                        const Geom& g, cudaStream_t s) {
+                        const Geom& g, cudaStream_t s, bool x_zero) {
   if (g.tz < 3) return;
-  const bool quad = g.n2 % 4 == 0 && g.n1 % 2 == 0 && ((uintptr_t)x | (uintptr_t)y | (uintptr_t)b) % 16 == 0 &&
-                    (uintptr_t)wq % 4 == 0;
-  if (quad) {
+  if (sweep7_quad_ok(g, x, y, b, wq)) {
     const dim3 grid((unsigned)((g.n2 / 4 + 255) / 256), (unsigned)((g.tz - 2 + kQRun - 1) / kQRun));
-    launch_dep(k_sweep7_3d_q4, grid, 256, 0, s, x, y, b, wq, wtab, cff, g.n1, g.n2, g.tz);
+    if (x_zero)
+      launch_dep(k_sweep7_3d_q4<true>, grid, 256, 0, s, x, y, b, wq, wtab, cff, g.n1, g.n2, g.tz);
+    else
+      launch_dep(k_sweep7_3d_q4<false>, grid, 256, 0, s, x, y, b, wq, wtab, cff, g.n1, g.n2, g.tz);
     return;
   }
+  if (x_zero) cudaMemsetAsync(const_cast<float*>(x), 0, (size_t)g.len * sizeof(float), s);  // the one-cell form reads x
   const dim3 grid((unsigned)((g.tx + 31) / 32), (unsigned)((g.ty + 7) / 8), (unsigned)((g.tz - 2 + kKRun - 1) / kKRun));
   launch_dep(k_sweep7_3d_q, grid, dim3(32, 8, 1), 0, s, x, y, b, wq, wtab, cff, g.tx, g.ty, g.tz);
 }
@@ -495,7 +550,8 @@ static void launch_op_t(const Op& op, cudaStream_t s) {
     case OPK_SWEEP5: launch_sweep5_2d<T>(x, y, b, w, cff, op.g, s); break;
     case OPK_SWEEP7:
       if (sizeof(T) == 4 && op.wq)
-        launch_sweep7_3d_q((const float*)x, (float*)y, (const float*)b, op.wq, op.wtab, (float)cff, op.g, s);
+        launch_sweep7_3d_q((const float*)x, (float*)y, (const float*)b, op.wq, op.wtab, (float)cff, op.g, s,
+                           op.assign != 0);
       else
         launch_sweep7_3d<T>(x, y, b, w, cff, op.g, s);
       break;

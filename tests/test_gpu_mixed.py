@@ -395,14 +395,19 @@ def test_coded_widiag_is_bit_identical(name):
     """The 3D 7-point FP32 sweeps reading omega*idiag as a one-byte code into
     a table (the default where every cell's code reproduces its float) give
     the streamed floats' history and solution bit for bit: in the four-cell
-    form (even row length) and in the one-cell form (odd row length)."""
+    form (even row length) and in the one-cell form (odd row length). So do
+    the forms that come with the codes: the cell-centred residual formed at
+    the coarse cells' children and restricted in one pass (fused_descent
+    on), and, in the V-cycle, the first level-1 sweep taking x as +0
+    without the zeroing pass."""
     base, mkind = CASES[name]
     out = []
-    for coded in (1, 0):
+    for coded, fuse in ((1, 1), (1, 0), (0, 1)):
         mg = cfmg.get_gmg(cfmg.Param(**base, tol=1e-10, maxite=40, residual_norm="l2", precision="mixed",
                                      verbose=False))
         mg.set_option("engine_cells", 2000)  # fine levels as standalone kernels
         mg.set_option("coded_widiag", coded)
+        mg.set_option("fused_descent", fuse)
         custom = _mask(base, mg.shape(1), mkind)
         if custom is not None:
             mg.oper[1].msk = custom
@@ -417,5 +422,6 @@ def test_coded_widiag_is_bit_identical(name):
         res, n, hist = cfmg.solve(mg, history=True)
         out.append((res, n, hist, mg.data[1].x))
     assert out[0][0] <= 1e-10
-    assert out[0][1] == out[1][1] and out[0][0] == out[1][0]
-    assert np.array_equal(out[0][2], out[1][2]) and np.array_equal(out[0][3], out[1][3])
+    for o in out[1:]:
+        assert out[0][1] == o[1] and out[0][0] == o[0]
+        assert np.array_equal(out[0][2], o[2]) and np.array_equal(out[0][3], o[3])
