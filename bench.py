@@ -81,9 +81,12 @@ def parse():
     ap.add_argument("--no-int", action="store_true", help="--quick: level-1 residual in FP64 arithmetic")
     ap.add_argument("--no-fuse", action="store_true",
                     help="--quick: no fused descent or fused solution update (plain smoothing passes)")
+    ap.add_argument("--fp64", action="store_true",
+                    help="--quick: the FP64 drop-in instead of the mixed form (for ncu captures of its kernels)")
     args = ap.parse_args()
-    if (args.tb is not None or args.no_int or args.no_fuse) and not (args.quick and args.workload == "config2"):
-        ap.error("--tb, --no-int and --no-fuse go with --quick (config 2) only")
+    if (args.tb is not None or args.no_int or args.no_fuse or args.fp64) and not (
+            args.quick and args.workload == "config2"):
+        ap.error("--tb, --no-int, --no-fuse and --fp64 go with --quick (config 2) only")
     if args.steps is None:
         args.steps = 30 if (args.impl == "ours" and args.workload == "config2") else 5
     return args
@@ -261,7 +264,7 @@ def run_ours(args, rank, world, local):
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
     param, vmsk, noise = W.config2(args.n, nlevels=args.nlevels or W.CONFIG2_LEVELS)
-    mgm, b = make_gmg(cfmg, param, vmsk, noise, "mixed", sp)
+    mgm, b = make_gmg(cfmg, param, vmsk, noise, "fp64" if args.fp64 else "mixed", sp)
     if args.host_loop:
         mgm.set_option("host_loop", 1)
     if args.tb is not None:
@@ -682,14 +685,31 @@ def bench_config3(args, local, sub=False):
 
     ms_e2e, _ = _timed(stream, e2e, steps)
 
-    # roofline: the level-1 FP32 7-point Jacobi sweep of the mixed form
-    nl, tl = profile(cfmg, mgm, "sweep", 1, "mixed", lambda: solve(mgm))
+    # roofline: the level-1 FP32 7-point Jacobi sweep of the mixed form. A
+    # sweep moves 13 B a cell (x, b and y as FP32, omega*idiag as a one-byte
+    # code); the first sweep of each cycle takes x as +0 without reading it
+    # (9 B a cell)
+    got = {}
+
+    def solve_n():
+        got["r"] = solve(mgm)
+
+    nl, tl = profile(cfmg, mgm, "sweep", 1, "mixed", solve_n)
+    ncyc = got["r"][1]
     g1 = mgm.levels[1]
     sweep_cells = g1.tx * g1.ty * (g1.tz - 2)  # linear range 1+tx*ty : len-tx*ty
     ms_launch = tl / max(nl, 1)
     peak, peak_src = hbm_peak()
-    bytes_per_launch = 16.0 * sweep_cells
+    nzero = min(ncyc, nl)
+    bytes_per_launch = sweep_cells * (13.0 * (nl - nzero) + 9.0 * nzero) / max(nl, 1)
     achieved = bytes_per_launch / (ms_launch * 1e-3) / 1e9 if ms_launch > 0 else 0.0
+    # the fixed-point level-1 residual pass (TMA-staged): x, b (FP64) and
+    # Q*diag (one byte) read, the FP32 right-hand side written, per interior cell
+    nr, trr = profile(cfmg, mgm, "residual", 1, "fp64", lambda: solve(mgm))
+    interior = n * n * (n // 2)
+    ms_r = trr / max(nr, 1)
+    bytes_r = 21.0 * interior
+    ach_r = bytes_r / (ms_r * 1e-3) / 1e9 if ms_r > 0 else 0.0
     mgm.close()
     return {"metric": f"ms/solve to 1e-9 rel residual (mixed FP32-in-FP64), {n}x{n}x{n // 2} cell-centred "
                       "7-point V-cycle",
@@ -706,10 +726,14 @@ def bench_config3(args, local, sub=False):
             "mixed_rel_err_vs_fp64": err,
             "e2e": {"value": ms_e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
             "gpu_launches": launches,
-            "roofline": {"kernel": "FP32 7-point Jacobi sweep, level 1", "bound": "hbm", "achieved": achieved,
-                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
-                         "traffic": None, "launches_timed": nl, "ms_per_launch": ms_launch,
+            "roofline": {"kernel": "k_sweep7_3d_q4: FP32 7-point Jacobi sweep, level 1", "bound": "hbm",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": peak_src, "traffic": None, "launches_timed": nl, "ms_per_launch": ms_launch,
                          "bytes_per_launch": bytes_per_launch},
+            "roofline_residual": {"kernel": "k_resid_int3d: TMA-staged fixed-point level-1 residual (with its "
+                                            "one-block final reduction)", "bound": "hbm", "achieved": ach_r,
+                                  "peak": peak, "unit": "GB/s", "frac": ach_r / peak, "launches_timed": nr,
+                                  "ms_per_launch": ms_r, "bytes_per_launch": bytes_r},
             "clocks": clk.summary()}
 
 
