@@ -408,6 +408,17 @@ bool tb_eligible(const cfmg_handle* h, int lev) {
   return !(h->engine_on && (long long)l.len <= engine_limit(h, CFMG_MIXED));
 }
 
+// 3D 19-point FP32 level of a closed topology, standalone: its smoothing
+// call as one streaming pass (k_tb3d.cu, L19). The halo must hold the pass's
+// first-sweep box (nh >= 2, as the reference's icp x jcp x kcp needs too).
+bool tb3d19_ok(const cfmg_handle* h, int lev) {
+  if (!h->tb_on || h->tb_version != 4 || h->record || xperio(h) || !threed(h) || h->d.op != CFMG_LAPLACIAN9)
+    return false;
+  const Level& l = h->lv[lev - 1];
+  if (l.nh < 2) return false;
+  return !(h->engine_on && (long long)l.len <= engine_limit(h, CFMG_MIXED));
+}
+
 // 3D 7-point: passes of up to 2 pairs (k_tb3d.cu), x -> partner buffer
 int smooth_tb3d(cfmg_handle* h, int lev, int nite) {
   Level& l = h->lv[lev - 1];
@@ -500,6 +511,18 @@ int smooth_t(cfmg_handle* h, int lev, int nite) {
     // is; sweep 1 over icp x jcp x kcp, sweep 2 over the interior; no fill!
     Box ext{l.nh, l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, l.nh, l.nz + l.nh + 1};
     Box in = interior(l);
+    if (sizeof(T) == 4 && tb3d19_ok(h, lev)) {  // the pair in one streaming pass, into the other x buffer
+      TRY(flush(h));
+      {
+        Launch k(h, CFMG_K_SWEEP, lev, CFMG_MIXED);
+        const View<float> vf = view<float>(l);
+        launch_smooth_tb3d19(vf.x, vf.y, vf.b, vf.widiag, (float)(1.0 - h->d.omega), l.tx, l.ty, l.tz, in, ext,
+                             h->stream);
+      }
+      h->lv[lev - 1].xswap ^= 1;
+      LAUNCH_OK(h);
+      return CFMG_OK;
+    }
     TRY(sweep<T>(h, lev, OPK_SWEEP19, v.x, v.y, &ext));
     return sweep<T>(h, lev, OPK_SWEEP19, v.y, v.x, &in);
   }

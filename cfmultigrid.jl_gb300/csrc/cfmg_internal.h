@@ -224,6 +224,9 @@ void launch_program(const Op* prog, int nops, double* red, cudaStream_t s);  // 
 // 3D 7-point streaming blocked passes (k_tb3d.cu): nite (1 or 2) pairs over U
 bool launch_smooth_tb3d(int nite, const float* x, float* xo, const float* b, const float* w, float cff, int tx,
                         int ty, int tz, int ui0, int ui1, int uj0, int uj1, int uk0, int uk1, cudaStream_t st);
+// the 3D 19-point smoothing call (one pair: the box ext, then the interior) in one streaming pass, x -> xo
+void launch_smooth_tb3d19(const float* x, float* xo, const float* b, const float* w, float cff, int tx, int ty, int tz,
+                          const Box& interior, const Box& ext, cudaStream_t st);
 // temporally blocked FP32 smoother (k_tb.cu): nite pairs of 5- or 9-point
 // sweeps over the box U in one pass, x -> xo; false if nite is not
 // 1..kTbMaxPairs. A pass of p pairs recomputes a halo of 2p cells around each

@@ -18,6 +18,17 @@
 // box U = [nh, n+nh+1]^3 with the same formula is bit-identical to the
 // reference's linear sweep range, while cells outside U keep their value.
 // The per-cell arithmetic is d_sweep7's Ar<float> sequence.
+//
+// L19: the 3D 19-point operator's smoothing call (smooth_laplacian9!,
+// src/laplacian9.jl:2-47): one pair whatever nite is, the first sweep over
+// the box E = icp x jcp x kcp (the interior and one cell around it), the
+// second over the interior box U, in one pass (S = 2). Level 1 updates the
+// cells of E, level 2 those of U; level 2 at a cell of U reads level 1 only
+// inside E, so what level 1 holds elsewhere is never used. The result goes
+// to the other x buffer, whose cells outside U hold +0 like the input's
+// (the mixed form's invariant). The per-cell arithmetic is v_sweep19's:
+// faces then edges, each a left fold, folded into b with the exact products
+// by -1/2 and -1/4.
 #include "ops_dev.cuh"
 
 namespace cfmg {
@@ -27,12 +38,12 @@ constexpr int kT3dThreads = 1024;
 constexpr int kT3dCells = kT3dW * kT3dH / kT3dThreads;  // cells per thread and plane (2)
 constexpr int kT3dPlane = kT3dW * kT3dH;
 
-template <int S>
+template <int S, bool L19>
 __global__ void __launch_bounds__(kT3dThreads, 1) k_smooth_tb3d(const float* __restrict__ x, float* __restrict__ xo,
                                                                 const float* __restrict__ b,
                                                                 const float* __restrict__ w, float cff, int tx, int ty,
                                                                 int tz, int ui0, int ui1, int uj0, int uj1, int uk0,
-                                                                int uk1, int kchunk) {
+                                                                int uk1, int kchunk, Box eb) {
   dep_wait();
   constexpr int H = S;
   constexpr int CW = kT3dW - 2 * H, CH = kT3dH - 2 * H;
@@ -95,13 +106,37 @@ __global__ void __launch_bounds__(kT3dThreads, 1) k_smooth_tb3d(const float* __r
           const int c = threadIdx.x + e * kT3dThreads;
           const int li = c % kT3dW, lj = c / kT3dW;
           const int gi = ti0 + li, gj = tj0 + lj;
-          const bool inU = gi >= ui0 && gi <= ui1 && gj >= uj0 && gj <= uj1 && q >= uk0 && q <= uk1;
+          const bool inU = (L19 && s == 1)
+                               ? (gi >= eb.i0 && gi <= eb.i1 && gj >= eb.j0 && gj <= eb.j1 && q >= eb.k0 && q <= eb.k1)
+                               : (gi >= ui0 && gi <= ui1 && gj >= uj0 && gj <= uj1 && q >= uk0 && q <= uk1);
           // neighbours, clamped to the tile (values outside the valid region are never used)
-          const int cw = li > 0 ? c - 1 : c, ce = li < kT3dW - 1 ? c + 1 : c;
-          const int cs = lj > 0 ? c - kT3dW : c, cn = lj < kT3dH - 1 ? c + kT3dW : c;
+          const bool hw = li > 0, he = li < kT3dW - 1, hs = lj > 0, hn = lj < kT3dH - 1;
+          const int cw = hw ? c - 1 : c, ce = he ? c + 1 : c;
+          const int cs = hs ? c - kT3dW : c, cn = hn ? c + kT3dW : c;
           typedef Ar<float> A;
-          const float f = A::add(A::add(A::add(A::add(A::add(X0[cw], X0[ce]), X0[cs]), X0[cn]), Xm[c]), Xp[c]);
-          const float v = A::sub(A::mul(cff, X0[c]), A::mul(Wq[c], A::sub(Bq[c], f)));
+          float v;
+          if (L19) {
+            const int cws = (hw && hs) ? c - 1 - kT3dW : c, ces = (he && hs) ? c + 1 - kT3dW : c;
+            const int cwn = (hw && hn) ? c - 1 + kT3dW : c, cen = (he && hn) ? c + 1 + kT3dW : c;
+            const float f = A::add(A::add(A::add(A::add(A::add(X0[cw], X0[ce]), X0[cs]), X0[cn]), Xm[c]), Xp[c]);
+            float e = A::add(X0[cws], X0[ces]);
+            e = A::add(e, X0[cwn]);
+            e = A::add(e, X0[cen]);
+            e = A::add(e, Xm[cw]);
+            e = A::add(e, Xm[ce]);
+            e = A::add(e, Xp[cw]);
+            e = A::add(e, Xp[ce]);
+            e = A::add(e, Xm[cs]);
+            e = A::add(e, Xm[cn]);
+            e = A::add(e, Xp[cs]);
+            e = A::add(e, Xp[cn]);
+            float t = A::fmx(f, -0.5f, Bq[c]);
+            t = A::fmx(e, -0.25f, t);
+            v = A::sub(A::mul(cff, X0[c]), A::mul(Wq[c], t));
+          } else {
+            const float f = A::add(A::add(A::add(A::add(A::add(X0[cw], X0[ce]), X0[cs]), X0[cn]), Xm[c]), Xp[c]);
+            v = A::sub(A::mul(cff, X0[c]), A::mul(Wq[c], A::sub(Bq[c], f)));
+          }
           out[e] = inU ? v : X0[c];
         }
         if (s < S) {
@@ -125,15 +160,15 @@ __global__ void __launch_bounds__(kT3dThreads, 1) k_smooth_tb3d(const float* __r
   }
 }
 
-template <int S>
+template <int S, bool L19 = false>
 static void launch_tb3d_s(const float* x, float* xo, const float* b, const float* w, float cff, int tx, int ty, int tz,
-                          int ui0, int ui1, int uj0, int uj1, int uk0, int uk1, cudaStream_t st) {
+                          int ui0, int ui1, int uj0, int uj1, int uk0, int uk1, cudaStream_t st, Box eb = Box{}) {
   constexpr int CW = kT3dW - 2 * S, CH = kT3dH - 2 * S;
   const size_t smem = (size_t)(3 * S + 2 * (S + 1)) * kT3dPlane * sizeof(float);
   static bool attr = false;
   static int nsm = 0;
   if (!attr) {
-    cudaFuncSetAttribute(k_smooth_tb3d<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_smooth_tb3d<S, L19>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -147,7 +182,15 @@ static void launch_tb3d_s(const float* x, float* xo, const float* b, const float
   const int kchunk = (nk + nchunk - 1) / nchunk;
   nchunk = (nk + kchunk - 1) / kchunk;
   dim3 grid((unsigned)ntx, (unsigned)nty, (unsigned)nchunk);
-  launch_dep(k_smooth_tb3d<S>, grid, kT3dThreads, smem, st, x, xo, b, w, cff, tx, ty, tz, ui0, ui1, uj0, uj1, uk0, uk1, kchunk);
+  launch_dep(k_smooth_tb3d<S, L19>, grid, kT3dThreads, smem, st, x, xo, b, w, cff, tx, ty, tz, ui0, ui1, uj0, uj1, uk0,
+             uk1, kchunk, eb);
+}
+
+// the 19-point operator's pair (E, then the interior box U) in one pass, x -> xo
+void launch_smooth_tb3d19(const float* x, float* xo, const float* b, const float* w, float cff, int tx, int ty, int tz,
+                          const Box& interior, const Box& ext, cudaStream_t st) {
+  launch_tb3d_s<2, true>(x, xo, b, w, cff, tx, ty, tz, interior.i0, interior.i1, interior.j0, interior.j1, interior.k0,
+                         interior.k1, st, ext);
 }
 
 // nite pairs (1 or 2) of 7-point sweeps over the box U in one pass, x -> xo

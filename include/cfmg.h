@@ -105,8 +105,8 @@ extern "C" {
                                         shared-memory passes: 5 (default) two columns per thread in packed
                                         FP32x2 arithmetic with padded tiles and vector loads, 3 the first
                                         packed form, 1 one column per thread; 4 as 3, plus streaming passes
-                                        for 3D 7-point levels; 0: one kernel per sweep. All give the same
-                                        bits. */
+                                        for 3D 7-point levels and the 3D 19-point pair in one pass; 0: one
+                                        kernel per sweep. All give the same bits. */
 #define CFMG_OPT_INT_RESIDUAL 3 /* mixed form, closed topology, 5-, 7- and 2D 9-point operators: 1
                                    (default) computes the level-1 residual exactly in 64-bit fixed point
                                    on the integer pipes; 0 in FP64 arithmetic */

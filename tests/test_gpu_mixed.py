@@ -47,6 +47,9 @@ BIG_CASES = {
                                           nlevels=5), "disk"),
     "config1_1024_centers_v": (dict(nx=1024, ny=1024, nz=1, case="twod", cycle="v", npre=2, npost=2, omega=0.8,
                                     nlevels=6), "disk"),
+    # 3D 19-point: the streaming pair pass over two tiles in i and j and several k chunks
+    "3d_70x44x30_centers_lap9_f": (dict(nx=70, ny=44, nz=30, case="threed", operator="laplacian9", cycle="f",
+                                        npre=2, npost=2, omega=0.8, nlevels=3), None),
     # x-periodic, wet everywhere: the blocked passes' tiles wrap across the seam
     "2d_xperio_512_centers_v": (dict(nx=512, ny=256, nz=1, case="twod", topology="xperio", cycle="v", npre=2,
                                      npost=2, omega=0.8, nlevels=5), None),
@@ -137,7 +140,8 @@ def test_mixed_matches_fp64_oracle(name):
 @pytest.mark.parametrize("name", ["config1_256_centers_v", "config2_512_vertices_lap9_f", "3d_48_centers_v",
                                   "config2_2048_vertices_lap9_f", "config1_1024_centers_v", "2d_xperio_vertices_v",
                                   "2d_xperio_512_centers_v", "2d_odd_301x203_vertices_lap9_f",
-                                  "2d_odd_301x203_centers_v", "2d_twolayer_256_centers_v", "3d_32_vertices_v"])
+                                  "2d_odd_301x203_centers_v", "2d_twolayer_256_centers_v", "3d_32_vertices_v",
+                                  "3d_32_vertices_lap9_v", "3d_70x44x30_centers_lap9_f"])
 def test_temporal_blocking_is_bit_identical(name):
     """The temporally blocked FP32 smoother (all sweeps of a call in one
     shared-memory pass), and its form whose last pre-smoothing pass also
@@ -147,8 +151,8 @@ def test_temporal_blocking_is_bit_identical(name):
     out = []
     # packed FP32x2 passes (lean form with and without the fused residual and
     # restriction, with and without the FP64 solution update in the last
-    # level-1 pass; first form; 3D: + streaming passes), scalar passes, one
-    # kernel per sweep
+    # level-1 pass; first form; 3D: + streaming passes, for the 19-point
+    # operator its one-pair pass), scalar passes, one kernel per sweep
     if base.get("case") == "threed":
         runs = ((4, 1, 1), (1, 1, 1), (0, 1, 1))
     else:
