@@ -394,6 +394,115 @@ void launch_sweep7_3d_q(const float* x, float* y, const float* b, const uint8_t*
   launch_dep(k_sweep7_3d_q, grid, dim3(32, 8, 1), 0, s, x, y, b, wq, wtab, cff, g.tx, g.ty, g.tz);
 }
 
+// The FP32 19-point sweep (smooth_laplacian9!'s body, src/laplacian9.jl:14-44)
+// four cells a thread, over a box: a thread owns a quad of consecutive
+// linear indices of a plane and a run of kQ19Run planes, carrying the quad's
+// neighbourhood of planes k-1, k and k+1 in registers (x of its row as a
+// 16-byte load and the cells beside it, the rows j -/+ 1 as 8-byte pairs and
+// their cells beside). Cells of the quad outside the box are computed but not
+// stored. v_sweep19's arithmetic, in its order. Needs n2 = tx*ty a multiple
+// of 4, tx even, 16-byte aligned arrays and a halo of at least 3 (every read
+// then stays inside the array).
+constexpr int kQ19Run = 4;
+struct Q19Plane {
+  float4 c;        // row j: the quad
+  float cw, ce;    // row j: beside the quad
+  float4 s, n;     // rows j-1 and j+1 under the quad
+  float sw, se, nw, ne;
+};
+__device__ __forceinline__ Q19Plane q19_load(const float* __restrict__ x, long long P, long long n1) {
+  Q19Plane r;
+  r.c = *reinterpret_cast<const float4*>(x + P);
+  r.cw = x[P - 1];
+  r.ce = x[P + 4];
+  const float2 s0 = *reinterpret_cast<const float2*>(x + P - n1), s1 = *reinterpret_cast<const float2*>(x + P - n1 + 2);
+  const float2 u0 = *reinterpret_cast<const float2*>(x + P + n1), u1 = *reinterpret_cast<const float2*>(x + P + n1 + 2);
+  r.s = make_float4(s0.x, s0.y, s1.x, s1.y);
+  r.n = make_float4(u0.x, u0.y, u1.x, u1.y);
+  r.sw = x[P - n1 - 1];
+  r.se = x[P - n1 + 4];
+  r.nw = x[P + n1 - 1];
+  r.ne = x[P + n1 + 4];
+  return r;
+}
+__device__ __forceinline__ float q4at(const float4& v, int c) { return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w; }
+__global__ void __launch_bounds__(256) k_sweep19_3d_q4(const float* __restrict__ x, float* __restrict__ y,
+                                                       const float* __restrict__ b, const float* __restrict__ w,
+                                                       float cff, long long n1, long long n2, Box bx, long long q0,
+                                                       long long nq) {
+  dep_wait();
+  const long long qi = q0 + (long long)blockIdx.x * 256 + threadIdx.x;  // quad of the plane
+  const int k0 = (bx.k0 - 1) + (int)blockIdx.y * kQ19Run;               // 0-based planes k0 .. k1-1
+  if (qi >= q0 + nq || k0 > bx.k1 - 1) return;
+  const int k1 = min(k0 + kQ19Run, bx.k1);
+  const long long Lp = 4 * qi;
+  const int jq = (int)(Lp / n1), iq = (int)(Lp - (long long)jq * n1);
+  bool inb[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    int i = iq + c, j = jq;
+    if (i >= n1) {
+      i -= (int)n1;
+      ++j;
+    }
+    inb[c] = i >= bx.i0 - 1 && i <= bx.i1 - 1 && j >= bx.j0 - 1 && j <= bx.j1 - 1;
+  }
+  if (!(inb[0] || inb[1] || inb[2] || inb[3])) return;
+  const bool all = inb[0] && inb[1] && inb[2] && inb[3];
+  typedef Ar<float> A;
+  long long I = Lp + n2 * k0;
+  Q19Plane pm = q19_load(x, I - n2, n1), pc = q19_load(x, I, n1);
+  for (int k = k0; k < k1; ++k, I += n2) {
+    const Q19Plane pp = q19_load(x, I + n2, n1);
+    const float4 bb = *reinterpret_cast<const float4*>(b + I), ww = *reinterpret_cast<const float4*>(w + I);
+    float o[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const float xw = c == 0 ? pc.cw : q4at(pc.c, c - 1), xe = c == 3 ? pc.ce : q4at(pc.c, c + 1);
+      const float sw = c == 0 ? pc.sw : q4at(pc.s, c - 1), se = c == 3 ? pc.se : q4at(pc.s, c + 1);
+      const float nw = c == 0 ? pc.nw : q4at(pc.n, c - 1), ne = c == 3 ? pc.ne : q4at(pc.n, c + 1);
+      const float mw = c == 0 ? pm.cw : q4at(pm.c, c - 1), me = c == 3 ? pm.ce : q4at(pm.c, c + 1);
+      const float pw = c == 0 ? pp.cw : q4at(pp.c, c - 1), pe = c == 3 ? pp.ce : q4at(pp.c, c + 1);
+      const float f = A::add(A::add(A::add(A::add(A::add(xw, xe), q4at(pc.s, c)), q4at(pc.n, c)), q4at(pm.c, c)),
+                             q4at(pp.c, c));
+      float e = A::add(sw, se);
+      e = A::add(e, nw);
+      e = A::add(e, ne);
+      e = A::add(e, mw);
+      e = A::add(e, me);
+      e = A::add(e, pw);
+      e = A::add(e, pe);
+      e = A::add(e, q4at(pm.s, c));
+      e = A::add(e, q4at(pm.n, c));
+      e = A::add(e, q4at(pp.s, c));
+      e = A::add(e, q4at(pp.n, c));
+      float t = A::fmx(f, -0.5f, q4at(bb, c));
+      t = A::fmx(e, -0.25f, t);
+      o[c] = A::sub(A::mul(cff, q4at(pc.c, c)), A::mul(q4at(ww, c), t));
+    }
+    if (all) {
+      *reinterpret_cast<float4*>(y + I) = make_float4(o[0], o[1], o[2], o[3]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        if (inb[c]) y[I + c] = o[c];
+    }
+    pm = pc;
+    pc = pp;
+  }
+}
+bool launch_sweep19_3d_q4(const float* x, float* y, const float* b, const float* w, float cff, const Geom& g,
+                          const Box& bx, cudaStream_t s) {
+  if (g.n2 % 4 != 0 || g.n1 % 2 != 0 || g.nh < 3 || ((uintptr_t)x | (uintptr_t)y | (uintptr_t)b | (uintptr_t)w) % 16)
+    return false;
+  if (box_empty(bx)) return true;
+  const long long q0 = (g.n1 * (bx.j0 - 1)) / 4, qe = (g.n1 * bx.j1 + 3) / 4;  // quads covering rows j0 .. j1
+  const long long nq = qe - q0;
+  const dim3 grid((unsigned)((nq + 255) / 256), (unsigned)((bx.k1 - bx.k0 + kQ19Run) / kQ19Run));
+  launch_dep(k_sweep19_3d_q4, grid, 256, 0, s, x, y, b, w, cff, g.n1, g.n2, bx, q0, nq);
+  return true;
+}
+
 template <class T>
 void launch_sweep9_2d(const T* x, T* y, const T* b, const T* w, T cff, const Geom& g, const Box& bx,
                       cudaStream_t s) {
@@ -556,7 +665,11 @@ static void launch_op_t(const Op& op, cudaStream_t s) {
         launch_sweep7_3d<T>(x, y, b, w, cff, op.g, s);
       break;
     case OPK_SWEEP9: launch_sweep9_2d<T>(x, y, b, w, cff, op.g, op.box, s); break;
-    case OPK_SWEEP19: launch_sweep19_3d<T>(x, y, b, w, cff, op.g, op.box, s); break;
+    case OPK_SWEEP19:
+      if (!(sizeof(T) == 4 && launch_sweep19_3d_q4((const float*)x, (float*)y, (const float*)b, (const float*)w,
+                                                   (float)cff, op.g, op.box, s)))
+        launch_sweep19_3d<T>(x, y, b, w, cff, op.g, op.box, s);
+      break;
     case OPK_SWEEPVC: launch_sweep_vc_2d<T>(x, y, b, w, (const T*)op.cE, (const T*)op.cN, cff, op.g, s); break;
     case OPK_RESID5: launch_resid5_2d<T>(y, x, b, d, op.m, op.g, s); break;
     case OPK_RESID7: launch_resid7_3d<T>(y, x, b, d, op.m, op.g, op.box, s); break;
