@@ -210,6 +210,72 @@ void launch_resid_restrict7c(const float* x, const float* b, const uint8_t* dc, 
   launch_dep(k_resid_restrict7c, box_grid(cb, kBoxBlk), kBoxBlk, 0, s, x, b, dc, m, rcoef, bc, gf, gc, cb);
 }
 
+// in-order global loads (asm volatile keeps them ahead of the arithmetic
+// that follows, so that all of a thread's loads are in flight together)
+__device__ __forceinline__ float ld_nc_ordered(const float* p) {
+  float v;
+  asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ float ld_ordered(const float* p) {
+  float v;
+  asm volatile("ld.global.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+
+// pcloop3d! (src/RP_on_centers.jl:84-114) in FP32 with every load of a
+// parent issued before its arithmetic: the 25 coarse values (the centre and
+// the 8 in-plane neighbours of each of the planes kc-1, kc, kc+1 that the
+// eight children's `square` terms use), the 8 Pcoef values and, unless
+// ASSIGN, the 8 fine x values. d_prolong<float, 1>'s arithmetic in its order.
+// The thread-per-parent form compiled to 32 registers with its loads spread
+// over the arithmetic; its warps waited on memory 85-90 % of the time.
+template <bool ASSIGN>
+__global__ void __launch_bounds__(256) k_prolong3c_f(float* __restrict__ xf, const float* __restrict__ x,
+                                                     const float* __restrict__ coef, Geom gf, Geom gc, int np_i,
+                                                     int np_j, int np_k) {
+  dep_wait();
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int q = blockIdx.y * blockDim.y + threadIdx.y;
+  const int qk = blockIdx.z;
+  if (p >= np_i || q >= np_j || qk >= np_k) return;
+  typedef Ar<float> A;
+  const int nh = gf.nh;
+  const int i = nh + 1 + 2 * p, j = nh + 1 + 2 * q, k = nh + 1 + 2 * qk;
+  const long long c1 = gc.n1, c2 = gc.n2, f1 = gf.n1, f2 = gf.n2;
+  const long long C = lin(gc, f2c(i, nh), f2c(j, nh), f2c(k, nh)), F = lin(gf, i, j, k);
+  // xs[dk][d]: plane C + (dk-1)*c2, offsets d = W, E, S, N, SW, SE, NW, NE
+  const long long off[8] = {-1, 1, -c1, c1, -1 - c1, 1 - c1, -1 + c1, 1 + c1};
+  float xs[3][8];
+#pragma unroll
+  for (int dk = 0; dk < 3; ++dk)
+#pragma unroll
+    for (int d = 0; d < 8; ++d) xs[dk][d] = ld_nc_ordered(x + C + (dk - 1) * c2 + off[d]);
+  const float x0 = ld_nc_ordered(x + C);
+  float cf[8], xo[8];
+#pragma unroll
+  for (int t = 0; t < 8; ++t) {  // child t: di = t & 1, dj = (t >> 1) & 1, dk = t >> 2
+    const long long Fi = F + (t & 1) + ((t >> 1) & 1) * f1 + (t >> 2) * f2;
+    cf[t] = ld_nc_ordered(coef + Fi);
+    xo[t] = ASSIGN ? 0.f : ld_ordered(xf + Fi);
+  }
+  const float x28 = A::mul(x0, 28.f);
+#pragma unroll
+  for (int dj = 0; dj <= 1; ++dj)
+#pragma unroll
+    for (int di = 0; di <= 1; ++di) {
+      const int dI = di, dJ = 2 + dj, dIJ = 4 + di + 2 * dj;  // W/E, S/N, the corner
+      auto sq = [&](int pl) { return A::add(A::mul(3.f, A::add(xs[pl][dI], xs[pl][dJ])), xs[pl][dIJ]); };
+      const float a = sq(0);
+      const float bb = A::mul(sq(1), 3.f);
+      const float c = sq(2);
+      const int t0 = di + 2 * dj, t1 = t0 + 4;
+      const long long F0 = F + di + dj * f1, F1 = F0 + f2;
+      xf[F0] = A::add(xo[t0], A::mul(cf[t0], A::add(A::add(bb, a), x28)));
+      xf[F1] = A::add(xo[t1], A::mul(cf[t1], A::add(A::add(bb, c), x28)));
+    }
+}
+
 // ------------------------------------------------------------------- halo
 // fill! for :xperio (src/halo.jl:6-9). One thread per (j,k) line copies the
 // nh columns through registers, so the copies of each statement read
@@ -575,6 +641,15 @@ void launch_prolong(int kind, T* xf, const T* xc, const T* Pcoef, const Geom& gf
   if (np_i <= 0 || np_j <= 0 || np_k <= 0) return;
   dim3 blk(64, 4, 1);
   dim3 grid((unsigned)((np_i + 63) / 64), (unsigned)((np_j + 3) / 4), (unsigned)np_k);
+  if (sizeof(T) == 4 && kind == 1) {
+    if (assign)
+      launch_dep(k_prolong3c_f<true>, grid, blk, 0, s, (float*)xf, (const float*)xc, (const float*)Pcoef, gf, gc, np_i,
+                 np_j, np_k);
+    else
+      launch_dep(k_prolong3c_f<false>, grid, blk, 0, s, (float*)xf, (const float*)xc, (const float*)Pcoef, gf, gc,
+                 np_i, np_j, np_k);
+    return;
+  }
 #define CFMG_PRO(K)                                                                                       \
   case K:                                                                                                 \
     if (assign)                                                                                           \
