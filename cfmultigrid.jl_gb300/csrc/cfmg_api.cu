@@ -71,6 +71,7 @@ struct cfmg_handle {
   // (k_resid3d.cu, CFMG_OPT_STAGED_RESIDUAL); r3_ran once that pass ran
   int8_t* dqp = nullptr;
   bool r3_on = true, r3_ran = false;
+  int r3_rows = 2;  // rows of its tile per thread (1 or 2)
   // mixed V-cycle, 3D 7-point: level 1's FP32 x is not zeroed before the
   // cycle; its first sweep reads it as +0 instead (x1_zero_ok)
   bool x1_zero = false;
@@ -1187,7 +1188,7 @@ int fused_residual(cfmg_handle* h) {
       float* r32 = h->d.cycle == CFMG_CYCLE_F ? l1.r32 : nullptr;
       const bool r3 = kind == OPK_RESID7 && h->r3_on &&
                       launch_resid_int3d(l1.x, l1.b, h->dqp, g, bx, h->dscal, l1.b32, r32, neumann, h->partials,
-                                         h->stream);
+                                         h->stream, h->r3_rows);
       h->r3_ran |= r3;
       if (!r3 && !launch_resid_int2d(kind, l1.x, l1.b, h->dq, g, bx, h->dscal, l1.b32, r32, neumann, h->partials,
                                      h->stream))
@@ -2693,6 +2694,7 @@ int cfmg_set_option(cfmg_handle* h, int option, long long value) {
   }
   if (option == CFMG_OPT_STAGED_RESIDUAL) {
     h->r3_on = value != 0;
+    h->r3_rows = value == 1 ? 1 : 2;
     drop_graphs(h);
     return CFMG_OK;
   }

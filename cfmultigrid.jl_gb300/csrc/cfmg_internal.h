@@ -374,7 +374,8 @@ bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t
 int dq_pitch(int tx);
 void launch_pad_dq(const int8_t* dq, int8_t* dqp, int tx, int txp, long long rows, cudaStream_t s);
 bool launch_resid_int3d(const double* x, const double* b, const int8_t* dqp, const Geom& g, const Box& bx,
-                        double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s);
+                        double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s,
+                        int rows_per_thread);
 void launch_rhs32_shift(const uint8_t* m, const double* mean_scale, float* b32, float* r32, long long n,
                         cudaStream_t s);
 void launch_make_dq(const double* diag, const uint8_t* m, double Q, int8_t* dq, long long n, int* ok, cudaStream_t s);

@@ -6,17 +6,18 @@
 // loads the x of the planes below and above each row separately: every x is
 // read three times and converted three times, and its warps, waiting on
 // those loads with few bytes in flight, ran at 2.3 TB/s. Here a block owns a
-// 32 x 8 column tile of the interior box and marches along k through a run
-// of kt planes. One thread issues each plane's loads as TMA copies
-// (cp.async.bulk.tensor) into a ring of kR3Stages shared-memory stages that
-// complete on mbarriers: x with a one-cell halo in i and j (a 36 x 10 box of
-// doubles starting on an even column), b (34 x 8 doubles) and dq (48 x 8
-// bytes from a copy whose rows are padded to a multiple of 16 bytes). The
-// threads convert each x of a plane once (their own cell, and one halo cell
-// for 84 of them) into a ring of three converted planes; the residual at
-// plane k takes its four in-plane neighbours from converted plane k and its
+// 32 x 16 column tile of the interior box (two rows a thread; 32 x 8 with
+// one row a thread as an option) and marches along k through a run of kt
+// planes. One thread issues each plane's loads as TMA copies
+// (cp.async.bulk.tensor) into a ring of shared-memory stages that complete
+// on mbarriers: x with a one-cell halo in i and j (a 36 x 18 box of doubles
+// starting on an even column), b (34 x 16 doubles) and dq (48 x 16 bytes
+// from a copy whose rows are padded to a multiple of 16 bytes). The threads
+// convert each x of a plane once (their own cells, and one halo cell for
+// 100 of them) into a ring of three converted planes; the residual at plane
+// k takes its four in-plane neighbours from converted plane k and its
 // k -/+ 1 neighbours from the thread's registers. The loads of the next
-// kR3Stages - 1 planes are in flight while a plane is computed, without
+// planes of the ring are in flight while a plane is computed, without
 // registers held for them, and every x comes from DRAM about once.
 //
 // Per cell the arithmetic is the strip form's: the same exact integer R, the
@@ -38,24 +39,31 @@
 namespace cfmg {
 namespace {
 
-constexpr int kR3TI = 32, kR3TJ = 8;          // column tile: 32 cells in i, 8 in j (one per thread)
-constexpr int kR3Stages = 4;                  // planes in the TMA ring
-constexpr int kR3XW = 36, kR3XH = 10;         // x box (halo of one cell, even first column)
-constexpr int kR3BW = 34;                     // b box (even first column)
-constexpr int kR3DW = 48;                     // dq box (first column a multiple of 16)
-constexpr int kR3PW = 34, kR3PH = 10;         // converted plane: tile + halo
-constexpr int kR3Halo = 2 * kR3PW + 2 * kR3TJ;  // 84 halo cells
-constexpr int kR3XBytes = kR3XW * kR3XH * 8;  // 2880
-constexpr int kR3BBytes = kR3BW * kR3TJ * 8;  // 2176
-constexpr int kR3DBytes = kR3DW * kR3TJ;      // 384
-constexpr int kR3XSlot = 2944;                // x box rounded up to 128 bytes
-constexpr int kR3StageBytes = kR3XSlot + kR3BBytes + kR3DBytes;  // 5504
-constexpr int kR3PBytes = kR3PW * kR3PH * 8;
-constexpr int kR3Smem = kR3Stages * kR3StageBytes + 3 * kR3PBytes + kR3Stages * 8;
-static_assert(kR3TI * kR3TJ == kMxThreads, "one thread per cell of the tile");
-static_assert(kR3Halo <= kMxThreads, "a halo cell per thread at most");
-static_assert(kR3XSlot >= kR3XBytes && kR3XSlot % 128 == 0 && kR3BBytes % 128 == 0 && kR3DBytes % 128 == 0,
-              "TMA destinations on 128-byte boundaries");
+// JT rows of the tile per thread: a 32 x 8*JT column tile, 256 threads.
+// JT = 2 halves the barriers, mbarrier waits and TMA issues per cell and
+// converts fewer halo cells (100 for 512 cells against 84 for 256).
+template <int JT>
+struct R3Cfg {
+  static constexpr int TI = 32, TJ = 8 * JT;   // column tile
+  static constexpr int Stages = JT == 1 ? 4 : 3;  // planes in the TMA ring
+  static constexpr int XW = 36, XH = TJ + 2;   // x box (halo of one cell, even first column)
+  static constexpr int BW = 34;                // b box (even first column)
+  static constexpr int DW = 48;                // dq box (first column a multiple of 16)
+  static constexpr int PW = 34, PH = TJ + 2;   // converted plane: tile + halo
+  static constexpr int Halo = 2 * PW + 2 * TJ;
+  static constexpr int XBytes = XW * XH * 8;
+  static constexpr int BBytes = BW * TJ * 8;
+  static constexpr int DBytes = DW * TJ;
+  static constexpr int XSlot = (XBytes + 127) / 128 * 128;  // x box rounded up to 128 bytes
+  static constexpr int StageBytes = XSlot + BBytes + DBytes;
+  static constexpr int PBytes = PW * PH * 8;
+  static constexpr int Smem = Stages * StageBytes + 3 * PBytes + Stages * 8;
+  static_assert(TI * 8 == kMxThreads, "a thread per column of the tile, JT rows each");
+  static_assert(Halo <= kMxThreads, "a halo cell per thread at most");
+  static_assert(BBytes % 128 == 0 && DBytes % 128 == 0, "TMA destinations on 128-byte boundaries");
+};
+
+int dq_pitch_of(int tx) { return (tx + 15) & ~15; }
 
 struct R3Space {
   int c0, r0, p0;    // 0-based column, row and plane of the box's first cell
@@ -104,30 +112,32 @@ __device__ __forceinline__ void tma3(unsigned dst, const CUtensorMap* map, int c
 struct R3Task {
   int c0t, r0t, ka, np;  // first column and row of the tile, first plane, planes streamed (kt + 2 at most)
 };
+template <int JT>
 __device__ __forceinline__ R3Task r3_task(const R3Space& sp, int T) {
   R3Task t;
   const int tI = T % sp.nti, rest = T / sp.nti;
   const int tJ = rest % sp.ntj, kc = rest / sp.ntj;
-  t.c0t = sp.c0 + kR3TI * tI;
-  t.r0t = sp.r0 + kR3TJ * tJ;
+  t.c0t = sp.c0 + R3Cfg<JT>::TI * tI;
+  t.r0t = sp.r0 + R3Cfg<JT>::TJ * tJ;
   t.ka = sp.p0 + kc * sp.kt;
   const int kb = min(t.ka + sp.kt, sp.p0 + sp.nk);
   t.np = kb - t.ka + 2;  // planes ka-1 .. kb
   return t;
 }
 
-template <bool NEUMANN>
+template <int JT, bool NEUMANN>
 __global__ void __launch_bounds__(kMxThreads) k_resid_int3d(const __grid_constant__ CUtensorMap mx,
                                                             const __grid_constant__ CUtensorMap mb,
                                                             const __grid_constant__ CUtensorMap md, R3Space sp,
                                                             double* ds, float* __restrict__ b32,
                                                             float* __restrict__ r32, double* __restrict__ partials) {
+  typedef R3Cfg<JT> G;
   extern __shared__ __align__(128) unsigned char smem[];
-  long long* pring = reinterpret_cast<long long*>(smem + kR3Stages * kR3StageBytes);
-  unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + kR3Stages * kR3StageBytes + 3 * kR3PBytes);
-  const int tid = threadIdx.x, ti = tid & 31, tj = tid >> 5;
+  long long* pring = reinterpret_cast<long long*>(smem + G::Stages * G::StageBytes);
+  unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + G::Stages * G::StageBytes + 3 * G::PBytes);
+  const int tid = threadIdx.x, ti = tid & 31, tj = tid >> 5;  // own cells: rows tj + 8u, u < JT
   if (tid == 0) {
-    for (int s = 0; s < kR3Stages; ++s)
+    for (int s = 0; s < G::Stages; ++s)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bars + s)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<unsigned long long>(&mx)) : "memory");
@@ -145,76 +155,87 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int3d(const __grid_constan
   // issue cursor (thread 0): the block's sequence of (task, plane) in order
   int iT = blockIdx.x, iq = 0;
   unsigned long long in = 0;
-  R3Task it = r3_task(sp, iT);
+  R3Task it = r3_task<JT>(sp, iT);
   auto issue_next = [&]() {
     if (iT >= ntasks) return;
-    const int s = (int)(in % kR3Stages);
+    const int s = (int)(in % G::Stages);
     const unsigned bar = smem_u32(bars + s);
-    unsigned char* st = smem + s * kR3StageBytes;
+    unsigned char* st = smem + s * G::StageBytes;
     const bool full = iq >= 1 && iq <= it.np - 2;  // b and dq for planes ka .. kb-1 only
-    const unsigned bytes = kR3XBytes + (full ? kR3BBytes + kR3DBytes : 0);
+    const unsigned bytes = G::XBytes + (full ? G::BBytes + G::DBytes : 0);
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
     const int p = it.ka - 1 + iq;
     tma3(smem_u32(st), &mx, (it.c0t - 1) & ~1, it.r0t - 1, p, bar);
     if (full) {
-      tma3(smem_u32(st + kR3XSlot), &mb, it.c0t & ~1, it.r0t, p, bar);
-      tma3(smem_u32(st + kR3XSlot + kR3BBytes), &md, it.c0t & ~15, it.r0t, p, bar);
+      tma3(smem_u32(st + G::XSlot), &mb, it.c0t & ~1, it.r0t, p, bar);
+      tma3(smem_u32(st + G::XSlot + G::BBytes), &md, it.c0t & ~15, it.r0t, p, bar);
     }
     ++in;
     if (++iq == it.np) {
       iT += gridDim.x;
       iq = 0;
-      if (iT < ntasks) it = r3_task(sp, iT);
+      if (iT < ntasks) it = r3_task<JT>(sp, iT);
     }
   };
   if (tid == 0)
-    for (int s = 0; s < kR3Stages; ++s) issue_next();
+    for (int s = 0; s < G::Stages; ++s) issue_next();
 
-  // this thread's halo cell (tid < 84): its place in the converted plane
+  // this thread's halo cell (tid < Halo): its place in the converted plane
   int hp = -1, hx = 0;  // index in the converted plane, and in the x box without the column offset
-  if (tid < kR3Halo) {
+  if (tid < G::Halo) {
     int hr, hc;
-    if (tid < kR3PW) {
+    if (tid < G::PW) {
       hr = 0;
       hc = tid;
-    } else if (tid < 2 * kR3PW) {
-      hr = kR3PH - 1;
-      hc = tid - kR3PW;
+    } else if (tid < 2 * G::PW) {
+      hr = G::PH - 1;
+      hc = tid - G::PW;
     } else {
-      const int h = tid - 2 * kR3PW;
+      const int h = tid - 2 * G::PW;
       hr = 1 + (h >> 1);
-      hc = (h & 1) ? kR3PW - 1 : 0;
+      hc = (h & 1) ? G::PW - 1 : 0;
     }
-    hp = hr * kR3PW + hc;
-    hx = hr * kR3XW + hc;
+    hp = hr * G::PW + hc;
+    hx = hr * G::XW + hc;
   }
-  const int op = (tj + 1) * kR3PW + ti + 1;  // own cell in the converted plane
-  float hi = 0.f, lo = 0.f;                  // double-float sum of f^2
+  float hi = 0.f, lo = 0.f;  // double-float sum of f^2
   __int128 s1 = 0;
   unsigned long long n = 0;  // planes consumed
   bool fault = false;
   for (int T = blockIdx.x; T < ntasks && !fault; T += gridDim.x) {
-    const R3Task t = r3_task(sp, T);
+    const R3Task t = r3_task<JT>(sp, T);
     const int ox = (t.c0t - 1) - ((t.c0t - 1) & ~1), ob = t.c0t - (t.c0t & ~1), od = t.c0t - (t.c0t & ~15);
-    const int col = t.c0t + ti, row = t.r0t + tj;
-    const bool own = col < sp.c0 + sp.ni && row < sp.r0 + sp.nj;
-    long long Cm = 0, Cc = 0, Bp = 0;
-    int dp = -1;
+    const int col = t.c0t + ti;
+    bool own[JT];
+    long long Cm[JT], Cc[JT], Bp[JT];
+    int dp[JT];
+#pragma unroll
+    for (int u = 0; u < JT; ++u) {
+      own[u] = col < sp.c0 + sp.ni && t.r0t + tj + 8 * u < sp.r0 + sp.nj;
+      Cm[u] = Cc[u] = Bp[u] = 0;
+      dp[u] = -1;
+    }
     for (int qq = 0; qq < t.np; ++qq, ++n) {
-      const int s = (int)(n % kR3Stages);
-      const bool ok = mbar_wait(smem_u32(bars + s), (unsigned)((n / kR3Stages) & 1));
-      const unsigned char* st = smem + s * kR3StageBytes;
+      const int s = (int)(n % G::Stages);
+      const bool ok = mbar_wait(smem_u32(bars + s), (unsigned)((n / G::Stages) & 1));
+      const unsigned char* st = smem + s * G::StageBytes;
       const double* xs = reinterpret_cast<const double*>(st);
-      long long* P = pring + (qq % 3) * (kR3PW * kR3PH);
-      const long long Cn = to_fix(xs[(tj + 1) * kR3XW + ti + 1 + ox], k);
-      P[op] = Cn;
-      if (hp >= 0) P[hp] = to_fix(xs[hx + ox], k);
-      long long Bn = 0;
-      int dn = -1;
-      if (qq >= 1 && qq <= t.np - 2) {
-        Bn = to_fix(reinterpret_cast<const double*>(st + kR3XSlot)[tj * kR3BW + ti + ob], k);
-        dn = (int)reinterpret_cast<const signed char*>(st + kR3XSlot + kR3BBytes)[tj * kR3DW + ti + od];
+      long long* P = pring + (qq % 3) * (G::PW * G::PH);
+      long long Cn[JT], Bn[JT];
+      int dn[JT];
+#pragma unroll
+      for (int u = 0; u < JT; ++u) {
+        const int r = tj + 8 * u;
+        Cn[u] = to_fix(xs[(r + 1) * G::XW + ti + 1 + ox], k);
+        P[(r + 1) * G::PW + ti + 1] = Cn[u];
+        Bn[u] = 0;
+        dn[u] = -1;
+        if (qq >= 1 && qq <= t.np - 2) {
+          Bn[u] = to_fix(reinterpret_cast<const double*>(st + G::XSlot)[r * G::BW + ti + ob], k);
+          dn[u] = (int)reinterpret_cast<const signed char*>(st + G::XSlot + G::BBytes)[r * G::DW + ti + od];
+        }
       }
+      if (hp >= 0) P[hp] = to_fix(xs[hx + ox], k);
       // the plane is converted and its stage free again; one thread refills it
       if (__syncthreads_or(!ok)) {
         fault = true;
@@ -225,34 +246,42 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int3d(const __grid_constan
         issue_next();
       }
       if (qq >= 2) {  // plane m = ka + qq - 2 from converted plane m and own C(m-1), C(m), C(m+1)
-        const long long* Pc = pring + ((qq - 1) % 3) * (kR3PW * kR3PH);
-        long long R = (long long)dp * Cc + Bp -
-                      (Pc[op - 1] + Pc[op + 1] + Pc[op - kR3PW] + Pc[op + kR3PW] + Cm + Cn);
-        R = (own && dp >= 0) ? R : 0LL;  // dry cells and cells outside the box
-        const float f = __fmul_rn(__ll2float_rn(R), fm);
-        if (own) {
-          const long long I = (long long)col + sp.n1 * row + sp.n2 * (t.ka + qq - 2);
-          b32[I] = f;
-          if (!NEUMANN && r32) r32[I] = f;
+        const long long* Pc = pring + ((qq - 1) % 3) * (G::PW * G::PH);
+#pragma unroll
+        for (int u = 0; u < JT; ++u) {
+          const int row = t.r0t + tj + 8 * u;
+          const int op = (tj + 8 * u + 1) * G::PW + ti + 1;
+          long long R = (long long)dp[u] * Cc[u] + Bp[u] -
+                        (Pc[op - 1] + Pc[op + 1] + Pc[op - G::PW] + Pc[op + G::PW] + Cm[u] + Cn[u]);
+          R = (own[u] && dp[u] >= 0) ? R : 0LL;  // dry cells and cells outside the box
+          const float f = __fmul_rn(__ll2float_rn(R), fm);
+          if (own[u]) {
+            const long long I = (long long)col + sp.n1 * row + sp.n2 * (t.ka + qq - 2);
+            b32[I] = f;
+            if (!NEUMANN && r32) r32[I] = f;
+          }
+          if (NEUMANN) s1 += (__int128)R;
+          // p + e = f^2 exactly; (hi, lo) += p + e by TwoSum (explicit _rn operations)
+          const float pp = __fmul_rn(f, f), e = __fmaf_rn(f, f, -pp);
+          const float sn = __fadd_rn(hi, pp), bp = __fsub_rn(sn, hi);
+          lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(__fsub_rn(hi, __fsub_rn(sn, bp)), __fsub_rn(pp, bp)), e));
+          hi = sn;
         }
-        if (NEUMANN) s1 += (__int128)R;
-        // p + e = f^2 exactly; (hi, lo) += p + e by TwoSum (explicit _rn operations)
-        const float pp = __fmul_rn(f, f), e = __fmaf_rn(f, f, -pp);
-        const float sn = __fadd_rn(hi, pp), bp = __fsub_rn(sn, hi);
-        lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(__fsub_rn(hi, __fsub_rn(sn, bp)), __fsub_rn(pp, bp)), e));
-        hi = sn;
       }
-      Cm = Cc;
-      Cc = Cn;
-      Bp = Bn;
-      dp = dn;
+#pragma unroll
+      for (int u = 0; u < JT; ++u) {
+        Cm[u] = Cc[u];
+        Cc[u] = Cn[u];
+        Bp[u] = Bn[u];
+        dp[u] = dn[u];
+      }
     }
     __syncthreads();  // the converted-plane ring is reused by the next task
   }
   if (fault) {  // block-uniform (__syncthreads_or): drain the copies in flight, then report
     if (tid == 0) {
       for (unsigned long long m = n; m < in; ++m)
-        if (!mbar_wait(smem_u32(bars + (m % kR3Stages)), (unsigned)((m / kR3Stages) & 1))) break;
+        if (!mbar_wait(smem_u32(bars + (m % G::Stages)), (unsigned)((m / G::Stages) & 1))) break;
       ds[S_FAULT] = 1.0;
       partials[blockIdx.x] = __longlong_as_double(0x7ff8000000000000LL);
       partials[kMxParts + blockIdx.x] = __longlong_as_double(0x7ff8000000000000LL);
@@ -333,33 +362,25 @@ bool encode3(CUtensorMap* m, CUtensorMapDataType dt, int esize, const void* base
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <bool NEUMANN>
+template <int JT, bool NEUMANN>
 int r3_grid() {
   static int blocks = 0;  // one wave: resident blocks per SM x SMs, at most kMxParts
   if (!blocks) {
     int dev = 0, nsm = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_resid_int3d<NEUMANN>, kMxThreads, kR3Smem);
+    cudaFuncSetAttribute(k_resid_int3d<JT, NEUMANN>, cudaFuncAttributeMaxDynamicSharedMemorySize, R3Cfg<JT>::Smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_resid_int3d<JT, NEUMANN>, kMxThreads, R3Cfg<JT>::Smem);
     blocks = nsm * (per > 0 ? per : 1);
     if (blocks > kMxParts || blocks <= 0) blocks = kMxParts;
   }
   return blocks;
 }
 
-}  // namespace
-
-int dq_pitch(int tx) { return (tx + 15) & ~15; }
-
-void launch_pad_dq(const int8_t* dq, int8_t* dqp, int tx, int txp, long long rows, cudaStream_t s) {
-  const long long n = rows * txp;
-  k_pad_dq<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dq, dqp, tx, txp, rows);
-}
-
-bool launch_resid_int3d(const double* x, const double* b, const int8_t* dqp, const Geom& g, const Box& bx,
-                        double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s) {
-  // TMA: global addresses on 16 bytes, row and plane pitches multiples of 16 bytes
-  if (!dqp || g.tx % 2 != 0 || ((uintptr_t)x | (uintptr_t)b | (uintptr_t)dqp) % 16 != 0) return false;
+template <int JT>
+bool launch_r3(const double* x, const double* b, const int8_t* dqp, const Geom& g, const Box& bx, double* ds,
+               float* b32, float* r32, bool neumann, double* partials, cudaStream_t s) {
+  typedef R3Cfg<JT> G;
   R3Space sp;
   sp.c0 = bx.i0 - 1;
   sp.r0 = bx.j0 - 1;
@@ -369,17 +390,17 @@ bool launch_resid_int3d(const double* x, const double* b, const int8_t* dqp, con
   sp.nk = bx.k1 - bx.k0 + 1;
   // the boxes start at column c0t-1 >= 0, row r0t-1 >= 0 and plane ka-1 >= 0
   if (sp.ni <= 0 || sp.nj <= 0 || sp.nk <= 0 || sp.c0 < 1 || sp.r0 < 1 || sp.p0 < 1) return false;
-  sp.nti = (sp.ni + kR3TI - 1) / kR3TI;
-  sp.ntj = (sp.nj + kR3TJ - 1) / kR3TJ;
+  sp.nti = (sp.ni + G::TI - 1) / G::TI;
+  sp.ntj = (sp.nj + G::TJ - 1) / G::TJ;
   sp.n1 = g.n1;
   sp.n2 = g.n2;
   CUtensorMap mx, mb, md;
-  const int txp = dq_pitch(g.tx);
-  if (!encode3(&mx, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, x, g.tx, g.tx, g.ty, g.tz, kR3XW, kR3XH) ||
-      !encode3(&mb, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, b, g.tx, g.tx, g.ty, g.tz, kR3BW, kR3TJ) ||
-      !encode3(&md, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, dqp, txp, txp, g.ty, g.tz, kR3DW, kR3TJ))
+  const int txp = dq_pitch_of(g.tx);
+  if (!encode3(&mx, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, x, g.tx, g.tx, g.ty, g.tz, G::XW, G::XH) ||
+      !encode3(&mb, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, b, g.tx, g.tx, g.ty, g.tz, G::BW, G::TJ) ||
+      !encode3(&md, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, dqp, txp, txp, g.ty, g.tz, G::DW, G::TJ))
     return false;
-  const int grid = neumann ? r3_grid<true>() : r3_grid<false>();
+  const int grid = neumann ? r3_grid<JT, true>() : r3_grid<JT, false>();
   // about 8 tasks per block: runs of kt planes (each streams kt + 2)
   const long long cols = (long long)sp.nti * sp.ntj;
   long long kt = (sp.nk * cols + 8LL * grid - 1) / (8LL * grid);
@@ -387,10 +408,28 @@ bool launch_resid_int3d(const double* x, const double* b, const int8_t* dqp, con
   sp.kt = (int)(kt > sp.nk ? sp.nk : kt);
   sp.nkc = (sp.nk + sp.kt - 1) / sp.kt;
   if (neumann)
-    launch_dep(k_resid_int3d<true>, grid, kMxThreads, kR3Smem, s, mx, mb, md, sp, ds, b32, r32, partials);
+    launch_dep(k_resid_int3d<JT, true>, grid, kMxThreads, G::Smem, s, mx, mb, md, sp, ds, b32, r32, partials);
   else
-    launch_dep(k_resid_int3d<false>, grid, kMxThreads, kR3Smem, s, mx, mb, md, sp, ds, b32, r32, partials);
+    launch_dep(k_resid_int3d<JT, false>, grid, kMxThreads, G::Smem, s, mx, mb, md, sp, ds, b32, r32, partials);
   return true;
+}
+
+}  // namespace
+
+int dq_pitch(int tx) { return dq_pitch_of(tx); }
+
+void launch_pad_dq(const int8_t* dq, int8_t* dqp, int tx, int txp, long long rows, cudaStream_t s) {
+  const long long n = rows * txp;
+  k_pad_dq<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dq, dqp, tx, txp, rows);
+}
+
+bool launch_resid_int3d(const double* x, const double* b, const int8_t* dqp, const Geom& g, const Box& bx,
+                        double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s,
+                        int rows_per_thread) {
+  // TMA: global addresses on 16 bytes, row and plane pitches multiples of 16 bytes
+  if (!dqp || g.tx % 2 != 0 || ((uintptr_t)x | (uintptr_t)b | (uintptr_t)dqp) % 16 != 0) return false;
+  if (rows_per_thread == 2) return launch_r3<2>(x, b, dqp, g, bx, ds, b32, r32, neumann, partials, s);
+  return launch_r3<1>(x, b, dqp, g, bx, ds, b32, r32, neumann, partials, s);
 }
 
 }  // namespace cfmg

@@ -131,11 +131,12 @@ extern "C" {
                                    read omega*idiag as a one-byte code diag into a 256-entry table (when
                                    every cell's code reproduces its float exactly) instead of a 4-byte
                                    float per cell; 0 the floats. Both give the same bits. */
-#define CFMG_OPT_STAGED_RESIDUAL 9 /* mixed form, 3D 7-point operator, integer residual: 1 (default) the
-                                      level-1 residual pass stages each plane of a 32 x 8 column tile in
-                                      shared memory by TMA and converts every x once (even tx only); 0 the
-                                      row-strip pass. The same residual and right-hand side; the norm's
-                                      partial sums are added in another order. */
+#define CFMG_OPT_STAGED_RESIDUAL 9 /* mixed form, 3D 7-point operator, integer residual: 2 (default) the
+                                      level-1 residual pass stages each plane of a 32 x 16 column tile in
+                                      shared memory by TMA and converts every x once (even tx only), two
+                                      tile rows a thread; 1 the same with 32 x 8 tiles, one row a thread;
+                                      0 the row-strip pass. The same residual and right-hand side; the
+                                      norm's partial sums are added in another order. */
 
 typedef struct cfmg_desc {
   int kase;     /* CFMG_TWOD / CFMG_THREED            (Param.case) */

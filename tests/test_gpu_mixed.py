@@ -231,7 +231,7 @@ def test_staged_residual_matches_strip_residual(name):
     bit."""
     base, mkind = CASES[name]
     out = {}
-    for on in (1, 0):
+    for on in (1, 2, 0):  # one and two tile rows per thread; the strip pass
         mg = cfmg.get_gmg(cfmg.Param(**base, tol=1e-10, maxite=40, residual_norm="l2", precision="mixed",
                                      verbose=False))
         msk = mg.download(1, "msk")
@@ -241,17 +241,19 @@ def test_staged_residual_matches_strip_residual(name):
         mg.set_option("staged_residual", on)
         res, n, hist = cfmg.solve(mg, history=True)
         out[on] = (res, n, hist, mg.data[1].x, msk.astype(bool), mg.shape(1)[0])
-    (r1, n1, h1, x1, w, tx), (r0, n0, h0, x0, _, _) = out[1], out[0]
-    assert r1 <= 1e-10 and r0 <= 1e-10 and n1 == n0, (r1, r0, n1, n0)
-    if tx % 2:
-        assert np.array_equal(h1, h0) and np.array_equal(x1, x0)
-        return
-    np.testing.assert_allclose(h1[0], h0[0], rtol=1e-13)
-    np.testing.assert_allclose(h1, h0, rtol=1e-6)
-    singular = base.get("location", "centers") == "centers"
-    a = _wet_mean_removed(x1, w) if singular else x1 * w
-    c = _wet_mean_removed(x0, w) if singular else x0 * w
-    assert np.linalg.norm(a - c) <= 1e-8 * np.linalg.norm(c)
+    r0, n0, h0, x0, w, tx = out[0]
+    for on in (1, 2):
+        r1, n1, h1, x1, _, _ = out[on]
+        assert r1 <= 1e-10 and r0 <= 1e-10 and n1 == n0, (on, r1, r0, n1, n0)
+        if tx % 2:
+            assert np.array_equal(h1, h0) and np.array_equal(x1, x0)
+            continue
+        np.testing.assert_allclose(h1[0], h0[0], rtol=1e-13)
+        np.testing.assert_allclose(h1, h0, rtol=1e-6)
+        singular = base.get("location", "centers") == "centers"
+        a = _wet_mean_removed(x1, w) if singular else x1 * w
+        c = _wet_mean_removed(x0, w) if singular else x0 * w
+        assert np.linalg.norm(a - c) <= 1e-8 * np.linalg.norm(c)
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
