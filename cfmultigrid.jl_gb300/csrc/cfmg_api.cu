@@ -75,6 +75,9 @@ struct cfmg_handle {
   // mixed V-cycle, 3D 7-point: level 1's FP32 x is not zeroed before the
   // cycle; its first sweep reads it as +0 instead (x1_zero_ok)
   bool x1_zero = false;
+  // CFMG_OPT_SKIP_DRY: 3D mixed passes skip groups of dry cells (their FP32
+  // fields hold +0 and stay +0)
+  bool dry_on = true;
   bool host_loop = false;  // CFMG_OPT_HOST_LOOP
   // call order: the operators' coefficients exist once cfmg_setup_operators,
   // cfmg_bind_level or an upload of a coefficient field ran; cfmg_adjoint
@@ -380,6 +383,7 @@ int sweep(cfmg_handle* h, int lev, int kind, const T* x, T* y, const Box* bx, bo
     op.wq = l.wq;
     op.wtab = h->wtab;
     op.assign = x_zero ? 1 : 0;
+    op.qact = h->dry_on ? l.qact : nullptr;
   }
   op.cff = 1.0 - h->d.omega;
   if (bx) {
@@ -627,6 +631,7 @@ int prolong_t(cfmg_handle* h, int lev, bool onto_zero = false) {
     np_k = f.kc1 - f.kc0 + 1;
   }
   op.n = (long long)op.np_i * op.np_j * np_k;
+  if (sizeof(T) == 4 && kind == 1 && h->dry_on) op.m = f.msk;  // parents of eight dry cells are skipped
   if (onto_zero) {
     if (!h->record && !(h->engine_on && (long long)f.len <= engine_limit(h, pc<T>()))) op.assign = 1;
     else TRY(zero_t<T>(h, lev, CFMG_X));
@@ -995,7 +1000,15 @@ int prepare_wq(cfmg_handle* h) {
   const int one = 1;
   CUDA_OK(h, cudaMemcpyAsync(ok, &one, sizeof(int), cudaMemcpyHostToDevice, h->stream));
   launch_wq_table(h->wtab, h->d.omega, Q, h->stream);
-  for (Level& l : h->lv) launch_make_wq(l.diag, l.widiag32, h->wtab, Q, l.wq, (long long)l.len, ok, h->stream);
+  for (Level& l : h->lv) {
+    launch_make_wq(l.diag, l.widiag32, h->wtab, Q, l.wq, (long long)l.len, ok, h->stream);
+    // four-cell 3D sweep: which (run of planes, quad) holds a wet cell
+    if (l.threed && l.tz >= 3 && ((long long)l.tx * l.ty) % 4 == 0) {
+      const long long nq = ((long long)l.tx * l.ty) / 4, nruns = (l.tz - 2 + kQRunPlanes - 1) / kQRunPlanes;
+      if (!l.qact) CUDA_OK(h, cudaMalloc((void**)&l.qact, (size_t)(nq * nruns)));
+      launch_make_qact(l.msk, l.qact, (long long)l.tx * l.ty, l.tz, kQRunPlanes, h->stream);
+    }
+  }
   int hok = 0;
   CUDA_OK(h, cudaMemcpyAsync(&hok, ok, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   CUDA_OK(h, cudaStreamSynchronize(h->stream));
@@ -1200,7 +1213,7 @@ int fused_residual(cfmg_handle* h) {
     if (neumann) {
       Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED);
       launch_rhs32_shift(l1.msk, h->dscal + S_MEAN2, l1.b32, h->d.cycle == CFMG_CYCLE_F ? l1.r32 : nullptr,
-                         (long long)l1.len, h->stream);
+                         (long long)l1.len, h->stream, h->dry_on);
     }
     LAUNCH_OK(h);
     return CFMG_OK;
@@ -1264,7 +1277,10 @@ int mixed_iteration(cfmg_handle* h, int kind) {
     if (st != CFMG_OK) return st;
     if (!h->upd_done) {
       Launch k(h, CFMG_K_CONVERT, 1, CFMG_MIXED);
-      if (int_path(h)) launch_update_scaled_max(l1.x, view<float>(l1).x, h->dscal, (long long)l1.len, h->stream);
+      // 3D: groups of dry cells are skipped (S_MAXO holds their max |x|, see cfmg_solve)
+      if (int_path(h))
+        launch_update_scaled_max(l1.x, view<float>(l1).x, h->dscal, (long long)l1.len, h->stream,
+                                 threed(h) && h->dry_on ? l1.msk : nullptr);
       else launch_update_scaled(l1.x, view<float>(l1).x, h->dscal + S_ICUR, (long long)l1.len, h->stream);
     }
     LAUNCH_OK(h);
@@ -1698,6 +1714,8 @@ int cfmg_destroy(cfmg_handle* h) {
     if (p) cudaFree(p);
   if (h->dq) cudaFree(h->dq);
   if (h->dqp) cudaFree(h->dqp);
+  for (Level& l : h->lv)
+    if (l.qact) cudaFree(l.qact);
   if (h->dhist) cudaFree(h->dhist);
   if (h->arena) cudaFree(h->arena);
   if (h->hscal) cudaFreeHost(h->hscal);
@@ -1968,8 +1986,9 @@ int cfmg_solve(cfmg_handle* h, double* res_out, int* nite_out, double* history) 
       // max |x| starts from it (the update in a smoothing pass sees U only)
       CUDA_OK(h, cudaMemsetAsync(h->dscal + S_MAXX, 0, 2 * sizeof(double), h->stream));
       CUDA_OK(h, cudaMemsetAsync(h->dscal + S_MAXO, 0, sizeof(double), h->stream));
+      // 3D with dry cells skipped by the update: S_MAXO is the max |x| of the dry cells
       launch_maxabs2(l1.x, l1.b, (long long)l1.len, l1.tx, l1.ty, l1.nh, l1.nx + l1.nh + 1, l1.nh, l1.ny + l1.nh + 1,
-                     h->dscal, h->stream);
+                     h->dscal, h->stream, threed(h) && h->dry_on ? l1.msk : nullptr);
       h->launches += 1;
     }
     TRY(fused_residual(h));
@@ -2689,6 +2708,11 @@ int cfmg_set_option(cfmg_handle* h, int option, long long value) {
   }
   if (option == CFMG_OPT_FUSED_UPDATE) {
     h->upd_on = value != 0;
+    drop_graphs(h);
+    return CFMG_OK;
+  }
+  if (option == CFMG_OPT_SKIP_DRY) {
+    h->dry_on = value != 0;
     drop_graphs(h);
     return CFMG_OK;
   }

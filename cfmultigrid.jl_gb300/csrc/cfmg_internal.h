@@ -64,6 +64,9 @@ struct Level {
   // 3D 7-point mixed form: the FP32 omega*idiag as a one-byte code c = diag
   // (0: omega*idiag = 0) into the handle's table wtab (prepare_wq, cfmg_api.cu)
   uint8_t* wq;
+  // the same levels, four-cell sweep: 1 for each (run of planes, quad of a
+  // plane) holding a wet cell (launch_make_qact); dry quads are skipped
+  uint8_t* qact;
   int xswap;  // 1: the FP32 x currently lives in y32 (after a temporally blocked smoothing)
   int ic0, ic1, jc0, jc1, kc0, kc1;  // interior box (1-based inclusive)
 };
@@ -97,7 +100,10 @@ void launch_sweep7_3d(const T* x, T* y, const T* b, const T* widiag, T cff, cons
 // x holds +0 in every cell and is not read (four-cell form only, see
 // sweep7_quad_ok)
 void launch_sweep7_3d_q(const float* x, float* y, const float* b, const uint8_t* wq, const float* wtab, float cff,
-                        const Geom& g, cudaStream_t s, bool x_zero = false);
+                        const Geom& g, cudaStream_t s, bool x_zero = false, const uint8_t* qact = nullptr);
+// quad activity flags of a 3D level for the four-cell sweep (runs of kQRunPlanes planes)
+constexpr int kQRunPlanes = 4;
+void launch_make_qact(const uint8_t* m, uint8_t* qact, long long n2, int tz, int run, cudaStream_t s);
 bool sweep7_quad_ok(const Geom& g, const void* x, const void* y, const void* b, const void* wq);
 // FP32 3D 7-point cell-centred residual at the children of the coarse box cb
 // restricted into the coarse b (k_ops.cu); dc: diag as one-byte codes
@@ -137,8 +143,9 @@ void launch_restrict(int kind, const T* xf, T* bc, const T* Rcoef, const Geom& g
 // prolongation: fine x += Pcoef * P(coarse x); same kinds; (nxf, nyf, nzf)
 // are the fine level's nx, ny, nz and [kf0, kf1] its k-range of parents.
 template <class T>
+// fmsk != null (FP32 3D cell-centred only): parents whose eight children are all dry are skipped
 void launch_prolong(int kind, T* xf, const T* xc, const T* Pcoef, const Geom& gf, const Geom& gc, int nxf, int nyf,
-                    int nzf, int kf0, int kf1, bool assign, cudaStream_t s);
+                    int nzf, int kf0, int kf1, bool assign, cudaStream_t s, const uint8_t* fmsk = nullptr);
 template <class T>
 void launch_fill_xperio(T* x, const Geom& g, cudaStream_t s);
 // norm: deterministic sum of msk*x^2 (FP64 accumulation) over the whole
@@ -209,6 +216,7 @@ struct Op {
   // standalone FP32 sweeps: omega*idiag read as wtab[wq[I]] instead of w[I] (same bits)
   const uint8_t* wq;
   const float* wtab;
+  const uint8_t* qact;  // the level's quad activity flags (see Level), or null: every quad swept
 };
 // scalar block of a whole-solve program
 enum SolveSlot { SS_NORMB = 0, SS_NR, SS_RES, SS_NITE, SS_NWET, SS_MEAN, SS_SCALE, SS_ISCALE, SS_T0, SS_T1,
@@ -376,13 +384,17 @@ void launch_pad_dq(const int8_t* dq, int8_t* dqp, int tx, int txp, long long row
 bool launch_resid_int3d(const double* x, const double* b, const int8_t* dqp, const Geom& g, const Box& bx,
                         double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s,
                         int rows_per_thread);
+// skip_dry: groups of 16 dry cells are neither read nor written (their b32 is +0 already)
 void launch_rhs32_shift(const uint8_t* m, const double* mean_scale, float* b32, float* r32, long long n,
-                        cudaStream_t s);
+                        cudaStream_t s, bool skip_dry = false);
 void launch_make_dq(const double* diag, const uint8_t* m, double Q, int8_t* dq, long long n, int* ok, cudaStream_t s);
 // max |x|, max |b| and max |x| outside the box U of every layer (S_MAXX, S_MAXB, S_MAXO)
+// m != null: "outside U" is instead every cell with m == 0 (the dry cells)
 void launch_maxabs2(const double* x, const double* b, long long n, int tx, int ty, int ui0, int ui1, int uj0, int uj1,
-                    double* ds, cudaStream_t s);
-void launch_update_scaled_max(double* x, const float* e, double* ds, long long n, cudaStream_t s);
+                    double* ds, cudaStream_t s, const uint8_t* m = nullptr);
+// msk != null: groups of 4 dry cells (e = +0 there) are skipped; their max |x| must be in S_MAXO
+void launch_update_scaled_max(double* x, const float* e, double* ds, long long n, cudaStream_t s,
+                              const uint8_t* msk = nullptr);
 
 // message returned by cfmg_last_error(NULL) (cfmg_api.cu)
 void set_global_error(const std::string& msg);

@@ -488,6 +488,7 @@ __global__ void k_rhs32_shift(const uint8_t* __restrict__ m, const double* __res
 
 // the same, 16 cells a thread in 16-byte accesses (m, b32, r32 16-byte
 // aligned); the last n % 16 cells by the scalar form in the final thread
+template <bool SKIP>
 __global__ void __launch_bounds__(256) k_rhs32_shift16(const uint8_t* __restrict__ m, const double* __restrict__ ms,
                                                        float* __restrict__ b32, float* __restrict__ r32,
                                                        long long n) {
@@ -505,6 +506,8 @@ __global__ void __launch_bounds__(256) k_rhs32_shift16(const uint8_t* __restrict
     return;
   }
   const uint4 mv = reinterpret_cast<const uint4*>(m)[t];
+  // SKIP: 16 dry cells hold b32 = +0 already (the residual pass writes 0 there)
+  if (SKIP && (mv.x | mv.y | mv.z | mv.w) == 0u) return;
   float4* bp = reinterpret_cast<float4*>(b32) + 4 * t;
   float4 v[4];
 #pragma unroll
@@ -549,7 +552,7 @@ __global__ void k_make_dq(const double* __restrict__ diag, const uint8_t* __rest
 // cells outside the box U = [ui0, ui1] x [uj0, uj1] of every layer (1-based;
 // tx, ty the array's row and plane extents) into ds[S_MAXO]; all start at 0
 __global__ void k_maxabs2(const double* __restrict__ x, const double* __restrict__ b, long long n, int tx, int ty,
-                          int ui0, int ui1, int uj0, int uj1, double* ds) {
+                          int ui0, int ui1, int uj0, int uj1, double* ds, const uint8_t* __restrict__ m) {
   dep_wait();
   unsigned long long mx = 0, mb = 0, mo = 0;
   const long long nrows = n / tx;  // rows of all layers
@@ -561,7 +564,7 @@ __global__ void k_maxabs2(const double* __restrict__ x, const double* __restrict
     for (int i0 = threadIdx.x; i0 < tx; i0 += blockDim.x) {
       const unsigned long long ux = (unsigned long long)__double_as_longlong(xr[i0]) & 0x7FFFFFFFFFFFFFFFULL;
       const unsigned long long ub = (unsigned long long)__double_as_longlong(br[i0]) & 0x7FFFFFFFFFFFFFFFULL;
-      const bool in_u = row_u && i0 + 1 >= ui0 && i0 + 1 <= ui1;
+      const bool in_u = m ? m[row * tx + i0] != 0 : (row_u && i0 + 1 >= ui0 && i0 + 1 <= ui1);
       mx = ux > mx ? ux : mx;
       mb = ub > mb ? ub : mb;
       mo = (!in_u && ux > mo) ? ux : mo;
@@ -626,9 +629,13 @@ __global__ void __launch_bounds__(kMxThreads) k_update_scaled_max(double* __rest
 
 // the same with 16-byte accesses (x and e 16-byte aligned): 4 cells a
 // group, two groups of a thread in flight; the last n % 4 cells by block 0
+//
+// msk (optional): a group of 4 dry cells is skipped (e = +0 there, so x stays
+// as it is up to the sign of a zero); the max |x| of the dry cells, which no
+// update changes, is in S_MAXO, from which S_MAXX starts.
 __global__ void __launch_bounds__(kMxThreads) k_update_scaled_max4(double* __restrict__ x, const float* __restrict__ e,
                                                                    const double* __restrict__ ds, long long n,
-                                                                   double* dsw) {
+                                                                   double* dsw, const uint8_t* __restrict__ msk) {
   dep_wait();
   const double is = ds[S_ICUR];
   const int pe = pow2_exponent(is);  // iscale = 2^pe
@@ -646,10 +653,20 @@ __global__ void __launch_bounds__(kMxThreads) k_update_scaled_max4(double* __res
   for (long long g0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; g0 < ng; g0 += 2 * st) {
     float4 ev[2];
     double2 xa[2], xb[2];
+    bool act[2];
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
       const long long g = g0 + u * st;
-      if (g < ng) {
+      act[u] = g < ng;
+      if (act[u] && msk) {
+        const uchar4 mm = reinterpret_cast<const uchar4*>(msk)[g];
+        act[u] = (mm.x | mm.y | mm.z | mm.w) != 0;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const long long g = g0 + u * st;
+      if (act[u]) {
         ev[u] = e4[g];
         xa[u] = x2[2 * g];
         xb[u] = x2[2 * g + 1];
@@ -658,7 +675,7 @@ __global__ void __launch_bounds__(kMxThreads) k_update_scaled_max4(double* __res
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
       const long long g = g0 + u * st;
-      if (g < ng) {
+      if (act[u]) {
         double2 ra, rb;
         ra.x = upd(xa[u].x, ev[u].x);
         ra.y = upd(xa[u].y, ev[u].y);
@@ -705,11 +722,14 @@ void launch_resid_int(int kind, const double* x, const double* b, const int8_t* 
 }
 
 void launch_rhs32_shift(const uint8_t* m, const double* mean_scale, float* b32, float* r32, long long n,
-                        cudaStream_t s) {
+                        cudaStream_t s, bool skip_dry) {
   const bool a16 = ((uintptr_t)m | (uintptr_t)b32 | (uintptr_t)r32) % 16 == 0;
   if (a16) {
     const long long nt = (n >> 4) + 1;  // groups of 16, and one thread for the rest
-    launch_dep(k_rhs32_shift16, (unsigned)((nt + 255) / 256), 256, 0, s, m, mean_scale, b32, r32, n);
+    if (skip_dry && !r32)
+      launch_dep(k_rhs32_shift16<true>, (unsigned)((nt + 255) / 256), 256, 0, s, m, mean_scale, b32, r32, n);
+    else
+      launch_dep(k_rhs32_shift16<false>, (unsigned)((nt + 255) / 256), 256, 0, s, m, mean_scale, b32, r32, n);
   } else {
     launch_dep(k_rhs32_shift, (unsigned)((n + 255) / 256), 256, 0, s, m, mean_scale, b32, r32, n);
   }
@@ -721,19 +741,20 @@ void launch_make_dq(const double* diag, const uint8_t* m, double Q, int8_t* dq, 
 }
 
 void launch_maxabs2(const double* x, const double* b, long long n, int tx, int ty, int ui0, int ui1, int uj0, int uj1,
-                    double* ds, cudaStream_t s) {
-  launch_dep(k_maxabs2, 1024, 256, 0, s, x, b, n, tx, ty, ui0, ui1, uj0, uj1, ds);
+                    double* ds, cudaStream_t s, const uint8_t* m) {
+  launch_dep(k_maxabs2, 1024, 256, 0, s, x, b, n, tx, ty, ui0, ui1, uj0, uj1, ds, m);
 }
 
-void launch_update_scaled_max(double* x, const float* e, double* ds, long long n, cudaStream_t s) {
+void launch_update_scaled_max(double* x, const float* e, double* ds, long long n, cudaStream_t s,
+                              const uint8_t* msk) {
   static int nsm = 0;
   if (!nsm) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   }
-  if (((uintptr_t)x | (uintptr_t)e) % 16 == 0)
-    launch_dep(k_update_scaled_max4, nsm * 4, kMxThreads, 0, s, x, e, ds, n, ds);
+  if (((uintptr_t)x | (uintptr_t)e) % 16 == 0 && (uintptr_t)msk % 4 == 0)
+    launch_dep(k_update_scaled_max4, nsm * 4, kMxThreads, 0, s, x, e, ds, n, ds, msk);
   else
     launch_dep(k_update_scaled_max, nsm * 4, kMxThreads, 0, s, x, e, ds, n, ds);  // 4 blocks per SM: measured 4 % faster than 8
 }

@@ -230,10 +230,12 @@ __device__ __forceinline__ float ld_ordered(const float* p) {
 // ASSIGN, the 8 fine x values. d_prolong<float, 1>'s arithmetic in its order.
 // The thread-per-parent form compiled to 32 registers with its loads spread
 // over the arithmetic; its warps waited on memory 85-90 % of the time.
+// fmsk (optional): a parent whose eight children are all dry is skipped; a
+// dry fine cell holds +0 and has Pcoef = 0, so the update would leave it +0.
 template <bool ASSIGN>
 __global__ void __launch_bounds__(256) k_prolong3c_f(float* __restrict__ xf, const float* __restrict__ x,
                                                      const float* __restrict__ coef, Geom gf, Geom gc, int np_i,
-                                                     int np_j, int np_k) {
+                                                     int np_j, int np_k, const uint8_t* __restrict__ fmsk) {
   dep_wait();
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const int q = blockIdx.y * blockDim.y + threadIdx.y;
@@ -244,6 +246,12 @@ __global__ void __launch_bounds__(256) k_prolong3c_f(float* __restrict__ xf, con
   const int i = nh + 1 + 2 * p, j = nh + 1 + 2 * q, k = nh + 1 + 2 * qk;
   const long long c1 = gc.n1, c2 = gc.n2, f1 = gf.n1, f2 = gf.n2;
   const long long C = lin(gc, f2c(i, nh), f2c(j, nh), f2c(k, nh)), F = lin(gf, i, j, k);
+  if (fmsk) {
+    unsigned any = 0;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) any |= fmsk[F + (t & 1) + ((t >> 1) & 1) * f1 + (t >> 2) * f2];
+    if (!any) return;
+  }
   // xs[dk][d]: plane C + (dk-1)*c2, offsets d = W, E, S, N, SW, SE, NW, NE
   const long long off[8] = {-1, 1, -c1, c1, -1 - c1, 1 - c1, -1 + c1, 1 + c1};
   float xs[3][8];
@@ -397,12 +405,16 @@ __global__ void __launch_bounds__(256) k_sweep7_3d_q(const float* __restrict__ x
 // ZERO: x is known to hold +0 in every cell (the first sweep of a cycle's
 // level-1 pre-smoothing): it is not read, and the same formula on +0
 // operands gives the same bits.
-constexpr int kQRun = 4;
+//
+// qact (optional): a quad whose cells are dry in every plane of the run is
+// skipped. In the mixed form's FP32 fields a dry cell holds +0 in x, y and b
+// and has omega*idiag = 0, so the sweep would write +0 over +0 there.
+constexpr int kQRun = kQRunPlanes;
 template <bool ZERO>
 __global__ void __launch_bounds__(256) k_sweep7_3d_q4(const float* __restrict__ x, float* __restrict__ y,
                                                       const float* __restrict__ b, const uint8_t* __restrict__ wq,
                                                       const float* __restrict__ wtab, float cff, long long n1,
-                                                      long long n2, int tz) {
+                                                      long long n2, int tz, const uint8_t* __restrict__ qact) {
   __shared__ float tab[256];
   dep_wait();
   tab[threadIdx.x] = wtab[threadIdx.x];
@@ -410,6 +422,7 @@ __global__ void __launch_bounds__(256) k_sweep7_3d_q4(const float* __restrict__ 
   const long long t = (long long)blockIdx.x * 256 + threadIdx.x;  // quad of the plane
   const int k0 = 1 + blockIdx.y * kQRun;
   if (4 * t >= n2 || k0 > tz - 2) return;
+  if (qact && !qact[(long long)blockIdx.y * (n2 >> 2) + t]) return;
   const int k1 = min(k0 + kQRun, tz - 1);
   typedef Ar<float> A;
   long long I = 4 * t + n2 * k0;
@@ -445,14 +458,14 @@ bool sweep7_quad_ok(const Geom& g, const void* x, const void* y, const void* b, 
          (uintptr_t)wq % 4 == 0;
 }
 void launch_sweep7_3d_q(const float* x, float* y, const float* b, const uint8_t* wq, const float* wtab, float cff,
-                        const Geom& g, cudaStream_t s, bool x_zero) {
+                        const Geom& g, cudaStream_t s, bool x_zero, const uint8_t* qact) {
   if (g.tz < 3) return;
   if (sweep7_quad_ok(g, x, y, b, wq)) {
     const dim3 grid((unsigned)((g.n2 / 4 + 255) / 256), (unsigned)((g.tz - 2 + kQRun - 1) / kQRun));
     if (x_zero)
-      launch_dep(k_sweep7_3d_q4<true>, grid, 256, 0, s, x, y, b, wq, wtab, cff, g.n1, g.n2, g.tz);
+      launch_dep(k_sweep7_3d_q4<true>, grid, 256, 0, s, x, y, b, wq, wtab, cff, g.n1, g.n2, g.tz, qact);
     else
-      launch_dep(k_sweep7_3d_q4<false>, grid, 256, 0, s, x, y, b, wq, wtab, cff, g.n1, g.n2, g.tz);
+      launch_dep(k_sweep7_3d_q4<false>, grid, 256, 0, s, x, y, b, wq, wtab, cff, g.n1, g.n2, g.tz, qact);
     return;
   }
   if (x_zero) cudaMemsetAsync(const_cast<float*>(x), 0, (size_t)g.len * sizeof(float), s);  // the one-cell form reads x
@@ -633,7 +646,7 @@ void launch_restrict(int kind, const T* xf, T* bc, const T* Rcoef, const Geom& g
 }
 template <class T>
 void launch_prolong(int kind, T* xf, const T* xc, const T* Pcoef, const Geom& gf, const Geom& gc, int nxf, int nyf,
-                    int nzf, int kf0, int kf1, bool assign, cudaStream_t s) {
+                    int nzf, int kf0, int kf1, bool assign, cudaStream_t s, const uint8_t* fmsk) {
   // parents: i = nh+1 : 2 : nx+nh (likewise j, and k in 3D)
   const int np_i = (nxf + 1) / 2, np_j = (nyf + 1) / 2;
   const bool threed = (kind == 1 || kind == 3);
@@ -644,10 +657,10 @@ void launch_prolong(int kind, T* xf, const T* xc, const T* Pcoef, const Geom& gf
   if (sizeof(T) == 4 && kind == 1) {
     if (assign)
       launch_dep(k_prolong3c_f<true>, grid, blk, 0, s, (float*)xf, (const float*)xc, (const float*)Pcoef, gf, gc, np_i,
-                 np_j, np_k);
+                 np_j, np_k, fmsk);
     else
       launch_dep(k_prolong3c_f<false>, grid, blk, 0, s, (float*)xf, (const float*)xc, (const float*)Pcoef, gf, gc,
-                 np_i, np_j, np_k);
+                 np_i, np_j, np_k, fmsk);
     return;
   }
 #define CFMG_PRO(K)                                                                                       \
@@ -698,7 +711,7 @@ void launch_norm(const T* x, const uint8_t* m, size_t n, double* partials, doubl
   template void launch_restrict<T>(int, const T*, T*, const T*, const Geom&, const Geom&, const Box&,            \
                                    cudaStream_t);                                                                \
   template void launch_prolong<T>(int, T*, const T*, const T*, const Geom&, const Geom&, int, int, int, int, int, \
-                                  bool, cudaStream_t);                                                           \
+                                  bool, cudaStream_t, const uint8_t*);                                           \
   template void launch_fill_xperio<T>(T*, const Geom&, cudaStream_t);                                            \
   template void launch_norm<T>(const T*, const uint8_t*, size_t, double*, double*, const double*, int, cudaStream_t);
 
@@ -735,7 +748,7 @@ static void launch_op_t(const Op& op, cudaStream_t s) {
     case OPK_SWEEP7:
       if (sizeof(T) == 4 && op.wq)
         launch_sweep7_3d_q((const float*)x, (float*)y, (const float*)b, op.wq, op.wtab, (float)cff, op.g, s,
-                           op.assign != 0);
+                           op.assign != 0, op.qact);
       else
         launch_sweep7_3d<T>(x, y, b, w, cff, op.g, s);
       break;
@@ -765,7 +778,7 @@ static void launch_op_t(const Op& op, cudaStream_t s) {
       const bool t3 = (kind == 1 || kind == 3);
       // launch_prolong derives the parent counts from (nx, ny, nz) of the fine level
       launch_prolong<T>(kind, y, x, (const T*)op.coef, op.g, op.gc, 2 * op.np_i, 2 * op.np_j,
-                        t3 ? 2 * (op.kf1 - op.kf0 + 1) : 1, op.kf0, op.kf1, op.assign != 0, s);
+                        t3 ? 2 * (op.kf1 - op.kf0 + 1) : 1, op.kf0, op.kf1, op.assign != 0, s, op.m);
       break;
     }
     case OPK_FILL: launch_fill_xperio<T>(y, op.g, s); break;

@@ -220,4 +220,30 @@ void launch_make_wq(const double* diag, const float* w32, const float* tab, doub
   launch_dep(k_make_wq, nb(n), kT, 0, s, diag, w32, tab, Q, wq, n, ok);
 }
 
+// qact[r * nq + t] = 1 when a cell of quad t (linear offsets 4t .. 4t+3 of a
+// plane) is wet in one of the planes 1 + run*r .. of the 3D sweep range
+// (0-based planes 1 .. tz-2); 0 when all of them are dry
+__global__ void k_make_qact(const uint8_t* __restrict__ m, uint8_t* __restrict__ qact, long long n2, int tz, int run,
+                            long long nq, int nruns) {
+  dep_wait();
+  const long long T = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (T >= nq * nruns) return;
+  const int r = (int)(T / nq);
+  const long long t = T - (long long)r * nq;
+  const int k0 = 1 + r * run, k1 = min(k0 + run, tz - 1);
+  unsigned any = 0;
+  for (int k = k0; k < k1; ++k)
+    for (int c = 0; c < 4; ++c) {
+      const long long o = 4 * t + c;
+      if (o < n2) any |= m[n2 * k + o];
+    }
+  qact[T] = any ? 1 : 0;
+}
+void launch_make_qact(const uint8_t* m, uint8_t* qact, long long n2, int tz, int run, cudaStream_t s) {
+  const long long nq = (n2 + 3) / 4;
+  const int nruns = (tz - 2 + run - 1) / run;
+  if (nruns <= 0) return;
+  launch_dep(k_make_qact, nb(nq * nruns), kT, 0, s, m, qact, n2, tz, run, nq, nruns);
+}
+
 }  // namespace cfmg

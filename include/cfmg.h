@@ -131,6 +131,12 @@ extern "C" {
                                    read omega*idiag as a one-byte code diag into a 256-entry table (when
                                    every cell's code reproduces its float exactly) instead of a 4-byte
                                    float per cell; 0 the floats. Both give the same bits. */
+#define CFMG_OPT_SKIP_DRY 10 /* mixed form, 3D 7-point operator: 1 (default) the four-cell sweeps, the
+                               cell-centred prolongation, the level-1 solution update and the wet-mean
+                               shift skip groups of cells that are all dry (their FP32 fields hold +0 and
+                               stay +0; the update's max |x| of them is taken once per solve); 0 every
+                               cell. Both give the same values (a -0 left in a dry cell of x can stay -0
+                               where the full update would make it +0). */
 #define CFMG_OPT_STAGED_RESIDUAL 9 /* mixed form, 3D 7-point operator, integer residual: 2 (default) the
                                       level-1 residual pass stages each plane of a 32 x 16 column tile in
                                       shared memory by TMA and converts every x once (even tx only), two

@@ -256,6 +256,36 @@ def test_staged_residual_matches_strip_residual(name):
         assert np.linalg.norm(a - c) <= 1e-8 * np.linalg.norm(c)
 
 
+@pytest.mark.parametrize("cycle", ["v", "f"])
+def test_skip_dry_is_bit_identical(cycle):
+    """Skipping groups of dry cells in the 3D passes (four-cell sweeps with
+    per-(plane run, quad) wet flags, the cell-centred prolongation, the FP64
+    update with the dry cells' max |x| taken once, the wet-mean shift) gives
+    the full passes' history and solution, on the configuration-3 recipe
+    (coastline cut by a bottom topography: most of the box dry)."""
+    import workloads as W
+
+    param, vmsk, noise = W.config3(64, 64, 32, nlevels=4)
+    param = dict(param, cycle=cycle)
+    out = []
+    for skip in (1, 0):
+        mg = cfmg.get_gmg(cfmg.Param(**param, tol=1e-10, maxite=60, residual_norm="l2", precision="mixed",
+                                     verbose=False))
+        mg.set_option("engine_cells", 2000)  # fine levels as standalone kernels
+        mg.set_option("skip_dry", skip)
+        mg.oper[1].msk = vmsk
+        cfmg.setup_operators(mg)
+        for lev in range(1, mg.nlevels + 1):
+            for f in ("x", "y", "r", "b"):
+                cfmg.set_to_zero(mg, lev, f)
+        mg.data[1].b = W.rhs(noise, mg.download(1, "msk"))
+        res, n, hist = cfmg.solve(mg, history=True)
+        out.append((res, n, hist, mg.data[1].x))
+        mg.close()
+    assert out[0][0] <= 1e-10 and out[0][1] == out[1][1] and out[0][0] == out[1][0]
+    assert np.array_equal(out[0][2], out[1][2]) and np.array_equal(out[0][3], out[1][3])
+
+
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_solve_graph_matches_host_loop(precision):
     """The whole solve! loop as one graph launch (a while node with the
