@@ -70,6 +70,7 @@ struct cfmg_handle {
   // 3D 7-point: dq with rows padded to 16 bytes for the TMA-staged pass
   // (k_resid3d.cu, CFMG_OPT_STAGED_RESIDUAL); r3_ran once that pass ran
   int8_t* dqp = nullptr;
+  uint8_t* tcol = nullptr;  // wet flags of the staged pass's (tile, plane) pairs
   bool r3_on = true, r3_ran = false;
   int r3_rows = 2;  // rows of its tile per thread (1 or 2)
   // mixed V-cycle, 3D 7-point: level 1's FP32 x is not zeroed before the
@@ -748,7 +749,8 @@ int resid_restrict3d(cfmg_handle* h, int lev) {
   TRY(flush(h));
   {
     Launch k(h, CFMG_K_RESIDUAL, lev, CFMG_MIXED);
-    launch_resid_restrict7c(vf.x, vf.b, f.wq, f.msk, vc.Rcoef, vc.b, geom(f), geom(c), interior(c), h->stream);
+    launch_resid_restrict7c(vf.x, vf.b, f.wq, f.msk, vc.Rcoef, vc.b, geom(f), geom(c), interior(c), h->stream,
+                            h->dry_on);
   }
   LAUNCH_OK(h);
   return CFMG_OK;
@@ -976,6 +978,11 @@ int prepare_int(cfmg_handle* h) {
     const int txp = dq_pitch(l1.tx);
     if (!h->dqp) CUDA_OK(h, cudaMalloc((void**)&h->dqp, (size_t)txp * l1.ty * l1.tz));
     launch_pad_dq(h->dq, h->dqp, l1.tx, txp, (long long)l1.ty * l1.tz, h->stream);
+    const long long nt = resid3d_tcol_size(geom(l1), interior(l1));
+    if (nt > 0) {
+      if (!h->tcol) CUDA_OK(h, cudaMalloc((void**)&h->tcol, (size_t)nt));
+      launch_make_tcol(l1.msk, h->tcol, geom(l1), interior(l1), h->stream);
+    }
   }
   int hok = 0;
   CUDA_OK(h, cudaMemcpyAsync(&hok, ok, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -1201,7 +1208,7 @@ int fused_residual(cfmg_handle* h) {
       float* r32 = h->d.cycle == CFMG_CYCLE_F ? l1.r32 : nullptr;
       const bool r3 = kind == OPK_RESID7 && h->r3_on &&
                       launch_resid_int3d(l1.x, l1.b, h->dqp, g, bx, h->dscal, l1.b32, r32, neumann, h->partials,
-                                         h->stream, h->r3_rows);
+                                         h->stream, h->r3_rows, h->dry_on ? h->tcol : nullptr);
       h->r3_ran |= r3;
       if (!r3 && !launch_resid_int2d(kind, l1.x, l1.b, h->dq, g, bx, h->dscal, l1.b32, r32, neumann, h->partials,
                                      h->stream))
@@ -1714,6 +1721,7 @@ int cfmg_destroy(cfmg_handle* h) {
     if (p) cudaFree(p);
   if (h->dq) cudaFree(h->dq);
   if (h->dqp) cudaFree(h->dqp);
+  if (h->tcol) cudaFree(h->tcol);
   for (Level& l : h->lv)
     if (l.qact) cudaFree(l.qact);
   if (h->dhist) cudaFree(h->dhist);

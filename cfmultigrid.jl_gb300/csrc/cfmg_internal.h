@@ -108,7 +108,8 @@ bool sweep7_quad_ok(const Geom& g, const void* x, const void* y, const void* b, 
 // FP32 3D 7-point cell-centred residual at the children of the coarse box cb
 // restricted into the coarse b (k_ops.cu); dc: diag as one-byte codes
 void launch_resid_restrict7c(const float* x, const float* b, const uint8_t* dc, const uint8_t* m, const float* rcoef,
-                             float* bc, const Geom& gf, const Geom& gc, const Box& cb, cudaStream_t s);
+                             float* bc, const Geom& gf, const Geom& gc, const Box& cb, cudaStream_t s,
+                             bool skip_dry = false);
 template <class T>
 void launch_sweep9_2d(const T* x, T* y, const T* b, const T* widiag, T cff, const Geom& g, const Box& bx,
                       cudaStream_t s);
@@ -381,9 +382,13 @@ bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t
 // (odd tx, misaligned arrays, no tensor-map encoder): use launch_resid_int2d.
 int dq_pitch(int tx);
 void launch_pad_dq(const int8_t* dq, int8_t* dqp, int tx, int txp, long long rows, cudaStream_t s);
+// tcol (optional): per-(tile, plane) wet flags (launch_make_tcol); tasks whose
+// planes are all dry are skipped (two rows a thread, and r32 not written, only)
 bool launch_resid_int3d(const double* x, const double* b, const int8_t* dqp, const Geom& g, const Box& bx,
                         double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s,
-                        int rows_per_thread);
+                        int rows_per_thread, const uint8_t* tcol = nullptr);
+long long resid3d_tcol_size(const Geom& g, const Box& bx);
+void launch_make_tcol(const uint8_t* m, uint8_t* tcol, const Geom& g, const Box& bx, cudaStream_t s);
 // skip_dry: groups of 16 dry cells are neither read nor written (their b32 is +0 already)
 void launch_rhs32_shift(const uint8_t* m, const double* mean_scale, float* b32, float* r32, long long n,
                         cudaStream_t s, bool skip_dry = false);

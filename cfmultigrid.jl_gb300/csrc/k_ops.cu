@@ -178,12 +178,14 @@ __global__ void __launch_bounds__(kThreads) k_prolong(T* __restrict__ xf, const 
 // float exactly). Each child's residual and the sum of the eight are
 // computed as v_resid7 and v_restrict<KIND 1> do, so the coarse b is the
 // same bits. Every child must lie in the fine interior box (checked by the
-// caller).
+// caller). skip_dry: a coarse cell whose eight children are dry gets +0
+// without the residual's loads (the masked residuals are signed zeros, so
+// the restricted value is a zero, of whichever sign).
 __global__ void __launch_bounds__(256) k_resid_restrict7c(const float* __restrict__ x, const float* __restrict__ b,
                                                           const uint8_t* __restrict__ dc,
                                                           const uint8_t* __restrict__ m,
                                                           const float* __restrict__ rcoef, float* __restrict__ bc,
-                                                          Geom gf, Geom gc, Box cb) {
+                                                          Geom gf, Geom gc, Box cb, bool skip_dry) {
   dep_wait();
   const BoxIdx q = box_idx(cb);
   if (!q.ok) return;
@@ -191,6 +193,11 @@ __global__ void __launch_bounds__(256) k_resid_restrict7c(const float* __restric
   const int nh = gc.nh;
   const long long n1 = gf.n1, n2 = gf.n2;
   const long long F = lin(gf, c2f(q.i, nh), c2f(q.j, nh), c2f(q.k, nh));
+  if (skip_dry && (m[F] | m[F + 1] | m[F + n1] | m[F + 1 + n1] | m[F + n2] | m[F + 1 + n2] | m[F + n1 + n2] |
+                   m[F + 1 + n1 + n2]) == 0) {
+    bc[lin(gc, q.i, q.j, q.k)] = 0.f;
+    return;
+  }
   auto r = [&](long long I) {
     return mask_mul(m[I], A::sub(A::add(A::mul((float)dc[I], x[I]), b[I]), faces6(x, I, n1, n2)));
   };
@@ -205,9 +212,11 @@ __global__ void __launch_bounds__(256) k_resid_restrict7c(const float* __restric
   bc[C] = A::mul(rcoef[C], s);
 }
 void launch_resid_restrict7c(const float* x, const float* b, const uint8_t* dc, const uint8_t* m, const float* rcoef,
-                             float* bc, const Geom& gf, const Geom& gc, const Box& cb, cudaStream_t s) {
+                             float* bc, const Geom& gf, const Geom& gc, const Box& cb, cudaStream_t s,
+                             bool skip_dry) {
   if (box_empty(cb)) return;
-  launch_dep(k_resid_restrict7c, box_grid(cb, kBoxBlk), kBoxBlk, 0, s, x, b, dc, m, rcoef, bc, gf, gc, cb);
+  launch_dep(k_resid_restrict7c, box_grid(cb, kBoxBlk), kBoxBlk, 0, s, x, b, dc, m, rcoef, bc, gf, gc, cb,
+             skip_dry);
 }
 
 // in-order global loads (asm volatile keeps them ahead of the arithmetic

@@ -125,12 +125,20 @@ __device__ __forceinline__ R3Task r3_task(const R3Space& sp, int T) {
   return t;
 }
 
+// tcol (optional, JT = 2 tiles): 1 for each (tile, interior plane) with a wet
+// cell. A task whose output planes are all dry is skipped: its cells' b32 is
+// +0 already and their residuals add exact zeros to the sums. The block's
+// tasks' flags are gathered in shared memory first (up to kR3MaxTasks per
+// block; later ones count as wet), and the issue cursor and the consumers
+// skip the same tasks.
+constexpr int kR3MaxTasks = 64;
 template <int JT, bool NEUMANN>
 __global__ void __launch_bounds__(kMxThreads) k_resid_int3d(const __grid_constant__ CUtensorMap mx,
                                                             const __grid_constant__ CUtensorMap mb,
                                                             const __grid_constant__ CUtensorMap md, R3Space sp,
                                                             double* ds, float* __restrict__ b32,
-                                                            float* __restrict__ r32, double* __restrict__ partials) {
+                                                            float* __restrict__ r32, double* __restrict__ partials,
+                                                            const uint8_t* __restrict__ tcol) {
   typedef R3Cfg<JT> G;
   extern __shared__ __align__(128) unsigned char smem[];
   long long* pring = reinterpret_cast<long long*>(smem + G::Stages * G::StageBytes);
@@ -151,11 +159,31 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int3d(const __grid_constan
   const double scale = ds[S_NEXT];
   const float fm = (float)ldexp(scale, -(k + q));  // power of two: R -> r * scale
   const int ntasks = sp.nti * sp.ntj * sp.nkc;
+  // wet flags of the block's tasks (bit m: task blockIdx.x + m * gridDim.x),
+  // the same in every thread
+  unsigned long long wt = ~0ULL;
+  if (tcol) {
+    wt = 0;
+    for (int m = 0; m < kR3MaxTasks; ++m) {
+      const int T = blockIdx.x + m * gridDim.x;
+      if (T >= ntasks) break;
+      const R3Task t = r3_task<JT>(sp, T);
+      const long long tile = (long long)((t.r0t - sp.r0) / R3Cfg<JT>::TJ) * sp.nti + (t.c0t - sp.c0) / R3Cfg<JT>::TI;
+      int any = 0;
+      for (int p = tid; p < t.np - 2; p += kMxThreads) any |= tcol[tile * sp.nk + (t.ka - sp.p0) + p];
+      if (__syncthreads_or(any)) wt |= 1ULL << m;
+    }
+  }
+  auto wet = [&](int T) {  // tasks beyond kR3MaxTasks count as wet
+    const int m = (T - (int)blockIdx.x) / (int)gridDim.x;
+    return m >= kR3MaxTasks || ((wt >> m) & 1ULL);
+  };
 
   // issue cursor (thread 0): the block's sequence of (task, plane) in order
   int iT = blockIdx.x, iq = 0;
+  while (iT < ntasks && !wet(iT)) iT += gridDim.x;
   unsigned long long in = 0;
-  R3Task it = r3_task<JT>(sp, iT);
+  R3Task it = r3_task<JT>(sp, iT < ntasks ? iT : 0);
   auto issue_next = [&]() {
     if (iT >= ntasks) return;
     const int s = (int)(in % G::Stages);
@@ -173,6 +201,7 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int3d(const __grid_constan
     ++in;
     if (++iq == it.np) {
       iT += gridDim.x;
+      while (iT < ntasks && !wet(iT)) iT += gridDim.x;
       iq = 0;
       if (iT < ntasks) it = r3_task<JT>(sp, iT);
     }
@@ -203,6 +232,7 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int3d(const __grid_constan
   unsigned long long n = 0;  // planes consumed
   bool fault = false;
   for (int T = blockIdx.x; T < ntasks && !fault; T += gridDim.x) {
+    if (!wet(T)) continue;
     const R3Task t = r3_task<JT>(sp, T);
     const int ox = (t.c0t - 1) - ((t.c0t - 1) & ~1), ob = t.c0t - (t.c0t & ~1), od = t.c0t - (t.c0t & ~15);
     const int col = t.c0t + ti;
@@ -320,6 +350,38 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int3d(const __grid_constan
   }
 }
 
+// tcol[(tJ * nti + tI) * nk + p] = 1 when tile (tI, tJ) of the JT = 2
+// tiling holds a wet cell in interior plane p
+__global__ void k_make_tcol(const uint8_t* __restrict__ m, uint8_t* __restrict__ tcol, R3Space sp) {
+  const long long T = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long ntiles = (long long)sp.nti * sp.ntj;
+  if (T >= ntiles * sp.nk) return;
+  const long long tile = T / sp.nk;
+  const int p = (int)(T - tile * sp.nk);
+  const int tI = (int)(tile % sp.nti), tJ = (int)(tile / sp.nti);
+  const int c0 = sp.c0 + R3Cfg<2>::TI * tI, r0 = sp.r0 + R3Cfg<2>::TJ * tJ;
+  const int c1 = min(c0 + R3Cfg<2>::TI, sp.c0 + sp.ni), r1 = min(r0 + R3Cfg<2>::TJ, sp.r0 + sp.nj);
+  unsigned any = 0;
+  for (int r = r0; r < r1; ++r)
+    for (int c = c0; c < c1; ++c) any |= m[(long long)c + sp.n1 * r + sp.n2 * (sp.p0 + p)];
+  tcol[T] = any ? 1 : 0;
+}
+
+R3Space r3_space(const Geom& g, const Box& bx, int ti, int tj) {
+  R3Space sp{};
+  sp.c0 = bx.i0 - 1;
+  sp.r0 = bx.j0 - 1;
+  sp.p0 = bx.k0 - 1;
+  sp.ni = bx.i1 - bx.i0 + 1;
+  sp.nj = bx.j1 - bx.j0 + 1;
+  sp.nk = bx.k1 - bx.k0 + 1;
+  sp.nti = (sp.ni + ti - 1) / ti;
+  sp.ntj = (sp.nj + tj - 1) / tj;
+  sp.n1 = g.n1;
+  sp.n2 = g.n2;
+  return sp;
+}
+
 __global__ void k_pad_dq(const int8_t* __restrict__ dq, int8_t* __restrict__ dqp, int tx, int txp, long long rows) {
   const long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= rows * txp) return;
@@ -379,21 +441,11 @@ int r3_grid() {
 
 template <int JT>
 bool launch_r3(const double* x, const double* b, const int8_t* dqp, const Geom& g, const Box& bx, double* ds,
-               float* b32, float* r32, bool neumann, double* partials, cudaStream_t s) {
+               float* b32, float* r32, bool neumann, double* partials, cudaStream_t s, const uint8_t* tcol) {
   typedef R3Cfg<JT> G;
-  R3Space sp;
-  sp.c0 = bx.i0 - 1;
-  sp.r0 = bx.j0 - 1;
-  sp.p0 = bx.k0 - 1;
-  sp.ni = bx.i1 - bx.i0 + 1;
-  sp.nj = bx.j1 - bx.j0 + 1;
-  sp.nk = bx.k1 - bx.k0 + 1;
+  R3Space sp = r3_space(g, bx, G::TI, G::TJ);
   // the boxes start at column c0t-1 >= 0, row r0t-1 >= 0 and plane ka-1 >= 0
   if (sp.ni <= 0 || sp.nj <= 0 || sp.nk <= 0 || sp.c0 < 1 || sp.r0 < 1 || sp.p0 < 1) return false;
-  sp.nti = (sp.ni + G::TI - 1) / G::TI;
-  sp.ntj = (sp.nj + G::TJ - 1) / G::TJ;
-  sp.n1 = g.n1;
-  sp.n2 = g.n2;
   CUtensorMap mx, mb, md;
   const int txp = dq_pitch_of(g.tx);
   if (!encode3(&mx, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, x, g.tx, g.tx, g.ty, g.tz, G::XW, G::XH) ||
@@ -408,9 +460,9 @@ bool launch_r3(const double* x, const double* b, const int8_t* dqp, const Geom& 
   sp.kt = (int)(kt > sp.nk ? sp.nk : kt);
   sp.nkc = (sp.nk + sp.kt - 1) / sp.kt;
   if (neumann)
-    launch_dep(k_resid_int3d<JT, true>, grid, kMxThreads, G::Smem, s, mx, mb, md, sp, ds, b32, r32, partials);
+    launch_dep(k_resid_int3d<JT, true>, grid, kMxThreads, G::Smem, s, mx, mb, md, sp, ds, b32, r32, partials, tcol);
   else
-    launch_dep(k_resid_int3d<JT, false>, grid, kMxThreads, G::Smem, s, mx, mb, md, sp, ds, b32, r32, partials);
+    launch_dep(k_resid_int3d<JT, false>, grid, kMxThreads, G::Smem, s, mx, mb, md, sp, ds, b32, r32, partials, tcol);
   return true;
 }
 
@@ -425,11 +477,24 @@ void launch_pad_dq(const int8_t* dq, int8_t* dqp, int tx, int txp, long long row
 
 bool launch_resid_int3d(const double* x, const double* b, const int8_t* dqp, const Geom& g, const Box& bx,
                         double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s,
-                        int rows_per_thread) {
+                        int rows_per_thread, const uint8_t* tcol) {
   // TMA: global addresses on 16 bytes, row and plane pitches multiples of 16 bytes
   if (!dqp || g.tx % 2 != 0 || ((uintptr_t)x | (uintptr_t)b | (uintptr_t)dqp) % 16 != 0) return false;
-  if (rows_per_thread == 2) return launch_r3<2>(x, b, dqp, g, bx, ds, b32, r32, neumann, partials, s);
-  return launch_r3<1>(x, b, dqp, g, bx, ds, b32, r32, neumann, partials, s);
+  // the skipped tasks' r32 would keep older values: skip only where r32 is not written
+  if (rows_per_thread == 2) return launch_r3<2>(x, b, dqp, g, bx, ds, b32, r32, neumann, partials, s, r32 ? nullptr : tcol);
+  return launch_r3<1>(x, b, dqp, g, bx, ds, b32, r32, neumann, partials, s, nullptr);
+}
+
+long long resid3d_tcol_size(const Geom& g, const Box& bx) {
+  const R3Space sp = r3_space(g, bx, R3Cfg<2>::TI, R3Cfg<2>::TJ);
+  return (long long)sp.nti * sp.ntj * sp.nk;
+}
+
+void launch_make_tcol(const uint8_t* m, uint8_t* tcol, const Geom& g, const Box& bx, cudaStream_t s) {
+  const R3Space sp = r3_space(g, bx, R3Cfg<2>::TI, R3Cfg<2>::TJ);
+  const long long n = (long long)sp.nti * sp.ntj * sp.nk;
+  if (n <= 0) return;
+  k_make_tcol<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(m, tcol, sp);
 }
 
 }  // namespace cfmg
