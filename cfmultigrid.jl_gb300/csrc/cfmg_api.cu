@@ -70,7 +70,8 @@ struct cfmg_handle {
   // 3D 7-point: dq with rows padded to 16 bytes for the TMA-staged pass
   // (k_resid3d.cu, CFMG_OPT_STAGED_RESIDUAL); r3_ran once that pass ran
   int8_t* dqp = nullptr;
-  uint8_t* tcol = nullptr;  // wet flags of the staged pass's (tile, plane) pairs
+  uint8_t* tcol = nullptr;   // wet flags of the staged pass's (tile, plane) pairs
+  uint8_t* sflag = nullptr;  // wet flags of the strip pass's (plane, row, strip) triples
   bool r3_on = true, r3_ran = false;
   int r3_rows = 2;  // rows of its tile per thread (1 or 2)
   // mixed V-cycle, 3D 7-point: level 1's FP32 x is not zeroed before the
@@ -632,7 +633,8 @@ int prolong_t(cfmg_handle* h, int lev, bool onto_zero = false) {
     np_k = f.kc1 - f.kc0 + 1;
   }
   op.n = (long long)op.np_i * op.np_j * np_k;
-  if (sizeof(T) == 4 && kind == 1 && h->dry_on) op.m = f.msk;  // parents of eight dry cells are skipped
+  // FP32 cycles of a closed topology: parents whose children are all dry are skipped
+  if (sizeof(T) == 4 && h->dry_on && !xperio(h)) op.m = f.msk;
   if (onto_zero) {
     if (!h->record && !(h->engine_on && (long long)f.len <= engine_limit(h, pc<T>()))) op.assign = 1;
     else TRY(zero_t<T>(h, lev, CFMG_X));
@@ -974,6 +976,13 @@ int prepare_int(cfmg_handle* h) {
   const int one = 1;
   CUDA_OK(h, cudaMemcpyAsync(ok, &one, sizeof(int), cudaMemcpyHostToDevice, h->stream));
   launch_make_dq(l1.diag, l1.msk, kind == OPK_RESID9 ? 4.0 : 1.0, h->dq, (long long)l1.len, ok, h->stream);
+  {
+    const long long ns = resid_sflag_size(kind, geom(l1), interior(l1));
+    if (ns > 0) {
+      if (!h->sflag) CUDA_OK(h, cudaMalloc((void**)&h->sflag, (size_t)ns));
+      launch_make_sflag(kind, l1.msk, h->sflag, geom(l1), interior(l1), h->stream);
+    }
+  }
   if (kind == OPK_RESID7) {
     const int txp = dq_pitch(l1.tx);
     if (!h->dqp) CUDA_OK(h, cudaMalloc((void**)&h->dqp, (size_t)txp * l1.ty * l1.tz));
@@ -1211,7 +1220,7 @@ int fused_residual(cfmg_handle* h) {
                                          h->stream, h->r3_rows, h->dry_on ? h->tcol : nullptr);
       h->r3_ran |= r3;
       if (!r3 && !launch_resid_int2d(kind, l1.x, l1.b, h->dq, g, bx, h->dscal, l1.b32, r32, neumann, h->partials,
-                                     h->stream))
+                                     h->stream, h->dry_on ? h->sflag : nullptr))
         launch_resid_int(kind, l1.x, l1.b, h->dq, g, bx, lo, n, h->dscal, l1.b32, r32, neumann, h->partials,
                          h->stream);
       launch_fused_final(h->partials, h->dscal, h->dscal + S_NORMB, neumann ? h->dscal + S_NWET : nullptr,
@@ -1722,6 +1731,7 @@ int cfmg_destroy(cfmg_handle* h) {
   if (h->dq) cudaFree(h->dq);
   if (h->dqp) cudaFree(h->dqp);
   if (h->tcol) cudaFree(h->tcol);
+  if (h->sflag) cudaFree(h->sflag);
   for (Level& l : h->lv)
     if (l.qact) cudaFree(l.qact);
   if (h->dhist) cudaFree(h->dhist);

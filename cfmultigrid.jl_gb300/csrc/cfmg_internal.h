@@ -375,8 +375,13 @@ void launch_resid_int(int kind, const double* x, const double* b, const int8_t* 
 // that many elements on either side, as level 1's x does in a handle's arena
 // (checked by cfmg_create).
 constexpr int kResidIntReach = 32;
+// sflag (optional): per-(plane, row, strip) wet flags (launch_make_sflag);
+// strip tasks whose rows are all dry are skipped
 bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t* dq, const Geom& g, const Box& bx,
-                        const double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s);
+                        const double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s,
+                        const uint8_t* sflag = nullptr);
+long long resid_sflag_size(int kind, const Geom& g, const Box& bx);
+void launch_make_sflag(int kind, const uint8_t* m, uint8_t* sflag, const Geom& g, const Box& bx, cudaStream_t s);
 // 3D 7-point form with TMA-staged planes (k_resid3d.cu). dqp: dq with rows
 // padded to txp = dq_pitch(tx) bytes (launch_pad_dq). false: not applicable
 // (odd tx, misaligned arrays, no tensor-map encoder): use launch_resid_int2d.

@@ -282,11 +282,15 @@ struct StripSpace {
   long long n1;
 };
 
+// sflag (optional): 1 for each (plane, row, strip) whose 30 columns hold a
+// wet cell; a task whose rows are all dry in its strip is skipped (its b32 is
+// +0 already, its residuals would add exact zeros to the sums).
 template <int KIND, bool NEUMANN>
 __global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __restrict__ x, const double* __restrict__ b,
                                                             const int8_t* __restrict__ dq, StripSpace sp,
                                                             const double* __restrict__ ds, float* __restrict__ b32,
-                                                            float* __restrict__ r32, double* __restrict__ partials) {
+                                                            float* __restrict__ r32, double* __restrict__ partials,
+                                                            const uint8_t* __restrict__ sflag) {
   dep_wait();
   constexpr int q = (KIND == OPK_RESID9) ? 2 : 0;  // Q = 2^q
   const int k = fix_exponent(ds);
@@ -311,6 +315,11 @@ __global__ void __launch_bounds__(kMxThreads) k_resid_int2d(const double* __rest
     const int c = sp.c0 + strip * kIntCols + lane - 1;  // this lane's column
     const bool col_ok = lane >= 1 && lane <= kIntCols && c < sp.c0 + sp.ncols;
     const int ra = chunk * sp.rows, rb = min(ra + sp.rows, sp.nrows);
+    if (sflag) {  // warp-uniform: the task's rows of this strip, a lane a row
+      unsigned any = 0;
+      for (int r = ra + lane; r < rb; r += 32) any |= sflag[((long long)plane * sp.nrows + r) * sp.nstrips + strip];
+      if (!__any_sync(0xffffffffu, any != 0)) continue;
+    }
     const long long I0 = sp.row0 + plane * sp.n2 + (long long)ra * n1 + c;  // row ra, this lane
     const double* xp = x + I0;
     // rows ra-1 and ra converted; x of rows ra+1, ra+2 and b, dq of row ra in flight
@@ -422,9 +431,9 @@ static int int2d_grid() {
   return blocks;
 }
 
-bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t* dq, const Geom& g, const Box& bx,
-                        const double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s) {
-  StripSpace sp;
+// the strips of the 2D (and 3D strip-form) residual: false when the form
+// does not apply
+static bool strip_space(int kind, const Geom& g, const Box& bx, StripSpace& sp) {
   sp.n1 = g.n1;
   sp.n2 = g.n2;
   sp.len = g.len;
@@ -452,6 +461,14 @@ bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t
   }
   if (sp.nrows <= 0 || sp.ncols <= 0 || sp.nplanes <= 0) return false;
   sp.nstrips = (sp.ncols + kIntCols - 1) / kIntCols;
+  return true;
+}
+
+bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t* dq, const Geom& g, const Box& bx,
+                        const double* ds, float* b32, float* r32, bool neumann, double* partials, cudaStream_t s,
+                        const uint8_t* sflag) {
+  StripSpace sp;
+  if (!strip_space(kind, g, bx, sp)) return false;
 #define CFMG_INT2(K)                                                                                        \
   if (kind == K) {                                                                                          \
     const int grid = neumann ? int2d_grid<K, true>() : int2d_grid<K, false>();                             \
@@ -461,9 +478,9 @@ bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t
     rows = rows < kIntUnroll ? kIntUnroll : (rows > 96 ? 96 : rows);                                        \
     sp.rows = (int)((rows + kIntUnroll - 1) / kIntUnroll * kIntUnroll);                                     \
     if (neumann)                                                                                            \
-      launch_dep(k_resid_int2d<K, true>, grid, kMxThreads, 0, s, x, b, dq, sp, ds, b32, r32, partials);             \
+      launch_dep(k_resid_int2d<K, true>, grid, kMxThreads, 0, s, x, b, dq, sp, ds, b32, r32, partials, sflag);      \
     else                                                                                                    \
-      launch_dep(k_resid_int2d<K, false>, grid, kMxThreads, 0, s, x, b, dq, sp, ds, b32, r32, partials);            \
+      launch_dep(k_resid_int2d<K, false>, grid, kMxThreads, 0, s, x, b, dq, sp, ds, b32, r32, partials, sflag);     \
     return true;                                                                                            \
   }
   CFMG_INT2(OPK_RESID5)
@@ -471,6 +488,35 @@ bool launch_resid_int2d(int kind, const double* x, const double* b, const int8_t
   CFMG_INT2(OPK_RESID7)
 #undef CFMG_INT2
   return false;
+}
+
+// sflag[(plane * nrows + row) * nstrips + strip] = 1 when the strip's
+// columns of that row hold a wet cell
+__global__ void k_make_sflag(const uint8_t* __restrict__ m, uint8_t* __restrict__ sflag, StripSpace sp) {
+  const long long T = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = (long long)sp.nplanes * sp.nrows * sp.nstrips;
+  if (T >= n) return;
+  const int strip = (int)(T % sp.nstrips);
+  const long long pr = T / sp.nstrips;
+  const int row = (int)(pr % sp.nrows), plane = (int)(pr / sp.nrows);
+  const long long base = sp.row0 + plane * sp.n2 + (long long)row * sp.n1;
+  const int c0 = sp.c0 + strip * kIntCols, c1 = min(c0 + kIntCols, sp.c0 + sp.ncols);
+  unsigned any = 0;
+  for (int c = c0; c < c1; ++c) any |= m[base + c];
+  sflag[T] = any ? 1 : 0;
+}
+
+long long resid_sflag_size(int kind, const Geom& g, const Box& bx) {
+  StripSpace sp;
+  if (!strip_space(kind, g, bx, sp)) return 0;
+  return (long long)sp.nplanes * sp.nrows * sp.nstrips;
+}
+
+void launch_make_sflag(int kind, const uint8_t* m, uint8_t* sflag, const Geom& g, const Box& bx, cudaStream_t s) {
+  StripSpace sp;
+  if (!strip_space(kind, g, bx, sp)) return;
+  const long long n = (long long)sp.nplanes * sp.nrows * sp.nstrips;
+  k_make_sflag<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(m, sflag, sp);
 }
 
 // cell-centred second pass: b32 = r32 = msk ? b32 - mean * scale : 0 with

@@ -158,15 +158,29 @@ __global__ void __launch_bounds__(kThreads) k_restrict(const T* __restrict__ x, 
 
 // Thread per fine parent (i, j, k) = (nh+1+2p, nh+1+2q, ...); each parent
 // updates its 4 (2D) or 8 (3D) children, which no other thread touches.
+// fmsk (optional, FP32 cycles): a parent whose children are all dry is
+// skipped; a dry fine cell holds +0 and has Pcoef = 0, so the update would
+// leave it +0.
 template <class T, int KIND, bool ASSIGN>
 __global__ void __launch_bounds__(kThreads) k_prolong(T* __restrict__ xf, const T* __restrict__ x,
                                                       const T* __restrict__ coef, Geom gf, Geom gc, int np_i,
-                                                      int np_j, int kf0, int kf1, int np_k) {
+                                                      int np_j, int kf0, int kf1, int np_k,
+                                                      const uint8_t* __restrict__ fmsk) {
   dep_wait();
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const int qj = blockIdx.y * blockDim.y + threadIdx.y;
   const int qk = blockIdx.z;
-  if (p < np_i && qj < np_j && qk < np_k) d_prolong<T, KIND, ASSIGN>(xf, x, coef, gf, gc, p, qj, qk, kf0);
+  if (p >= np_i || qj >= np_j || qk >= np_k) return;
+  if (fmsk) {
+    const int nh = gf.nh;
+    const bool t3 = KIND == 1 || KIND == 3;
+    const long long F = lin(gf, nh + 1 + 2 * p, nh + 1 + 2 * qj, t3 ? nh + 1 + 2 * qk : kf0 + qk);
+    const long long f1 = gf.n1, f2 = gf.n2;
+    unsigned any = fmsk[F] | fmsk[F + 1] | fmsk[F + f1] | fmsk[F + 1 + f1];
+    if (t3) any |= fmsk[F + f2] | fmsk[F + 1 + f2] | fmsk[F + f1 + f2] | fmsk[F + 1 + f1 + f2];
+    if (!any) return;
+  }
+  d_prolong<T, KIND, ASSIGN>(xf, x, coef, gf, gc, p, qj, qk, kf0);
 }
 
 // ------------------------------------------ residual + restriction, 3D
@@ -675,9 +689,9 @@ void launch_prolong(int kind, T* xf, const T* xc, const T* Pcoef, const Geom& gf
 #define CFMG_PRO(K)                                                                                       \
   case K:                                                                                                 \
     if (assign)                                                                                           \
-      launch_dep(k_prolong<T, K, true>, grid, blk, 0, s, xf, xc, Pcoef, gf, gc, np_i, np_j, kf0, kf1, np_k);      \
+      launch_dep(k_prolong<T, K, true>, grid, blk, 0, s, xf, xc, Pcoef, gf, gc, np_i, np_j, kf0, kf1, np_k, fmsk); \
     else                                                                                                  \
-      launch_dep(k_prolong<T, K, false>, grid, blk, 0, s, xf, xc, Pcoef, gf, gc, np_i, np_j, kf0, kf1, np_k);     \
+      launch_dep(k_prolong<T, K, false>, grid, blk, 0, s, xf, xc, Pcoef, gf, gc, np_i, np_j, kf0, kf1, np_k, fmsk); \
     break;
   switch (kind) {
     CFMG_PRO(0)

@@ -131,12 +131,14 @@ extern "C" {
                                    read omega*idiag as a one-byte code diag into a 256-entry table (when
                                    every cell's code reproduces its float exactly) instead of a 4-byte
                                    float per cell; 0 the floats. Both give the same bits. */
-#define CFMG_OPT_SKIP_DRY 10 /* mixed form, 3D 7-point operator: 1 (default) the four-cell sweeps, the
-                               cell-centred prolongation, the level-1 solution update and the wet-mean
-                               shift skip groups of cells that are all dry (their FP32 fields hold +0 and
-                               stay +0; the update's max |x| of them is taken once per solve); 0 every
-                               cell. Both give the same values (a -0 left in a dry cell of x can stay -0
-                               where the full update would make it +0). */
+#define CFMG_OPT_SKIP_DRY 10 /* mixed form, closed topology: 1 (default) passes skip groups of cells
+                               that are all dry (their FP32 fields hold +0 and stay +0): the FP32
+                               prolongation's parents, the strip residual's tasks; for the 3D 7-point
+                               operator also the four-cell sweeps' quads, the staged residual's tile
+                               runs, the residual-restriction's coarse cells, the level-1 solution
+                               update (the dry cells' max |x| taken once per solve) and the wet-mean
+                               shift; 0 every cell. Both give the same values (a zero in a dry cell can
+                               keep its sign where the full pass would flip it). */
 #define CFMG_OPT_STAGED_RESIDUAL 9 /* mixed form, 3D 7-point operator, integer residual: 2 (default) the
                                       level-1 residual pass stages each plane of a 32 x 16 column tile in
                                       shared memory by TMA and converts every x once (even tx only), two

@@ -256,29 +256,46 @@ def test_staged_residual_matches_strip_residual(name):
         assert np.linalg.norm(a - c) <= 1e-8 * np.linalg.norm(c)
 
 
-@pytest.mark.parametrize("cycle", ["v", "f"])
-def test_skip_dry_is_bit_identical(cycle):
-    """Skipping groups of dry cells in the 3D passes (four-cell sweeps with
-    per-(plane run, quad) wet flags, the cell-centred prolongation, the FP64
-    update with the dry cells' max |x| taken once, the wet-mean shift) gives
-    the full passes' history and solution, on the configuration-3 recipe
-    (coastline cut by a bottom topography: most of the box dry)."""
+@pytest.mark.parametrize("case", ["3d_v", "3d_f", "2d_config2_512", "2d_config1_centers"])
+def test_skip_dry_is_bit_identical(case):
+    """Skipping groups of dry cells (3D: four-cell sweeps with per-(plane run,
+    quad) wet flags, the FP64 update with the dry cells' max |x| taken once,
+    the wet-mean shift, the staged residual's dry tile runs, the residual-
+    restriction's dry coarse cells; 2D and 3D: the prolongation's dry
+    parents, the strip residual's dry tasks) gives the full passes' history
+    and solution: on the configuration-3 recipe (coastline cut by a bottom
+    topography, most of the box dry), the configuration-2 coastline at 512^2
+    and a cell-centred disk."""
     import workloads as W
 
-    param, vmsk, noise = W.config3(64, 64, 32, nlevels=4)
-    param = dict(param, cycle=cycle)
+    if case.startswith("3d"):
+        param, vmsk, noise = W.config3(64, 64, 32, nlevels=4)
+        param = dict(param, cycle=case[-1])
+    elif case == "2d_config2_512":
+        param, vmsk, noise = W.config2(512, nlevels=4)
+    else:
+        base, _ = CASES["config1_256_centers_v"]
+        param = dict(base)
+        vmsk = None
+        noise = None
     out = []
     for skip in (1, 0):
         mg = cfmg.get_gmg(cfmg.Param(**param, tol=1e-10, maxite=60, residual_norm="l2", precision="mixed",
                                      verbose=False))
         mg.set_option("engine_cells", 2000)  # fine levels as standalone kernels
         mg.set_option("skip_dry", skip)
-        mg.oper[1].msk = vmsk
+        mg.oper[1].msk = vmsk if vmsk is not None else _mask(param, mg.shape(1), "disk")
         cfmg.setup_operators(mg)
         for lev in range(1, mg.nlevels + 1):
             for f in ("x", "y", "r", "b"):
                 cfmg.set_to_zero(mg, lev, f)
-        mg.data[1].b = W.rhs(noise, mg.download(1, "msk"))
+        if noise is not None:
+            mg.data[1].b = W.rhs(noise, mg.download(1, "msk"))
+        else:
+            msk = mg.download(1, "msk").astype(np.float64)
+            b = np.asfortranarray(np.random.default_rng(31).standard_normal(mg.shape(1))) * msk
+            F.subtract_mean(b, msk)
+            mg.data[1].b = b
         res, n, hist = cfmg.solve(mg, history=True)
         out.append((res, n, hist, mg.data[1].x))
         mg.close()
