@@ -440,12 +440,13 @@ __global__ void __launch_bounds__(256) k_sweep7_3d_q4(const float* __restrict__ 
                                                       long long n2, int tz, const uint8_t* __restrict__ qact) {
   __shared__ float tab[256];
   dep_wait();
-  tab[threadIdx.x] = wtab[threadIdx.x];
-  __syncthreads();
   const long long t = (long long)blockIdx.x * 256 + threadIdx.x;  // quad of the plane
   const int k0 = 1 + blockIdx.y * kQRun;
-  if (4 * t >= n2 || k0 > tz - 2) return;
-  if (qact && !qact[(long long)blockIdx.y * (n2 >> 2) + t]) return;
+  const bool live = 4 * t < n2 && k0 <= tz - 2 && (!qact || qact[(long long)blockIdx.y * (n2 >> 2) + t]);
+  if (!__syncthreads_or(live)) return;  // a block of dry quads reads nothing more
+  tab[threadIdx.x] = wtab[threadIdx.x];
+  __syncthreads();
+  if (!live) return;
   const int k1 = min(k0 + kQRun, tz - 1);
   typedef Ar<float> A;
   long long I = 4 * t + n2 * k0;
