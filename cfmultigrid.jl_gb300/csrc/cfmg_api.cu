@@ -80,6 +80,7 @@ struct cfmg_handle {
   // CFMG_OPT_SKIP_DRY: 3D mixed passes skip groups of dry cells (their FP32
   // fields hold +0 and stay +0)
   bool dry_on = true;
+  bool small_on = true;  // CFMG_OPT_SMALL_SMOOTH
   bool host_loop = false;  // CFMG_OPT_HOST_LOOP
   // call order: the operators' coefficients exist once cfmg_setup_operators,
   // cfmg_bind_level or an upload of a coefficient field ran; cfmg_adjoint
@@ -508,9 +509,51 @@ int smooth_tb(cfmg_handle* h, int lev, int nite) {
 }
 
 // mg.smoother[lev] (src/gmg_setup.jl:124-139 selects among these)
+// A long smoothing call (the coarsest solve) on a level whose four arrays fit
+// one block's shared memory runs as one block (k_small_smooth) instead of
+// 2*nite engine Ops: the pending Ops before it are flushed as their own
+// program. Closed topology, the 5- and 2D 9-point and the 3D 7-point
+// operators.
+template <class T>
+bool small_smooth_ok(const cfmg_handle* h, int lev, int nite) {
+  if (h->record || xperio(h) || nite < 4 || !h->small_on) return false;
+  if (!(h->d.op == CFMG_LAPLACIAN || (h->d.op == CFMG_LAPLACIAN9 && !threed(h)))) return false;
+  if (sizeof(T) == 4 && lev == 1 && h->x1_zero) return false;  // that sweep must not read x
+  const Level& l = h->lv[lev - 1];
+  if (l.xswap) return false;
+  const size_t lo = threed(h) ? (size_t)l.tx * l.ty : (size_t)l.tx;  // the linear ranges start here
+  return 4 * l.len * sizeof(T) <= kSmallSmemMax && l.len > 2 * lo;
+}
+
+template <class T>
+int small_smooth_run(cfmg_handle* h, int lev, int nite) {
+  const Level& l = h->lv[lev - 1];
+  const View<T> v = view<T>(l);
+  TRY(flush(h));
+  SmallSm s;
+  std::memset(&s, 0, sizeof(s));
+  s.x = const_cast<T*>(v.x);
+  s.y = const_cast<T*>(v.y);
+  s.b = v.b;
+  s.w = v.widiag;
+  s.g = geom(l);
+  s.stencil = threed(h) ? 7 : (h->d.op == CFMG_LAPLACIAN9 ? 9 : 5);
+  s.npairs = nite;
+  s.ext = Box{l.nh, l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, 1, l.nz};
+  s.in = interior(l);
+  s.cff = 1.0 - h->d.omega;
+  {
+    Launch k(h, CFMG_K_SWEEP, lev, pc<T>() ? CFMG_MIXED : CFMG_FP64);
+    launch_small_smooth<T>(s, h->stream);
+  }
+  LAUNCH_OK(h);
+  return CFMG_OK;
+}
+
 template <class T>
 int smooth_t(cfmg_handle* h, int lev, int nite) {
   if (tb_eligible<T>(h, lev)) return smooth_tb(h, lev, nite);
+  if (small_smooth_ok<T>(h, lev, nite)) return small_smooth_run<T>(h, lev, nite);
   const Level& l = h->lv[lev - 1];
   View<T> v = view<T>(l);
   if (h->d.op == CFMG_LAPLACIAN9 && threed(h)) {
@@ -2726,6 +2769,11 @@ int cfmg_set_option(cfmg_handle* h, int option, long long value) {
   }
   if (option == CFMG_OPT_FUSED_UPDATE) {
     h->upd_on = value != 0;
+    drop_graphs(h);
+    return CFMG_OK;
+  }
+  if (option == CFMG_OPT_SMALL_SMOOTH) {
+    h->small_on = value != 0;
     drop_graphs(h);
     return CFMG_OK;
   }

@@ -105,6 +105,21 @@ void launch_sweep7_3d_q(const float* x, float* y, const float* b, const uint8_t*
 constexpr int kQRunPlanes = 4;
 void launch_make_qact(const uint8_t* m, uint8_t* qact, long long n2, int tz, int run, cudaStream_t s);
 bool sweep7_quad_ok(const Geom& g, const void* x, const void* y, const void* b, const void* wq);
+// one smoothing call (npairs pairs) of a level held in one block's shared
+// memory (k_ops.cu); stencil 5 (2D 5-point), 9 (2D 9-point), 7 (3D 7-point)
+struct SmallSm {
+  void* x;
+  void* y;
+  const void* b;
+  const void* w;
+  Geom g;
+  int stencil, npairs;
+  Box ext, in;
+  double cff;
+};
+constexpr size_t kSmallSmemMax = 200 * 1024;  // 4 arrays of the level
+template <class T>
+void launch_small_smooth(const SmallSm& s, cudaStream_t st);
 // FP32 3D 7-point cell-centred residual at the children of the coarse box cb
 // restricted into the coarse b (k_ops.cu); dc: diag as one-byte codes
 void launch_resid_restrict7c(const float* x, const float* b, const uint8_t* dc, const uint8_t* m, const float* rcoef,

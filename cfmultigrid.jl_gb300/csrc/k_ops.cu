@@ -307,6 +307,76 @@ __global__ void __launch_bounds__(256) k_prolong3c_f(float* __restrict__ xf, con
     }
 }
 
+// ------------------------------------------- small level in shared memory
+// A smoothing call of npairs pairs on a level whose x, y, b and omega*idiag
+// fit one block's shared memory (the coarsest solve: 2*ndeepest sweeps on a
+// few hundred cells): one block loads the four arrays, runs every sweep with
+// a block barrier between sweeps, and writes x and y back. Launched as the
+// engine's separate Ops, each sweep would cost a cluster barrier and the
+// round trip through L2. The sweep ranges and the per-cell arithmetic are
+// smooth_t's: the linear range n1 .. len-n1 with v_sweep5 (2D 5-point), the
+// box icp x jcp then the interior with v_sweep9 (2D 9-point), the linear
+// range n2 .. len-n2 with v_sweep7 (3D 7-point); Jacobi sweeps, so the order
+// of the cells within a sweep does not matter, and the bits are the same.
+constexpr int kSmallThreads = 1024;
+template <class T>
+__global__ void __launch_bounds__(kSmallThreads) k_small_smooth(SmallSm s) {
+  dep_wait();
+  extern __shared__ __align__(16) unsigned char ssm_raw[];
+  const long long len = s.g.len;
+  T* X = reinterpret_cast<T*>(ssm_raw);
+  T* Y = X + len;
+  T* B = Y + len;
+  T* W = B + len;
+  for (long long t = threadIdx.x; t < len; t += blockDim.x) {
+    X[t] = static_cast<const T*>(s.x)[t];
+    Y[t] = static_cast<const T*>(s.y)[t];
+    B[t] = static_cast<const T*>(s.b)[t];
+    W[t] = static_cast<const T*>(s.w)[t];
+  }
+  __syncthreads();
+  const T cff = (T)s.cff;
+  const long long n1 = s.g.n1, n2 = s.g.n2;
+  auto sweep = [&](const T* src, T* dst, bool first) {
+    if (s.stencil == 5) {
+      for (long long I = n1 + threadIdx.x; I < len - n1; I += blockDim.x) dst[I] = v_sweep5(src, B, W, cff, n1, I);
+    } else if (s.stencil == 7) {
+      for (long long I = n2 + threadIdx.x; I < len - n2; I += blockDim.x) dst[I] = v_sweep7(src, B, W, cff, n1, n2, I);
+    } else {
+      const Box& bx = first ? s.ext : s.in;
+      const int ni = bx.i1 - bx.i0 + 1, nj = bx.j1 - bx.j0 + 1;
+      const long long n = (long long)ni * nj * (bx.k1 - bx.k0 + 1);
+      for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+        const int i = bx.i0 + (int)(t % ni);
+        const long long q = t / ni;
+        const long long I = lin(s.g, i, bx.j0 + (int)(q % nj), bx.k0 + (int)(q / nj));
+        dst[I] = v_sweep9(src, B, W, cff, n1, I);
+      }
+    }
+    __syncthreads();
+  };
+  for (int p = 0; p < s.npairs; ++p) {
+    sweep(X, Y, true);
+    sweep(Y, X, false);
+  }
+  for (long long t = threadIdx.x; t < len; t += blockDim.x) {
+    static_cast<T*>(s.x)[t] = X[t];
+    static_cast<T*>(s.y)[t] = Y[t];
+  }
+}
+template <class T>
+void launch_small_smooth(const SmallSm& s, cudaStream_t st) {
+  const size_t smem = 4 * (size_t)s.g.len * sizeof(T);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_small_smooth<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmemMax);
+    attr = true;
+  }
+  launch_dep(k_small_smooth<T>, 1, kSmallThreads, smem, st, s);
+}
+template void launch_small_smooth<double>(const SmallSm&, cudaStream_t);
+template void launch_small_smooth<float>(const SmallSm&, cudaStream_t);
+
 // ------------------------------------------------------------------- halo
 // fill! for :xperio (src/halo.jl:6-9). One thread per (j,k) line copies the
 // nh columns through registers, so the copies of each statement read

@@ -303,6 +303,37 @@ def test_skip_dry_is_bit_identical(case):
     assert np.array_equal(out[0][2], out[1][2]) and np.array_equal(out[0][3], out[1][3])
 
 
+@pytest.mark.parametrize("name", ["config1_256_centers_v", "config2_512_vertices_lap9_f", "3d_48_centers_v",
+                                  "3d_32_vertices_v", "2d_twolayer_256_centers_v"])
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_small_smooth_is_bit_identical(name, precision):
+    """The coarsest solve run by one block in shared memory (the default for
+    small levels) gives the engine's separate sweeps' history and solution
+    bit for bit, in the mixed form (FP64 or FP32 coarsest) and the FP64
+    drop-in."""
+    base, mkind = {**CASES, **BIG_CASES}[name]
+    out = []
+    for small in (1, 0):
+        mg = cfmg.get_gmg(cfmg.Param(**base, tol=1e-10, maxite=40, residual_norm="l2", precision=precision,
+                                     verbose=False))
+        mg.set_option("small_smooth", small)
+        custom = _mask(base, mg.shape(1), mkind)
+        if custom is not None:
+            mg.oper[1].msk = custom
+            cfmg.setup_operators(mg)
+            for lev in range(1, mg.nlevels + 1):
+                for f in ("x", "y", "r", "b"):
+                    cfmg.set_to_zero(mg, lev, f)
+        msk = mg.download(1, "msk").astype(np.float64)
+        b = np.asfortranarray(np.random.default_rng(33).standard_normal(mg.shape(1))) * msk
+        F.subtract_mean(b, msk)
+        mg.data[1].b = b
+        res, n, hist = cfmg.solve(mg, history=True)
+        out.append((res, n, hist, mg.data[1].x))
+    assert out[0][1] == out[1][1] and out[0][0] == out[1][0]
+    assert np.array_equal(out[0][2], out[1][2]) and np.array_equal(out[0][3], out[1][3])
+
+
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_solve_graph_matches_host_loop(precision):
     """The whole solve! loop as one graph launch (a while node with the
