@@ -80,7 +80,7 @@ struct cfmg_handle {
   // CFMG_OPT_SKIP_DRY: 3D mixed passes skip groups of dry cells (their FP32
   // fields hold +0 and stay +0)
   bool dry_on = true;
-  bool small_on = true;  // CFMG_OPT_SMALL_SMOOTH
+  int small_min = 4;  // CFMG_OPT_SMALL_SMOOTH: fewest pairs of a call run in one block (0: never)
   bool host_loop = false;  // CFMG_OPT_HOST_LOOP
   // call order: the operators' coefficients exist once cfmg_setup_operators,
   // cfmg_bind_level or an upload of a coefficient field ran; cfmg_adjoint
@@ -516,7 +516,7 @@ int smooth_tb(cfmg_handle* h, int lev, int nite) {
 // operators.
 template <class T>
 bool small_smooth_ok(const cfmg_handle* h, int lev, int nite) {
-  if (h->record || xperio(h) || nite < 4 || !h->small_on) return false;
+  if (h->record || xperio(h) || h->small_min <= 0 || nite < h->small_min) return false;
   if (!(h->d.op == CFMG_LAPLACIAN || (h->d.op == CFMG_LAPLACIAN9 && !threed(h)))) return false;
   if (sizeof(T) == 4 && lev == 1 && h->x1_zero) return false;  // that sweep must not read x
   const Level& l = h->lv[lev - 1];
@@ -2773,7 +2773,8 @@ int cfmg_set_option(cfmg_handle* h, int option, long long value) {
     return CFMG_OK;
   }
   if (option == CFMG_OPT_SMALL_SMOOTH) {
-    h->small_on = value != 0;
+    if (value < 0) return fail(h, CFMG_ERR_ARG, "small_smooth must be >= 0");
+    h->small_min = (int)value;
     drop_graphs(h);
     return CFMG_OK;
   }

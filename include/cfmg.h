@@ -131,10 +131,10 @@ extern "C" {
                                    read omega*idiag as a one-byte code diag into a 256-entry table (when
                                    every cell's code reproduces its float exactly) instead of a 4-byte
                                    float per cell; 0 the floats. Both give the same bits. */
-#define CFMG_OPT_SMALL_SMOOTH 11 /* closed topology, 5-, 2D 9- and 3D 7-point operators: 1 (default) a
-                                     smoothing call of at least 4 pairs (the coarsest solve) on a level
-                                     whose x, y, b and omega*idiag fit 200 KB runs as one block in shared
-                                     memory; 0 as separate sweeps. Both give the same bits. */
+#define CFMG_OPT_SMALL_SMOOTH 11 /* closed topology, 5-, 2D 9- and 3D 7-point operators: a smoothing
+                                     call of at least this many pairs (default 4: the coarsest solve) on
+                                     a level whose x, y, b and omega*idiag fit 200 KB runs as one block in
+                                     shared memory; 0 never (separate sweeps). The same bits. */
 #define CFMG_OPT_SKIP_DRY 10 /* mixed form, closed topology: 1 (default) passes skip groups of cells
                                that are all dry (their FP32 fields hold +0 and stay +0): the FP32
                                prolongation's parents, the strip residual's tasks; for the 3D 7-point
