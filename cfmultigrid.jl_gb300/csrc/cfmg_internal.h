@@ -118,6 +118,9 @@ struct SmallSm {
   double cff;
 };
 constexpr size_t kSmallSmemMax = 200 * 1024;  // 4 arrays of the level
+// FP64 levels of at least this many cells run on a cluster of 8 CTAs (the
+// FP64 pipe of one SM bounds the one-block form)
+constexpr long long kSmallCluMinCells = 512;
 template <class T>
 void launch_small_smooth(const SmallSm& s, cudaStream_t st);
 // FP32 3D 7-point cell-centred residual at the children of the coarse box cb

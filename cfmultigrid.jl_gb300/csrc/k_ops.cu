@@ -364,13 +364,125 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_smooth(SmallSm s) {
     static_cast<T*>(s.y)[t] = Y[t];
   }
 }
+// The same on kSmallCtas SMs (FP64, where one SM's FP64 pipe bounds the
+// one-block form): a cluster whose CTAs each hold the whole level in their
+// shared memory and sweep one contiguous share of the swept cells, storing
+// each new value into their own copy and, through distributed shared memory,
+// into every other CTA's copy; a cluster barrier (release/acquire) ends each
+// sweep, after which every copy is the full new iterate. Each CTA writes its
+// share of x and y back. The cells and their arithmetic are the one-block
+// form's.
+constexpr int kSmallCtas = 8, kSmallCluThreads = 256;
+__device__ __forceinline__ unsigned small_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void small_cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void st_remote(double* local, unsigned rank, double v) {
+  unsigned a = (unsigned)__cvta_generic_to_shared(local), ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+  asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(ra), "d"(v) : "memory");
+}
+__global__ void __launch_bounds__(kSmallCluThreads) k_small_smooth_cluster(SmallSm s) {
+  dep_wait();
+  typedef double T;
+  extern __shared__ __align__(16) unsigned char ssm_raw[];
+  const long long len = s.g.len;
+  T* X = reinterpret_cast<T*>(ssm_raw);
+  T* Y = X + len;
+  T* B = Y + len;
+  T* W = B + len;
+  for (long long t = threadIdx.x; t < len; t += blockDim.x) {
+    X[t] = static_cast<const T*>(s.x)[t];
+    Y[t] = static_cast<const T*>(s.y)[t];
+    B[t] = static_cast<const T*>(s.b)[t];
+    W[t] = static_cast<const T*>(s.w)[t];
+  }
+  small_cluster_barrier();  // every copy loaded before any CTA stores into another's
+  const unsigned rank = small_rank();
+  const T cff = (T)s.cff;
+  const long long n1 = s.g.n1, n2 = s.g.n2;
+  // the swept cells of a sweep as an index space 0 .. n-1 -> cell I
+  auto space = [&](bool first, long long& n) {
+    if (s.stencil == 5) n = len - 2 * n1;
+    else if (s.stencil == 7) n = len - 2 * n2;
+    else {
+      const Box& bx = first ? s.ext : s.in;
+      n = (long long)(bx.i1 - bx.i0 + 1) * (bx.j1 - bx.j0 + 1) * (bx.k1 - bx.k0 + 1);
+    }
+  };
+  auto cell = [&](bool first, long long t) -> long long {
+    if (s.stencil == 5) return n1 + t;
+    if (s.stencil == 7) return n2 + t;
+    const Box& bx = first ? s.ext : s.in;
+    const int ni = bx.i1 - bx.i0 + 1, nj = bx.j1 - bx.j0 + 1;
+    const long long q = t / ni;
+    return lin(s.g, bx.i0 + (int)(t % ni), bx.j0 + (int)(q % nj), bx.k0 + (int)(q / nj));
+  };
+  auto sweep = [&](const T* src, T* dst, bool first) {
+    long long n;
+    space(first, n);
+    const long long a = n * rank / kSmallCtas, e = n * (rank + 1) / kSmallCtas;
+    for (long long t = a + threadIdx.x; t < e; t += blockDim.x) {
+      const long long I = cell(first, t);
+      const T v = s.stencil == 5 ? v_sweep5(src, B, W, cff, n1, I)
+                                 : (s.stencil == 7 ? v_sweep7(src, B, W, cff, n1, n2, I) : v_sweep9(src, B, W, cff, n1, I));
+      for (unsigned r = 0; r < kSmallCtas; ++r) {
+        if (r == rank) dst[I] = v;
+        else st_remote(dst + I, r, v);
+      }
+    }
+    small_cluster_barrier();
+  };
+  for (int p = 0; p < s.npairs; ++p) {
+    sweep(X, Y, true);
+    sweep(Y, X, false);
+  }
+  // each CTA writes back the cells it swept (the others are unchanged)
+  for (int f = 0; f < 2; ++f) {
+    long long n;
+    space(f == 0, n);
+    const long long a = n * rank / kSmallCtas, e = n * (rank + 1) / kSmallCtas;
+    for (long long t = a + threadIdx.x; t < e; t += blockDim.x) {
+      const long long I = cell(f == 0, t);
+      if (f == 0) static_cast<T*>(s.y)[I] = Y[I];
+      else static_cast<T*>(s.x)[I] = X[I];
+    }
+  }
+}
+
 template <class T>
 void launch_small_smooth(const SmallSm& s, cudaStream_t st) {
   const size_t smem = 4 * (size_t)s.g.len * sizeof(T);
-  static bool attr = false;
+  static bool attr = false, attr_c = false;
   if (!attr) {
     cudaFuncSetAttribute(k_small_smooth<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmemMax);
     attr = true;
+  }
+  if (sizeof(T) == 8 && s.g.len >= kSmallCluMinCells) {
+    if (!attr_c) {
+      cudaFuncSetAttribute(k_small_smooth_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmemMax);
+      attr_c = true;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kSmallCtas, 1, 1);
+    cfg.blockDim = dim3(kSmallCluThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[2];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = kSmallCtas;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = tl_dep_launch ? 2 : 1;
+    cudaLaunchKernelEx(&cfg, k_small_smooth_cluster, s);
+    return;
   }
   launch_dep(k_small_smooth<T>, 1, kSmallThreads, smem, st, s);
 }
