@@ -129,7 +129,10 @@ struct cfmg_batch {
   Op* sops = nullptr;          // the Ops of all cycle steps (device)
   int4* stab = nullptr;        // their chunk (or tile) tables {Op, chunk, instance, 0} (device)
   BSmall* ssm = nullptr;       // small-level smoothing descriptors (device)
+  int2* rent = nullptr;        // coarse-run entries {0, Op} / {1, BSmall} (device)
+  int4* runs = nullptr;        // coarse runs {instance, first entry, end entry, 0} (device)
   bool host_loop = false;      // CFMG_BOPT_HOST_LOOP
+  bool coarse_runs = true;     // CFMG_BOPT_COARSE_RUNS
   bool int_all = false;        // every instance has the integer residual form
   int4* ttab = nullptr;        // its warp tasks {instance, strip, row chunk, 0}
   long long* tstart = nullptr; // first task of each instance (ninst + 1)
@@ -137,10 +140,11 @@ struct cfmg_batch {
   int kind = 0;
   bool neumann = false;
   struct Step {
-    int tb, stencil, nite;     // tb: OPK_TB Ops of one (stencil, nite); tb == 2: BSmall blocks
-    long long tab0;            // offset into stab (or ssm)
-    long long nchunks;         // table entries (or BSmall blocks)
-    int smem;                  // BSmall: shared memory bytes
+    int tb, stencil, nite;     // tb: OPK_TB Ops of one (stencil, nite), 1 scalar tiles, 4 lean packed
+                               // tiles; 2: BSmall blocks; 3: coarse runs
+    long long tab0;            // offset into stab (or ssm, or runs)
+    long long nchunks;         // table entries (or BSmall blocks, or runs)
+    int smem;                  // BSmall, coarse runs: shared memory bytes
   };
   std::vector<Step> steps;
 };
@@ -481,7 +485,9 @@ int smooth_tb(cfmg_handle* h, int lev, int nite) {
       op.box = Box{l.nh, l.nx + l.nh + 1, l.nh, l.ny + l.nh + 1, 1, l.tz};
       op.np_i = n;
       op.np_j = stencil;
-      tb_tiles(n, op.box.i0, op.box.i1, op.box.j0, op.box.j1, &op.kf0, &op.kf1);
+      op.form = h->tb_version >= 5 ? 5 : 1;  // the tile form of the standalone passes
+      if (op.form == 5) tb5_tiles(n, op.box.i0, op.box.i1, op.box.j0, op.box.j1, &op.kf0, &op.kf1);
+      else tb_tiles(n, op.box.i0, op.box.i1, op.box.j0, op.box.j1, &op.kf0, &op.kf1);
       op.n = (long long)op.kf0 * op.kf1 * l.tz;
       h->pending.push_back(op);
       l.xswap ^= 1;
@@ -2358,8 +2364,13 @@ int lockstep_body(cfmg_batch* b) {
     if (b->neumann) launch_brhs(b->bi, b->l1tab, b->l1chunks, b->active, b->stream);
   }
   for (const cfmg_batch::Step& st : b->steps) {
-    if (st.tb == 2) {
+    if (st.tb == 3) {
+      launch_brun(b->sops, b->ssm, b->rent, b->runs + st.tab0, (int)st.nchunks, st.smem, b->active, b->stream);
+    } else if (st.tb == 2) {
       launch_bsmall(b->ssm + st.tab0, (int)st.nchunks, st.smem, b->active, b->stream);
+    } else if (st.tb == 4) {
+      if (!launch_btb5(st.stencil, st.nite, b->sops, b->stab + st.tab0, st.nchunks, b->active, b->stream))
+        return bfail(b, CFMG_ERR_UNSUPPORTED, "blocked pass shape");
     } else if (st.tb) {
       if (!launch_btb(st.stencil, st.nite, b->sops, b->stab + st.tab0, st.nchunks, b->active, b->stream))
         return bfail(b, CFMG_ERR_UNSUPPORTED, "blocked pass shape");
@@ -2394,12 +2405,18 @@ int lockstep_build(cfmg_batch* b) {
   else vsteps_v(vs, d, D, false);
   std::vector<std::vector<std::vector<Op>>> rec(ninst);  // [inst][step] -> Ops
   std::vector<std::vector<BSmall>> smalls(vs.size());     // [step] -> small-level smoothing blocks
+  // [inst][step]: the instance takes part in the step / the step is on one
+  // of its coarse levels (at most its engine threshold), which run as
+  // coarse runs when CFMG_BOPT_COARSE_RUNS is on
+  std::vector<std::vector<char>> part(ninst), coarse(ninst);
   for (int i = 0; i < ninst; ++i) {
     cfmg_handle* h = b->inst[i];
     for (int pass = 0; pass < 2; ++pass) {
       h->record_tb = pass == 0;
       for (Level& l : h->lv) l.xswap = 0;
       rec[i].assign(vs.size(), {});
+      part[i].assign(vs.size(), 0);
+      coarse[i].assign(vs.size(), 0);
       for (auto& sm : smalls)
         sm.erase(std::remove_if(sm.begin(), sm.end(), [&](const BSmall& q) { return q.inst == i; }), sm.end());
       for (size_t k = 0; k < vs.size(); ++k) {
@@ -2407,6 +2424,9 @@ int lockstep_build(cfmg_batch* b) {
         if (L(h) < v.need) continue;
         if (k == 0) v.depth = L(h);
         if (L(h) == 1 && v.op != V_ZERO && v.op != V_COARSEST) continue;
+        part[i][k] = 1;
+        const Level& lv = h->lv[L(h) - v.depth];  // the step's level (the finer one of a transfer)
+        coarse[i][k] = b->coarse_runs && h->engine_on && (long long)lv.len <= engine_limit(h, CFMG_MIXED);
         BSmall sm;
         if (L(h) > 1 && small_smooth(h, v, sm)) {
           sm.inst = i;
@@ -2415,7 +2435,10 @@ int lockstep_build(cfmg_batch* b) {
         }
         int rc = record_vstep(h, v, rec[i][k]);
         if (rc != CFMG_OK) return bfail(b, rc, "instance " + std::to_string(i) + ": " + h->err);
-        for (Op& op : rec[i][k]) op.inst = i;
+        for (Op& op : rec[i][k]) {
+          op.inst = i;
+          if (op.kind == OPK_TB) coarse[i][k] = 0;  // blocked passes keep their own kernel
+        }
       }
       bool home = true;
       for (const Level& l : h->lv) home = home && l.xswap == 0;
@@ -2443,32 +2466,78 @@ int lockstep_build(cfmg_batch* b) {
     b->steps.push_back(st);
   };
   std::vector<BSmall> all_small;
+  // coarse runs: an instance's consecutive coarse steps collect in pend[i]
+  // and all collected runs go out as one launch (one block per run) before
+  // the first step that some instance with a run takes on a larger level.
+  // Instances are independent, so only each instance's own order matters.
+  std::vector<int2> rent;
+  std::vector<int4> runs;
+  std::vector<std::vector<int2>> pend(ninst);
+  std::vector<int> pend_smem(ninst, 0);
+  auto small_bytes = [](const BSmall& q) { return (int)(4 * q.g.len * (q.prec == 0 ? 8 : 4)); };
+  auto flush_runs = [&]() {
+    cfmg_batch::Step st;
+    st.tb = 3; st.stencil = 0; st.nite = 0; st.smem = 0;
+    st.tab0 = (long long)runs.size();
+    for (int i = 0; i < ninst; ++i) {
+      if (pend[i].empty()) continue;
+      runs.push_back(make_int4(i, (int)rent.size(), (int)(rent.size() + pend[i].size()), 0));
+      rent.insert(rent.end(), pend[i].begin(), pend[i].end());
+      st.smem = std::max(st.smem, pend_smem[i]);
+      pend[i].clear();
+      pend_smem[i] = 0;
+    }
+    st.nchunks = (long long)runs.size() - st.tab0;
+    if (st.nchunks > 0) b->steps.push_back(st);
+  };
   for (size_t k = 0; k < vs.size(); ++k) {
-    if (!smalls[k].empty()) {  // independent of the other instances' Ops of this step
+    bool cut = false;
+    for (int i = 0; i < ninst && !cut; ++i) cut = part[i][k] && !coarse[i][k] && !pend[i].empty();
+    if (cut) flush_runs();
+    std::vector<BSmall> fine_small;
+    for (const BSmall& q : smalls[k]) {
+      if (!coarse[q.inst][k]) {
+        fine_small.push_back(q);
+        continue;
+      }
+      pend[q.inst].push_back(make_int2(1, (int)all_small.size()));
+      pend_smem[q.inst] = std::max(pend_smem[q.inst], small_bytes(q));
+      all_small.push_back(q);
+    }
+    for (int i = 0; i < ninst; ++i) {
+      if (!coarse[i][k]) continue;
+      for (const Op& op : rec[i][k]) {
+        pend[i].push_back(make_int2(0, (int)all.size()));
+        all.push_back(op);
+      }
+    }
+    if (!fine_small.empty()) {  // independent of the other instances' Ops of this step
       cfmg_batch::Step st;
       st.tb = 2; st.stencil = 0; st.nite = 0;
       st.tab0 = (long long)all_small.size();
-      st.nchunks = (long long)smalls[k].size();
+      st.nchunks = (long long)fine_small.size();
       st.smem = 0;
-      for (const BSmall& q : smalls[k]) st.smem = std::max(st.smem, (int)(4 * q.g.len * (q.prec == 0 ? 8 : 4)));
-      all_small.insert(all_small.end(), smalls[k].begin(), smalls[k].end());
+      for (const BSmall& q : fine_small) st.smem = std::max(st.smem, small_bytes(q));
+      all_small.insert(all_small.end(), fine_small.begin(), fine_small.end());
       b->steps.push_back(st);
     }
     size_t depth = 0;
-    for (int i = 0; i < ninst; ++i) depth = std::max(depth, rec[i][k].size());
+    for (int i = 0; i < ninst; ++i)
+      if (!coarse[i][k]) depth = std::max(depth, rec[i][k].size());
     for (size_t q = 0; q < depth; ++q) {
       std::vector<Op> gen;
-      std::vector<std::vector<Op>> tbs(8);  // [stencil 9?][pairs]
+      std::vector<std::vector<Op>> tbs(16);  // [lean packed form?][stencil 9?][pairs]
       for (int i = 0; i < ninst; ++i) {
-        if (q >= rec[i][k].size()) continue;
+        if (coarse[i][k] || q >= rec[i][k].size()) continue;
         const Op& op = rec[i][k][q];
-        if (op.kind == OPK_TB) tbs[(op.np_j == 9 ? 4 : 0) + op.np_i].push_back(op);
+        if (op.kind == OPK_TB) tbs[(op.form == 5 ? 8 : 0) + (op.np_j == 9 ? 4 : 0) + op.np_i].push_back(op);
         else gen.push_back(op);
       }
-      for (int t = 0; t < 8; ++t) add_step(tbs[t], 1, t >= 4 ? 9 : 5, t & 3);
+      for (int t = 0; t < 16; ++t) add_step(tbs[t], t >= 8 ? 4 : 1, (t & 4) ? 9 : 5, t & 3);
       add_step(gen, 0, 0, 0);
     }
   }
+  flush_runs();  // the cycle's last coarse steps
   // level-1 state and chunks
   std::vector<BInst> hb(ninst);
   std::vector<long long> l1(ninst + 1, 0);
@@ -2550,9 +2619,17 @@ int lockstep_build(cfmg_batch* b) {
     BCUDA(b, cudaMalloc((void**)&b->ssm, sizeof(BSmall) * all_small.size()));
     BCUDA(b, cudaMemcpy(b->ssm, all_small.data(), sizeof(BSmall) * all_small.size(), cudaMemcpyHostToDevice));
   }
+  if (!runs.empty()) {
+    BCUDA(b, cudaMalloc((void**)&b->rent, sizeof(int2) * rent.size()));
+    BCUDA(b, cudaMemcpy(b->rent, rent.data(), sizeof(int2) * rent.size(), cudaMemcpyHostToDevice));
+    BCUDA(b, cudaMalloc((void**)&b->runs, sizeof(int4) * runs.size()));
+    BCUDA(b, cudaMemcpy(b->runs, runs.data(), sizeof(int4) * runs.size(), cudaMemcpyHostToDevice));
+  }
   if (!all.empty()) {
     BCUDA(b, cudaMalloc((void**)&b->sops, sizeof(Op) * all.size()));
     BCUDA(b, cudaMemcpy(b->sops, all.data(), sizeof(Op) * all.size(), cudaMemcpyHostToDevice));
+  }
+  if (!tab.empty()) {  // every step may be a coarse run (instances of a few levels)
     BCUDA(b, cudaMalloc((void**)&b->stab, sizeof(int4) * tab.size()));
     BCUDA(b, cudaMemcpy(b->stab, tab.data(), sizeof(int4) * tab.size(), cudaMemcpyHostToDevice));
   }
@@ -2646,7 +2723,7 @@ int cfmg_batch_destroy(cfmg_batch* b) {
   for (void* p : {(void*)b->progs, (void*)b->ptrs, (void*)b->nops, (void*)b->counter, (void*)b->red, (void*)b->sc,
                   (void*)b->nwet, (void*)b->bi, (void*)b->l1start, (void*)b->l1tab, (void*)b->bpart,
                   (void*)b->active, (void*)b->nactive, (void*)b->sops, (void*)b->stab, (void*)b->ssm,
-                  (void*)b->ttab, (void*)b->tstart})
+                  (void*)b->ttab, (void*)b->tstart, (void*)b->rent, (void*)b->runs})
     if (p) cudaFree(p);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
@@ -2665,6 +2742,11 @@ int cfmg_batch_set_option(cfmg_batch* b, int option, long long value) {
   if (!b) return CFMG_ERR_ARG;
   if (option == CFMG_BOPT_HOST_LOOP) {
     b->host_loop = value != 0;
+    return CFMG_OK;
+  }
+  if (option == CFMG_BOPT_COARSE_RUNS) {
+    if (b->coarse_runs != (value != 0)) b->built = false;  // the iteration's launches change
+    b->coarse_runs = value != 0;
     return CFMG_OK;
   }
   return bfail(b, CFMG_ERR_ARG, "unknown batch option");
@@ -2687,7 +2769,8 @@ int cfmg_batch_solve(cfmg_batch* b, int zero_x, double* res, int* nite, double* 
     for (void** p : {(void**)&b->progs, (void**)&b->ptrs, (void**)&b->nops, (void**)&b->counter, (void**)&b->red,
                      (void**)&b->sc, (void**)&b->nwet, (void**)&b->bi, (void**)&b->l1start, (void**)&b->l1tab,
                      (void**)&b->bpart, (void**)&b->active, (void**)&b->nactive, (void**)&b->sops,
-                     (void**)&b->stab, (void**)&b->ssm, (void**)&b->ttab, (void**)&b->tstart})
+                     (void**)&b->stab, (void**)&b->ssm, (void**)&b->ttab, (void**)&b->tstart, (void**)&b->rent,
+                     (void**)&b->runs})
       if (*p) {
         cudaFree(*p);
         *p = nullptr;

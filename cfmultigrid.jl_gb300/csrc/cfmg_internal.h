@@ -236,6 +236,7 @@ struct Op {
   const uint8_t* wq;
   const float* wtab;
   const uint8_t* qact;  // the level's quad activity flags (see Level), or null: every quad swept
+  int form;  // OPK_TB: 5 the lean packed tiles (k_btb5), else the scalar tiles (k_btb)
 };
 // scalar block of a whole-solve program
 enum SolveSlot { SS_NORMB = 0, SS_NR, SS_RES, SS_NITE, SS_NWET, SS_MEAN, SS_SCALE, SS_ISCALE, SS_T0, SS_T1,
@@ -344,6 +345,12 @@ struct BSmall {
 };
 constexpr int kBSmallBytes = 96 * 1024;  // shared memory of one block: 4 arrays
 void launch_bsmall(const BSmall* s, int n, int smem, const int* active, cudaStream_t st);
+// Coarse runs: one block per run {instance, first entry, end entry, 0}
+// executes the instance's consecutive coarse-level steps in order, entries
+// {0, Op} or {1, BSmall}; smem = the largest BSmall staging of the runs.
+constexpr int kBRunThreads = 512;
+void launch_brun(const Op* ops, const BSmall* sm, const int2* ent, const int4* runs, int nruns, int smem,
+                 const int* active, cudaStream_t st);
 
 // Work tables: one int4 per chunk (or tile) = {Op or instance, chunk of it,
 // instance, 0}; a launch compacts the active entries of each window.
@@ -351,6 +358,10 @@ void launch_bstage(const Op* ops, const int4* tab, long long nchunks, const int*
 void tb_tiles(int nite, int ui0, int ui1, int uj0, int uj1, int* ntx, int* nty);
 bool launch_btb(int stencil, int nite, const Op* ops, const int4* tab, long long ntiles, const int* active,
                 cudaStream_t s);
+// the same for the lean packed pass (OPK_TB Ops of form 5)
+void tb5_tiles(int nite, int ui0, int ui1, int uj0, int uj1, int* ntx, int* nty);
+bool launch_btb5(int stencil, int nite, const Op* ops, const int4* tab, long long ntiles, const int* active,
+                 cudaStream_t s);
 void launch_binit(const BInst* bi, int ninst, int zero_x, int* active, int* nactive, cudaStream_t s);
 void launch_bres(int kind, bool neumann, const BInst* bi, const int4* tab, long long nchunks, const int* active,
                  double* partials, cudaStream_t s);

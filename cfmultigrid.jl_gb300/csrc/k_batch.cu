@@ -558,6 +558,41 @@ __global__ void __launch_bounds__(kBThreads) k_bsmall(const BSmall* __restrict__
   }
 }
 
+// Coarse runs: block b executes run runs[b] = {instance, first entry, end
+// entry, 0} of the entry list, in order, with a block barrier after each
+// entry: ent = {0, Op index} runs the Op over its whole index space,
+// {1, BSmall index} a small-level smoothing in shared memory. Same per-item
+// code as k_bstage and k_bsmall, so the same values.
+__global__ void __launch_bounds__(kBRunThreads) k_brun(const Op* __restrict__ ops, const BSmall* __restrict__ sm,
+                                                       const int2* __restrict__ ent, const int4* __restrict__ runs,
+                                                       const int* __restrict__ active) {
+  dep_wait();
+  extern __shared__ double dsm[];
+  __shared__ Op op;
+  const int4 rn = runs[blockIdx.x];
+  if (!active[rn.x]) return;
+  for (int e = rn.y; e < rn.z; ++e) {
+    const int2 en = ent[e];
+    if (en.x == 1) {
+      const BSmall& s = sm[en.y];
+      const long long len = s.g.len;
+      if (s.prec == 0) {
+        bsmall_run<double>(s, dsm, dsm + len, dsm + 2 * len, dsm + 3 * len);
+      } else {
+        float* f = (float*)dsm;
+        bsmall_run<float>(s, f, f + len, f + 2 * len, f + 3 * len);
+      }
+    } else {
+      if (threadIdx.x < sizeof(Op) / sizeof(int)) ((int*)&op)[threadIdx.x] = ((const int*)&ops[en.y])[threadIdx.x];
+      __syncthreads();
+      if (op.prec == 0) exec<double, 2>(op, threadIdx.x, kBRunThreads, op.n);
+      else exec<float, 4>(op, threadIdx.x, kBRunThreads, op.n);
+    }
+    __syncthreads();  // the next entry reads this one's output (and rewrites op)
+  }
+}
+static_assert(sizeof(Op) / sizeof(int) <= kBRunThreads, "one thread per word of an Op");
+
 // the `while` condition: another iteration while any instance continues
 __global__ void k_bcond(cudaGraphConditionalHandle hc, int* nactive) {
   dep_wait();
@@ -655,6 +690,17 @@ void launch_bsmall(const BSmall* sm, int n, int smem, const int* active, cudaStr
     attr = true;
   }
   launch_dep(k_bsmall, n, kBThreads, smem, st, sm, active);
+}
+
+void launch_brun(const Op* ops, const BSmall* sm, const int2* ent, const int4* runs, int nruns, int smem,
+                 const int* active, cudaStream_t st) {
+  if (nruns <= 0) return;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_brun, cudaFuncAttributeMaxDynamicSharedMemorySize, kBSmallBytes);
+    attr = true;
+  }
+  launch_dep(k_brun, nruns, kBRunThreads, smem, st, ops, sm, ent, runs, active);
 }
 
 void launch_bcond(cudaGraphConditionalHandle hc, int* nactive, cudaStream_t s) {

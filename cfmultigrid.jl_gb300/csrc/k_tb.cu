@@ -435,14 +435,14 @@ __device__ __forceinline__ void tb5_resid(const float* __restrict__ src, float* 
 // solution update x += e * iscale to the core cells of U instead, with the
 // arithmetic of k_update_scaled_max, and collects max |x| of the results
 // into ds[S_MAXX]. Outside U e is +0, so those cells keep their value.
-template <int ST, int NITE, int TY, int ROWS, int MINB, bool EPI, bool PER = false, bool UPD = false>
-__global__ void __launch_bounds__(kT5Tx * TY, MINB) k_smooth_tb5(const float* __restrict__ x, float* __restrict__ xo,
-                                                                 const float* __restrict__ b,
-                                                                 const float* __restrict__ w, float cff, int tx,
-                                                                 int ty, int ui0, int ui1, int uj0, int uj1,
-                                                                 TbEpi ep) {
-  dep_wait();
-  extern __shared__ float smem[];
+//
+// One tile (bx, by) of layer bz per call: the standalone kernel takes its
+// block index, the batched one the tiles of its work table.
+template <int ST, int NITE, int TY, int ROWS, bool EPI, bool PER, bool UPD>
+__device__ __forceinline__ void tb5_tile(const float* __restrict__ x, float* __restrict__ xo,
+                                         const float* __restrict__ b, const float* __restrict__ w, float cff, int tx,
+                                         int ty, int ui0, int ui1, int uj0, int uj1, TbEpi ep, int bx, int by,
+                                         int bz, float* smem) {
   // with the epilogue the core is 2 cells narrower: r is needed one cell
   // beyond it, and x one cell beyond that
   constexpr int H = 2 * NITE + (EPI ? 2 : 0), TH = TY * ROWS;
@@ -454,11 +454,11 @@ __global__ void __launch_bounds__(kT5Tx * TY, MINB) k_smooth_tb5(const float* __
   ushort* Msm = reinterpret_cast<ushort*>(Dsm + TH * kT5Tx);
   const int lx = threadIdx.x;
   const int r0 = threadIdx.y * ROWS;  // first tile row of this thread
-  const int ti0 = ui0 + (int)blockIdx.x * CW - H, tj0 = uj0 + (int)blockIdx.y * CH - H;  // tile origin (1-based)
+  const int ti0 = ui0 + bx * CW - H, tj0 = uj0 + by * CH - H;  // tile origin (1-based)
   const int gi0 = ti0 + 2 * lx;  // global column of the even cell
   // linear index of the thread's even cell in its first row (may lie
   // outside the array for boundary tiles: used only under the bounds tests)
-  const long long I0 = (long long)tx * ty * blockIdx.z + (long long)(gi0 - 1) + (long long)tx * (tj0 + r0 - 1);
+  const long long I0 = (long long)tx * ty * bz + (long long)(gi0 - 1) + (long long)tx * (tj0 + r0 - 1);
   const bool cols_in = ti0 >= ui0 && ti0 + kT5W - 1 <= ui1, rows_in = tj0 >= uj0 && tj0 + TH - 1 <= uj1;
   const bool tile_in_u = rows_in && (PER || cols_in);  // periodic: every column is updated
   // the parity of I0 is the same for every thread of the tile
@@ -699,6 +699,18 @@ __global__ void __launch_bounds__(kT5Tx * TY, MINB) k_smooth_tb5(const float* __
   }
 }
 
+template <int ST, int NITE, int TY, int ROWS, int MINB, bool EPI, bool PER = false, bool UPD = false>
+__global__ void __launch_bounds__(kT5Tx * TY, MINB) k_smooth_tb5(const float* __restrict__ x, float* __restrict__ xo,
+                                                                 const float* __restrict__ b,
+                                                                 const float* __restrict__ w, float cff, int tx,
+                                                                 int ty, int ui0, int ui1, int uj0, int uj1,
+                                                                 TbEpi ep) {
+  dep_wait();
+  extern __shared__ float smem[];
+  tb5_tile<ST, NITE, TY, ROWS, EPI, PER, UPD>(x, xo, b, w, cff, tx, ty, ui0, ui1, uj0, uj1, ep, (int)blockIdx.x,
+                                              (int)blockIdx.y, (int)blockIdx.z, smem);
+}
+
 template <int ST, int NITE>
 __global__ void __launch_bounds__(kTbW * kTbTy, 1) k_smooth_tb(const float* __restrict__ x, float* __restrict__ xo,
                                                                const float* __restrict__ b,
@@ -755,6 +767,56 @@ __global__ void __launch_bounds__(kTbW * kTbTy, 1) k_btb(const Op* __restrict__ 
       tb_tile<ST, NITE>((const float*)op.x, (float*)op.y, (const float*)op.b, (const float*)op.w, (float)op.cff,
                         op.g.tx, op.g.ty, op.box.i0, op.box.i1, op.box.j0, op.box.j1, rem % op.kf0, rem / op.kf0, bz,
                         smem);
+      __syncthreads();
+    }
+    __syncthreads();  // list is rewritten by the next window
+  }
+}
+
+// Batched form of the lean packed pass (8 x 6 rows a tile, as the
+// standalone pass): the same windowed walk over a tile table as k_btb, each
+// active tile run by tb5_tile; the barrier after a tile keeps the next
+// tile's loads behind this tile's last shared-memory reads.
+template <int ST, int NITE>
+__global__ void __launch_bounds__(kT5Tx * 8, 2) k_btb5(const Op* __restrict__ ops, const int4* __restrict__ tab,
+                                                       long long ntiles, int win, const int* __restrict__ active) {
+  dep_wait();
+  extern __shared__ float smem[];
+  constexpr int nt = kT5Tx * 8;
+  __shared__ int list[nt];
+  __shared__ int wsum[nt / 32 + 1];
+  const int tid = threadIdx.y * kT5Tx + threadIdx.x;
+  for (long long base = (long long)blockIdx.x * win; base < ntiles; base += (long long)gridDim.x * win) {
+    const long long c = base + tid;
+    bool ok = false;
+    if (tid < win && c < ntiles) ok = active[tab[c].z] != 0;
+    const unsigned bal = __ballot_sync(0xffffffffu, ok);
+    const int lane = tid & 31, wid = tid >> 5;
+    if (lane == 0) wsum[wid] = __popc(bal);
+    __syncthreads();
+    if (tid == 0) {
+      int a = 0;
+      for (int w = 0; w < nt / 32; ++w) {
+        const int v = wsum[w];
+        wsum[w] = a;
+        a += v;
+      }
+      wsum[nt / 32] = a;
+    }
+    __syncthreads();
+    if (ok) list[wsum[wid] + __popc(bal & ((1u << lane) - 1u))] = tid;
+    __syncthreads();
+    const int cnt = wsum[nt / 32];
+    for (int q = 0; q < cnt; ++q) {
+      const int4 en = tab[base + list[q]];
+      const Op& op = ops[en.x];
+      const long long per_layer = (long long)op.kf0 * op.kf1;
+      const int bz = (int)(en.y / per_layer);
+      const int rem = (int)(en.y - (long long)bz * per_layer);
+      tb5_tile<ST, NITE, 8, 6, false, false, false>((const float*)op.x, (float*)op.y, (const float*)op.b,
+                                                    (const float*)op.w, (float)op.cff, op.g.tx, op.g.ty, op.box.i0,
+                                                    op.box.i1, op.box.j0, op.box.j1, TbEpi{}, rem % op.kf0,
+                                                    rem / op.kf0, bz, smem);
       __syncthreads();
     }
     __syncthreads();  // list is rewritten by the next window
@@ -884,6 +946,48 @@ void tb_tiles(int nite, int ui0, int ui1, int uj0, int uj1, int* ntx, int* nty) 
   const int H = 2 * nite, CW = kTbW - 2 * H, CH = kTbH - 2 * H;
   *ntx = (ui1 - ui0 + CW) / CW;
   *nty = (uj1 - uj0 + CH) / CH;
+}
+
+// tile counts of one lean packed pass (8 x 6 rows) over the box U
+void tb5_tiles(int nite, int ui0, int ui1, int uj0, int uj1, int* ntx, int* nty) {
+  const int H = 2 * nite, CW = kT5W - 2 * H, CH = 8 * 6 - 2 * H;
+  *ntx = (ui1 - ui0 + CW) / CW;
+  *nty = (uj1 - uj0 + CH) / CH;
+}
+
+template <int ST, int NITE>
+static void launch_btb5_n(const Op* ops, const int4* tab, long long ntiles, const int* active, cudaStream_t s) {
+  const size_t smem = 2 * (size_t)t5_plane<8, 6>() * sizeof(float);
+  static bool attr = false;
+  static int nsm = 0;
+  if (!attr) {
+    cudaFuncSetAttribute(k_btb5<ST, NITE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    attr = true;
+  }
+  // two resident CTAs per SM, each taking windows of `win` tiles
+  const long long g = 2LL * nsm;
+  long long win = (ntiles + g - 1) / g;
+  if (win > kT5Tx * 8) win = kT5Tx * 8;
+  const long long windows = (ntiles + win - 1) / win;
+  const long long grid = windows < g ? windows : g;
+  launch_dep(k_btb5<ST, NITE>, (unsigned)grid, dim3(kT5Tx, 8, 1), smem, s, ops, tab, ntiles, (int)win, active);
+}
+
+bool launch_btb5(int stencil, int nite, const Op* ops, const int4* tab, long long ntiles, const int* active,
+                 cudaStream_t s) {
+  if (ntiles <= 0) return true;
+#define CFMG_BTB5(ST, N)                                             \
+  if (stencil == ST && nite == N) {                                  \
+    launch_btb5_n<ST, N>(ops, tab, ntiles, active, s);               \
+    return true;                                                     \
+  }
+  CFMG_BTB5(5, 1) CFMG_BTB5(5, 2) CFMG_BTB5(5, 3)
+  CFMG_BTB5(9, 1) CFMG_BTB5(9, 2) CFMG_BTB5(9, 3)
+#undef CFMG_BTB5
+  return false;
 }
 
 template <int ST, int NITE>

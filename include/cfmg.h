@@ -271,6 +271,13 @@ CFMG_API int cfmg_adjoint_solve(cfmg_handle* h, const double* cot, double* grad_
  * lockstep iteration instead of the `while` node (the same kernels; for
  * profilers that do not descend into conditional graph nodes). */
 #define CFMG_BOPT_HOST_LOOP 0
+/* cfmg_batch_set_option(b, CFMG_BOPT_COARSE_RUNS, 0/1): with 1 (default) the
+ * steps of an iteration on an instance's coarse levels (those its engine
+ * threshold, CFMG_OPT_ENGINE_CELLS, would put in the program engine) run as
+ * one block per instance, a run of consecutive steps per launch, instead of
+ * one launch per step; 0 launches every step for all instances. Same
+ * values either way. */
+#define CFMG_BOPT_COARSE_RUNS 1
 typedef struct cfmg_batch cfmg_batch;
 CFMG_API int cfmg_batch_create(const cfmg_desc* d, int ninst, const int* nx, const int* ny, const int* nlevels,
                                cfmg_batch** out);

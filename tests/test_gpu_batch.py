@@ -174,3 +174,38 @@ def test_batch_against_oracle(cycle):
         assert np.linalg.norm(a - c) <= 1e-6 * np.linalg.norm(c), (i, np.linalg.norm(a - c) / np.linalg.norm(c))
     assert converged >= 12, converged
     assert len(kinds) == 2
+
+
+@pytest.mark.parametrize("cycle,location,hi", [("f", "centers", 512), ("v", "centers", 512), ("f", "centers", 128),
+                                                ("f", "vertices", 320)])
+def test_batch_launch_forms_are_bit_identical(cycle, location, hi):
+    """Three launch forms of the same batched iteration give the same bits:
+    the default (coarse levels' steps as one block per instance and run of
+    steps, CFMG_BOPT_COARSE_RUNS = 1; fine levels' blocked smoothing in the
+    lean packed tiles, k_btb5), one launch per coarse step for all instances
+    (coarse_runs 0), and the scalar blocked tiles (k_btb, the instances'
+    temporal_blocking 3). Each executes the same per-item arithmetic, so the
+    residuals, cycle counts and solutions agree exactly. hi = 128: every
+    level of every instance is coarse (the whole cycle runs in runs)."""
+    probs = W.config4(ninst=12, seed=7, lo=64, hi=hi)
+    op = "laplacian9" if location == "vertices" else "laplacian"
+    p = _param(cycle=cycle, location=location, operator=op, maxite=60)
+    out = []
+    for runs, tb in ((1, 5), (0, 5), (1, 3)):
+        batch = cfmg.Batch(p, [q[0] for q in probs], [q[0] for q in probs], [q[1] for q in probs])
+        batch.set_option("coarse_runs", runs)
+        for i, (n, nlev, msk, noise) in enumerate(probs):
+            if location == "vertices":
+                msk = F.get_mask_at_corners(msk)
+            batch.instance(i).set_option("temporal_blocking", tb)
+            _setup(batch.instance(i), msk, noise)
+        res, nite, _ = batch.solve()
+        xs = [batch.instance(i).data[1].x.copy() for i in range(len(probs))]
+        out.append((res, nite, xs))
+        batch.close()
+    r1, n1, x1 = out[0]
+    for k, (r0, n0, x0) in enumerate(out[1:]):
+        assert np.array_equal(n1, n0) and np.array_equal(r1, r0), (k, n1, n0, r1, r0)
+        for i in range(len(probs)):
+            assert np.array_equal(x1[i], x0[i]), (k, i)
+    assert np.all(n1 >= 1) and np.sum(r1 <= 1e-10) >= 3, (n1, r1)
