@@ -39,7 +39,7 @@ EXPORTS = (
 OPTIONS = {"engine_cells": 0, "temporal_blocking": 1, "coarsest_fp64": 2, "int_residual": 3, "host_loop": 4,
            "fused_descent": 5, "fused_update": 6, "dependent_launch": 7,
            "coded_widiag": 8, "staged_residual": 9, "skip_dry": 10, "small_smooth": 11}
-BATCH_OPTIONS = {"host_loop": 0, "coarse_runs": 1}
+BATCH_OPTIONS = {"host_loop": 0, "coarse_runs": 1, "interleave": 2}
 KERNEL_CLASSES = {"sweep": 0, "residual": 1, "restrict": 2, "prolong": 3, "norm": 4, "fill": 5, "convert": 6,
                   "engine": 7,
                   "descent": 8}

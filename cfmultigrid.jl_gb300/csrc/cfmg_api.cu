@@ -133,6 +133,7 @@ struct cfmg_batch {
   int4* runs = nullptr;        // coarse runs {instance, first entry, end entry, 0} (device)
   bool host_loop = false;      // CFMG_BOPT_HOST_LOOP
   bool coarse_runs = true;     // CFMG_BOPT_COARSE_RUNS
+  bool interleave = true;      // CFMG_BOPT_INTERLEAVE
   bool int_all = false;        // every instance has the integer residual form
   int4* ttab = nullptr;        // its warp tasks {instance, strip, row chunk, 0}
   long long* tstart = nullptr; // first task of each instance (ninst + 1)
@@ -2456,11 +2457,21 @@ int lockstep_build(cfmg_batch* b) {
     cfmg_batch::Step st;
     st.tb = tb; st.stencil = stencil; st.nite = nite; st.smem = 0;
     st.tab0 = (long long)tab.size();
-    for (const Op& op : ops) {
-      const int o = (int)all.size();
-      all.push_back(op);
-      const long long nc = tb ? op.n : (op.n + kBChunk - 1) / kBChunk;
-      for (long long c = 0; c < nc; ++c) tab.push_back(make_int4(o, (int)c, op.inst, 0));
+    std::vector<long long> nc(ops.size());
+    long long mx = 0;
+    const int o0 = (int)all.size();
+    for (size_t j = 0; j < ops.size(); ++j) {
+      all.push_back(ops[j]);
+      nc[j] = tb ? ops[j].n : (ops[j].n + kBStageChunk - 1) / kBStageChunk;
+      mx = std::max(mx, nc[j]);
+    }
+    if (b->interleave) {  // chunk c of every Op, then chunk c + 1, ...
+      for (long long c = 0; c < mx; ++c)
+        for (size_t j = 0; j < ops.size(); ++j)
+          if (c < nc[j]) tab.push_back(make_int4(o0 + (int)j, (int)c, ops[j].inst, 0));
+    } else {
+      for (size_t j = 0; j < ops.size(); ++j)
+        for (long long c = 0; c < nc[j]; ++c) tab.push_back(make_int4(o0 + (int)j, (int)c, ops[j].inst, 0));
     }
     st.nchunks = (long long)tab.size() - st.tab0;
     b->steps.push_back(st);
@@ -2601,9 +2612,19 @@ int lockstep_build(cfmg_batch* b) {
     BCUDA(b, cudaMalloc((void**)&b->tstart, sizeof(long long) * ts.size()));
     BCUDA(b, cudaMemcpy(b->tstart, ts.data(), sizeof(long long) * ts.size(), cudaMemcpyHostToDevice));
   }
-  std::vector<int4> l1t((size_t)b->l1chunks);
-  for (int i = 0; i < ninst; ++i)
-    for (long long c = l1[i]; c < l1[i + 1]; ++c) l1t[c] = make_int4(i, (int)(c - l1[i]), i, 0);
+  // {instance, chunk, instance, partial slot}; interleaved like the steps' tables
+  std::vector<int4> l1t;
+  l1t.reserve((size_t)b->l1chunks);
+  if (b->interleave) {
+    long long mx = 0;
+    for (int i = 0; i < ninst; ++i) mx = std::max(mx, l1[i + 1] - l1[i]);
+    for (long long c = 0; c < mx; ++c)
+      for (int i = 0; i < ninst; ++i)
+        if (c < l1[i + 1] - l1[i]) l1t.push_back(make_int4(i, (int)c, i, (int)(l1[i] + c)));
+  } else {
+    for (int i = 0; i < ninst; ++i)
+      for (long long c = l1[i]; c < l1[i + 1]; ++c) l1t.push_back(make_int4(i, (int)(c - l1[i]), i, (int)c));
+  }
   BCUDA(b, cudaMalloc((void**)&b->l1tab, sizeof(int4) * l1t.size()));
   BCUDA(b, cudaMemcpy(b->l1tab, l1t.data(), sizeof(int4) * l1t.size(), cudaMemcpyHostToDevice));
   BCUDA(b, cudaMalloc((void**)&b->bi, sizeof(BInst) * ninst));
@@ -2747,6 +2768,11 @@ int cfmg_batch_set_option(cfmg_batch* b, int option, long long value) {
   if (option == CFMG_BOPT_COARSE_RUNS) {
     if (b->coarse_runs != (value != 0)) b->built = false;  // the iteration's launches change
     b->coarse_runs = value != 0;
+    return CFMG_OK;
+  }
+  if (option == CFMG_BOPT_INTERLEAVE) {
+    if (b->interleave != (value != 0)) b->built = false;  // the work tables change
+    b->interleave = value != 0;
     return CFMG_OK;
   }
   return bfail(b, CFMG_ERR_ARG, "unknown batch option");

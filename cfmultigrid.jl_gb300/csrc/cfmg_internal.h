@@ -305,6 +305,7 @@ bool launch_smooth_tb_upd(int stencil, int nite, const float* x, const float* b,
 // Ops; a chunk of an instance that has converged is skipped.
 constexpr int kBChunk = 1024;
 constexpr int kBThreads = 256;
+constexpr int kBStageChunk = 8192;  // items of one entry of a generic step's table (k_bstage)
 // per-instance scalar block (double): see k_bfinal for their use
 enum BSlot { BS_NORMB = 0, BS_RES, BS_NITE, BS_NWET, BS_NEXT, BS_CUR, BS_ICUR, BS_MEAN, BS_T0, BS_T1, BS_ZEROX,
              BS_MAXX, BS_MAXB, BS_SHIFT, BS_HIST };

@@ -85,9 +85,10 @@ __device__ __forceinline__ double bmax(double v, double* sh) {
 }
 
 // ------------------------------------------------------------ cycle steps
-// Generic step: the active chunks of a list of Ops (tab[c] = {op, chunk of
-// the op, instance}), each executed with the per-item code of the program
-// engine, 4 (FP32) or 2 (FP64) items per thread in flight.
+// Generic step: the active chunks (kBStageChunk items) of a list of Ops
+// (tab[c] = {op, chunk of the op, instance}), each executed with the
+// per-item code of the program engine, 4 (FP32) or 2 (FP64) items per
+// thread in flight.
 __global__ void __launch_bounds__(kBThreads, 2) k_bstage(const Op* __restrict__ ops, const int4* __restrict__ tab,
                                                          long long nchunks, int win, const int* __restrict__ active) {
   dep_wait();
@@ -105,8 +106,8 @@ __global__ void __launch_bounds__(kBThreads, 2) k_bstage(const Op* __restrict__ 
         __syncthreads();
         cur = en.x;
       }
-      const long long t0 = (long long)en.y * kBChunk;
-      const long long e = t0 + kBChunk < op.n ? t0 + kBChunk : op.n;
+      const long long t0 = (long long)en.y * kBStageChunk;
+      const long long e = t0 + kBStageChunk < op.n ? t0 + kBStageChunk : op.n;
       if (op.prec == 0) exec<double, 2>(op, t0 + threadIdx.x, kBThreads, e);
       else exec<float, 4>(op, t0 + threadIdx.x, kBThreads, e);
     }
@@ -156,10 +157,11 @@ __global__ void __launch_bounds__(kBThreads) k_binit(const BInst* __restrict__ b
 }
 
 // Fused FP64 residual over the active level-1 chunks (tab[c] = {instance,
-// chunk of its level 1, instance}): r = b - A x per cell (the residual
-// operator's arithmetic), the chunk's sum r^2 and sum r to partials[2c],
-// partials[2c+1], and the scaled FP32 right-hand side (vertex-centred) or
-// the FP64 r (cell-centred, for the mean-removing pass).
+// chunk of its level 1, instance, slot}): r = b - A x per cell (the
+// residual operator's arithmetic), the chunk's sum r^2 and sum r to
+// partials[2 slot], partials[2 slot + 1], and the scaled FP32 right-hand
+// side (vertex-centred) or the FP64 r (cell-centred, for the mean-removing
+// pass).
 template <int KIND, bool NEUMANN>
 __global__ void __launch_bounds__(kBThreads) k_bres(const BInst* __restrict__ bi, const int4* __restrict__ tab,
                                                     long long nchunks, int win, const int* __restrict__ active,
@@ -172,8 +174,8 @@ __global__ void __launch_bounds__(kBThreads) k_bres(const BInst* __restrict__ bi
   for (long long base = (long long)blockIdx.x * win; base < nchunks; base += (long long)gridDim.x * win) {
     const int cnt = active_window(tab, base, nchunks, win, active, list, wsum);
     for (int q = 0; q < cnt; ++q) {
-      const long long c = base + list[q];
-      const int4 en = tab[c];
+      const int4 en = tab[base + list[q]];
+      const long long c = en.w;  // the chunk's partial-sum slot (its instance's chunks are consecutive slots)
       const BInst& B = bi[en.x];
       const double scale = B.sc[BS_NEXT];
       const long long t0 = (long long)en.y * kBChunk;

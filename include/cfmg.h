@@ -278,6 +278,13 @@ CFMG_API int cfmg_adjoint_solve(cfmg_handle* h, const double* cot, double* grad_
  * one launch per step; 0 launches every step for all instances. Same
  * values either way. */
 #define CFMG_BOPT_COARSE_RUNS 1
+/* cfmg_batch_set_option(b, CFMG_BOPT_INTERLEAVE, 0/1): with 1 (default) the
+ * work tables of the lockstep launches list chunk (or tile) c of every
+ * instance before chunk c + 1 of any, so that the chunks of one instance
+ * fall to different blocks and the few instances still iterating late in a
+ * batch are spread over the whole GPU; 0 lists each instance's chunks
+ * together. Same values either way. */
+#define CFMG_BOPT_INTERLEAVE 2
 typedef struct cfmg_batch cfmg_batch;
 CFMG_API int cfmg_batch_create(const cfmg_desc* d, int ninst, const int* nx, const int* ny, const int* nlevels,
                                cfmg_batch** out);

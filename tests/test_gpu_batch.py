@@ -176,28 +176,36 @@ def test_batch_against_oracle(cycle):
     assert len(kinds) == 2
 
 
-@pytest.mark.parametrize("cycle,location,hi", [("f", "centers", 512), ("v", "centers", 512), ("f", "centers", 128),
-                                                ("f", "vertices", 320)])
-def test_batch_launch_forms_are_bit_identical(cycle, location, hi):
-    """Three launch forms of the same batched iteration give the same bits:
+@pytest.mark.parametrize("cycle,location,hi,int_res", [("f", "centers", 512, 1), ("v", "centers", 512, 1),
+                                                        ("f", "centers", 128, 1), ("f", "vertices", 320, 1),
+                                                        ("f", "centers", 320, 0)])
+def test_batch_launch_forms_are_bit_identical(cycle, location, hi, int_res):
+    """Four launch forms of the same batched iteration give the same bits:
     the default (coarse levels' steps as one block per instance and run of
     steps, CFMG_BOPT_COARSE_RUNS = 1; fine levels' blocked smoothing in the
-    lean packed tiles, k_btb5), one launch per coarse step for all instances
-    (coarse_runs 0), and the scalar blocked tiles (k_btb, the instances'
-    temporal_blocking 3). Each executes the same per-item arithmetic, so the
-    residuals, cycle counts and solutions agree exactly. hi = 128: every
-    level of every instance is coarse (the whole cycle runs in runs)."""
+    lean packed tiles, k_btb5; work tables interleaved across instances,
+    CFMG_BOPT_INTERLEAVE = 1), one launch per coarse step for all instances
+    (coarse_runs 0), the scalar blocked tiles (k_btb, the instances'
+    temporal_blocking 3), and each instance's chunks listed together
+    (interleave 0: the level-1 residual's partial sums keep their slots).
+    Each executes the same per-item arithmetic and sums, so the residuals,
+    cycle counts and solutions agree exactly. hi = 128: every level of every
+    instance is coarse (the whole cycle runs in runs). int_res 0: the FP64
+    form of the level-1 residual, whose per-chunk partial sums the
+    interleaved table writes to their instance-ordered slots."""
     probs = W.config4(ninst=12, seed=7, lo=64, hi=hi)
     op = "laplacian9" if location == "vertices" else "laplacian"
     p = _param(cycle=cycle, location=location, operator=op, maxite=60)
     out = []
-    for runs, tb in ((1, 5), (0, 5), (1, 3)):
+    for runs, tb, inter in ((1, 5, 1), (0, 5, 1), (1, 3, 1), (1, 5, 0)):
         batch = cfmg.Batch(p, [q[0] for q in probs], [q[0] for q in probs], [q[1] for q in probs])
         batch.set_option("coarse_runs", runs)
+        batch.set_option("interleave", inter)
         for i, (n, nlev, msk, noise) in enumerate(probs):
             if location == "vertices":
                 msk = F.get_mask_at_corners(msk)
             batch.instance(i).set_option("temporal_blocking", tb)
+            batch.instance(i).set_option("int_residual", int_res)
             _setup(batch.instance(i), msk, noise)
         res, nite, _ = batch.solve()
         xs = [batch.instance(i).data[1].x.copy() for i in range(len(probs))]
