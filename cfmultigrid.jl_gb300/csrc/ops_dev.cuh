@@ -308,13 +308,26 @@ __device__ __forceinline__ void d_prolong(T* xf, const T* x, const T* coef, cons
     const int k = kf0 + qk;
     const long long C = lin(gc, ic, jc, k), F = lin(gf, i, j, k);
     const T x9 = A::mul(x[C], T(9));
+    // every load of the four children before the first store, so that they
+    // are in flight together (the compiler cannot move a load of one child
+    // above the store of another: the arrays might alias)
+    T bb[4], cf[4], xo[4];
 #pragma unroll
     for (int dj = 0; dj <= 1; ++dj)
 #pragma unroll
       for (int di = 0; di <= 1; ++di) {
-        T bb = square3(x, C, (long long)(2 * di - 1), (2 * dj - 1) * c1, 0LL);
-        long long Fi = F + di + dj * f1;
-        xf[Fi] = A::add(ASSIGN ? T(0) : xf[Fi], A::mul(coef[Fi], A::add(bb, x9)));
+        const int c = 2 * dj + di;
+        const long long Fi = F + di + dj * f1;
+        bb[c] = square3(x, C, (long long)(2 * di - 1), (2 * dj - 1) * c1, 0LL);
+        cf[c] = coef[Fi];
+        xo[c] = ASSIGN ? T(0) : xf[Fi];
+      }
+#pragma unroll
+    for (int dj = 0; dj <= 1; ++dj)
+#pragma unroll
+      for (int di = 0; di <= 1; ++di) {
+        const int c = 2 * dj + di;
+        xf[F + di + dj * f1] = A::add(xo[c], A::mul(cf[c], A::add(bb[c], x9)));
       }
   } else if (KIND == 1) {
     const int k = nh + 1 + 2 * qk;
@@ -337,11 +350,17 @@ __device__ __forceinline__ void d_prolong(T* xf, const T* x, const T* coef, cons
     const int k = kf0 + qk;
     const long long C = lin(gc, ic, jc, k), F = lin(gf, i, j, k);
     const T x00 = x[C], x10 = x[C + 1], x01 = x[C + c1], x11 = x[C + 1 + c1];
-    xf[F] = A::add(ASSIGN ? T(0) : xf[F], A::mul(coef[F], x00));
-    xf[F + 1] = A::add(ASSIGN ? T(0) : xf[F + 1], A::mul(coef[F + 1], A::add(x00, x10)));
-    xf[F + f1] = A::add(ASSIGN ? T(0) : xf[F + f1], A::mul(coef[F + f1], A::add(x00, x01)));
-    xf[F + 1 + f1] =
-        A::add(ASSIGN ? T(0) : xf[F + 1 + f1], A::mul(coef[F + 1 + f1], A::add(A::add(A::add(x00, x10), x01), x11)));
+    const long long o[4] = {0, 1, f1, 1 + f1};
+    T cf[4], xo[4];  // loads of the four children first, as in KIND 0
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      cf[c] = coef[F + o[c]];
+      xo[c] = ASSIGN ? T(0) : xf[F + o[c]];
+    }
+    xf[F] = A::add(xo[0], A::mul(cf[0], x00));
+    xf[F + 1] = A::add(xo[1], A::mul(cf[1], A::add(x00, x10)));
+    xf[F + f1] = A::add(xo[2], A::mul(cf[2], A::add(x00, x01)));
+    xf[F + 1 + f1] = A::add(xo[3], A::mul(cf[3], A::add(A::add(A::add(x00, x10), x01), x11)));
   } else {
     const int k = nh + 1 + 2 * qk;
     const int kc = f2c(k, nh);
