@@ -759,9 +759,10 @@ def bench_config3(args, local, sub=False):
 def bench_config4(args, local, sub=False):
     """Configuration 4: 2048 independent 2D cell-centred 5-point masked
     solves (sizes log-uniform 64^2..1024^2, disk or noise masks) to 1e-10 in
-    one graph launch of the batched solver; the schedule is picked by the
-    autotuner on a stratified sample. Reports the batch time and the p50/p99
-    of the per-instance completion time (device clock)."""
+    one graph launch of the batched solver; the schedule and the tile form of
+    the blocked passes are picked by the autotuner on a stratified sample.
+    Reports the batch time and the p50/p99 of the per-instance completion
+    time (device clock)."""
     import numpy as np
     import torch
 
@@ -804,6 +805,7 @@ def bench_config4(args, local, sub=False):
     t_tune = time.perf_counter() - t0
     t0 = time.perf_counter()
     batch = make(p, list(range(len(probs))))
+    autotune.apply_form(batch, report.get("form", autotune.DEFAULT_FORM))
     if args.host_loop and not sub:
         batch.set_option("host_loop", 1)
     t_setup = time.perf_counter() - t0
@@ -828,6 +830,7 @@ def bench_config4(args, local, sub=False):
             "dtype": "f32-in-f64", "data": "synthetic (seeded sizes, disk/noise masks, N(0,1) rhs)",
             "config": {"workload": "config4: batched 2D cell-centred 5-point, sizes log-uniform 64^2..1024^2",
                        "instances": len(probs), "fine_cells": cells, "schedule": dataclasses_asdict(p),
+                       "tile_form": report.get("form", autotune.DEFAULT_FORM),
                        "autotune": report, "tune_s": t_tune, "setup_s": t_setup, "inputs_s": t_gen,
                        "timing": "host wall clock around each one-launch batch solve (it returns after the "
                                  "device finished)"},

@@ -477,7 +477,11 @@ class Batch:
 
     def set_option(self, name: str, value: int) -> None:
         """Batch options: "host_loop" (1: the host repeats the lockstep
-        iteration instead of the graph's while node; for profilers)."""
+        iteration instead of the graph's while node; for profilers),
+        "coarse_runs" (1, default: each instance's coarse-level steps run as
+        one block per run of steps; 0: a launch per step), "interleave" (1,
+        default: work tables list chunk c of every instance before chunk
+        c + 1; 0: each instance's chunks together). Same values either way."""
         self._check(self._L.cfmg_batch_set_option(self._b, _lib.BATCH_OPTIONS[name], int(value)))
 
     def close(self):
