@@ -65,9 +65,11 @@ def _defines(prefix):
 
 
 def test_option_and_class_tables_match_header():
-    """The Python names of the option and kernel-class codes are the
-    header's #define values (a mismatch would set the wrong knob)."""
+    """The Python names of the option, batch-option and kernel-class codes
+    are the header's #define values (a mismatch would set the wrong knob)."""
     opts = _defines("CFMG_OPT_")
     assert {("CFMG_OPT_" + k.upper()): v for k, v in _lib.OPTIONS.items()} == opts
     classes = _defines("CFMG_K_")
     assert {("CFMG_K_" + k.upper()): v for k, v in _lib.KERNEL_CLASSES.items()} == classes
+    bopts = _defines("CFMG_BOPT_")
+    assert {("CFMG_BOPT_" + k.upper()): v for k, v in _lib.BATCH_OPTIONS.items()} == bopts
